@@ -1,0 +1,390 @@
+"""nova-gb300 benchmark: PBVI belief-backups/s on one GB300 per rank.
+
+Workload (default `pbvi_n4096`): seeded random sparse POMDP with n=4096
+states, m=16 actions, z=32 observations, ns=32 successors per (s, a),
+r=8192 beliefs with rz=64 support states, gamma=0.95 (nova's PBVI update,
+|Gamma| = r). A step is one PBVI backup of every belief
+(pomdp_pbvi_update_gpu); the metric is beliefs backed up per second.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config NAME]
+
+Our arm prints one JSON line with: value (device-resident, tensor-core
+scoring), the plain FP32 exact-scoring form on the same state, e2e through
+the host-buffer entry point pomdp_pbvi_update_cpu (host<->device copies
+inside the timed region), the roofline of the scoring kernel, the CPU
+baseline (the oracle's port of nova's CPU loop, timed on a bounded sample on
+this host's cores), clocks sampled during the timed region, and the MDP
+Bellman sweep on n=2^20. The reference arm (--impl reference) times nova's
+CPU algorithm on this host's cores (the oracle port; nova's own CPU sources
+are not present on the GPU host) on the same workload.
+
+Multi-GPU: every rank runs an independent replica of the workload (PBVI
+beliefs of one POMDP need the full alpha set each step, and this build has
+no collective); value is the sum over ranks of beliefs backed up divided by
+the maximum time over ranks.
+"""
+import argparse
+import ctypes as ct
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "PBVI belief-backups/s at n=4096: BF16-TC vs plain FP32, |ΔV(b0)|≤1e-4 vs FP64"
+UNIT = "belief-backups/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="pbvi_n4096")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-mdp", action="store_true")
+    return ap.parse_args()
+
+
+def workload(args):
+    from nova_gb300 import synth
+    cfg = dict(synth.POMDP_CONFIGS[args.config])
+    return synth.random_pomdp(**cfg, seed=args.seed), cfg
+
+
+def workload_name(cfg, args):
+    return "%s (n=%d,m=%d,z=%d,ns=%d,r=%d,rz=%d,gamma=%g,seed=%d)" % (
+        args.config, cfg["n"], cfg["m"], cfg["z"], cfg["ns"], cfg["r"], cfg["rz"], cfg["gamma"], args.seed)
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_sample(model, Gamma, seconds, threads):
+    """Time nova's loop-form backup (the oracle port) on (belief, action)
+    pairs against the full alpha set, on `threads` host threads, for about
+    `seconds`. Returns (belief-backups/s, pairs done, wall seconds)."""
+    from oracle import oracle as orc
+    run = orc.pbvi_belief_action_sampler(model, Gamma)
+    m = model["m"]
+    lock = threading.Lock()
+    counter = [0]
+    done = [0]
+    deadline = [None]
+
+    def worker():
+        while True:
+            with lock:
+                k = counter[0]
+                if deadline[0] is not None and time.perf_counter() > deadline[0]:
+                    return
+                counter[0] += 1
+            i, a = (k // m) % model["r"], k % m
+            run(i, a)
+            with lock:
+                done[0] += 1
+
+    t0 = time.perf_counter()
+    deadline[0] = t0 + seconds
+    ts = [threading.Thread(target=worker) for _ in range(threads)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    wall = time.perf_counter() - t0
+    return done[0] / m / wall, done[0], wall
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.reader = threading.Thread(target=self._read, daemon=True)
+            self.reader.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.reader.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for nme, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nme)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d["hbm_gbs"], d["bf16_tflops"], "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    model, cfg = workload(args)
+    cores = host_cores()
+    per_step = max(1.0, args.cpu_seconds / 3.0)
+    for _ in range(args.warmup):
+        cpu_sample(model, model["GammaInitial"], min(per_step, 2.0), cores)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, pairs, wall = cpu_sample(model, model["GammaInitial"], per_step, cores)
+        vals.append((v, pairs, wall))
+    total = time.perf_counter() - t0
+    pairs = sum(p for _, p, _ in vals)
+    value = pairs / model["m"] / sum(w for _, _, w in vals)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / max(1, args.steps),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload_name(cfg, args), "parallelism": "host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "per step: (belief, action) pairs of nova's loop-form backup against the full "
+                                   "alpha set (r=%d) for %.1f s on %d threads; %d pairs in total"
+                                   % (cfg["r"], per_step, cores, pairs)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_mdp(args, dist_rank):
+    """Bellman sweep n=2^20, m=8, ns=16 (HBM-bound): GB/s of algorithmic bytes."""
+    import torch
+    from nova_gb300 import synth
+    from nova_gb300.mdp import MDP
+    from nova_gb300.mdp_vi import MDPValueIterationGPU
+    from nova_gb300 import nova_mdp_vi as nmvi
+    cfg = synth.MDP_CONFIGS["vi_n1m"]
+    md = synth.random_mdp(n=cfg["n"], m=cfg["m"], ns=cfg["ns"], gamma=cfg["gamma"], horizon=cfg["horizon"],
+                          seed=args.seed)
+    m = MDP.from_arrays(md)
+    m.initialize_gpu()
+    vi = MDPValueIterationGPU(m, Vinitial=np.zeros(md["n"], np.float32))
+    f = nmvi._nova
+    for _ in range(5):
+        f.mdp_vi_update_gpu(vi.mdpPtr, vi)
+    sweeps = 50
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(sweeps):
+        f.mdp_vi_update_gpu(vi.mdpPtr, vi)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / sweeps
+    n, mm, ns = md["n"], md["m"], md["ns"]
+    alg_bytes = 2 * n * mm * ns * 4 + n * mm * 4 + 3 * n * 4
+    hbm, _, _ = measured_peaks()
+    gbs = alg_bytes / (ms * 1e-3) / 1e9
+    pol, nsweeps, resid = MDPValueIterationGPU(m, Vinitial=np.zeros(md["n"], np.float32)).solve_until_converged(
+        tol=1e-6, maxSweeps=cfg["horizon"])
+    return {"workload": "vi_n1m (n=2^20,m=8,ns=16,gamma=0.99)", "ms_per_sweep": ms, "GB_per_s": gbs,
+            "algorithmic_bytes_per_sweep": alg_bytes, "frac_of_hbm": gbs / hbm,
+            "note": "per-sweep time includes the launch and synchronisation of mdp_vi_update_gpu",
+            "converged_sweeps": nsweeps, "final_residual_fp64": resid, "converged": bool(resid < 1e-6)}
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from nova_gb300 import nova_pomdp_pbvi as npp
+    from nova_gb300.pomdp import POMDP
+    from nova_gb300.pomdp_pbvi import POMDPPBVIGPU, POMDPPBVICPU
+    lib = npp._nova
+
+    model, cfg = workload(args)
+    p = POMDP.from_arrays(model)
+    p.initialize_gpu()
+    alg = POMDPPBVIGPU(p, GammaInitial=model["GammaInitial"])
+    alg.set_scoring(npp.SCORING_BF16)
+
+    for _ in range(args.warmup):
+        alg.update()
+    torch.cuda.synchronize()
+
+    # ---- timed region: K backups, device-resident inputs --------------------
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stats = []
+    launches0 = lib.nova_gb300_kernel_launches()
+    with ClockSampler(local_rank) as clocks:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            alg.update()
+            stats.append(alg.stats())
+        e1.record()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    launches = lib.nova_gb300_kernel_launches() - launches0
+    ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    r = cfg["r"]
+    value = world * r * args.steps / (ms * 1e-3)
+
+    # ---- roofline of the scoring kernel --------------------------------------
+    hbm, bf16, peak_kind = measured_peaks()
+    n_pad = ((cfg["n"] + 63) // 64) * 64
+    gemm = [(s["uniqueAlphas"], s["msGemm"]) for s in stats if s["msGemm"] > 0]
+    if gemm:
+        flops = [2.0 * r * u * n_pad * cfg["m"] * cfg["z"] for u, _ in gemm]
+        achieved = sum(flops) / (sum(t for _, t in gemm) * 1e-3) / 1e12
+        roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+                    "frac": achieved / bf16, "traffic": None,
+                    "kernel": "tcgen05 BF16 scoring GEMM with fused top-K epilogue",
+                    "flops_per_launch": flops[-1], "peak_source": peak_kind}
+    else:
+        roofline = {"bound": "tensor", "achieved": None, "peak": bf16, "unit": "TFLOP/s", "frac": None,
+                    "traffic": None, "kernel": "tensor-core scoring did not run (exact scoring only)",
+                    "peak_source": peak_kind}
+
+    # ---- plain FP32 form on the same state -----------------------------------
+    plain = None
+    if args.plain_steps > 0:
+        alg.set_scoring(npp.SCORING_EXACT)
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record()
+        for _ in range(args.plain_steps):
+            alg.update()
+        p1.record()
+        torch.cuda.synchronize()
+        pms = p0.elapsed_time(p1)
+        plain = {"value": r * args.plain_steps / (pms * 1e-3), "unit": UNIT, "steps": args.plain_steps,
+                 "ms_per_step": pms / args.plain_steps,
+                 "form": "FP32 SIMT scoring of every unique alpha in nova's operation order"}
+        alg.set_scoring(npp.SCORING_BF16)
+
+    # ---- e2e through the host-buffer entry point ----------------------------
+    pol = alg.get_policy()
+    Gnow = pol.gamma_array()
+    e2e = None
+    if args.e2e_steps > 0:
+        host = POMDPPBVICPU(p, GammaInitial=Gnow)
+        host.update()  # builds the tables; not timed
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            host.update()
+        wall = time.perf_counter() - t0
+        rn4 = cfg["r"] * cfg["n"] * 4
+        e2e = {"value": r * args.e2e_steps / wall, "unit": UNIT, "h2d_bytes_per_step": 2 * rn4 + 4 * cfg["r"],
+               "d2h_bytes_per_step": rn4 + 4 * cfg["r"],
+               "api": "pomdp_pbvi_update_cpu (host Gamma/GammaPrime/pi; wall clock)"}
+        del host
+
+    # ---- CPU baseline (oracle port of nova's loop) on a bounded sample ------
+    cpu = None
+    if rank == 0 and args.cpu_seconds > 0:
+        cores = host_cores()
+        v, pairs, wall = cpu_sample(model, Gnow, args.cpu_seconds, cores)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "%d (belief, action) pairs of nova's loop-form backup against the current alpha set "
+                         "(r=%d) in %.1f s on %d threads" % (pairs, cfg["r"], wall, cores)}
+
+    mdp = None if args.no_mdp else run_mdp(args, rank)
+
+    last = stats[-1]
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": workload_name(cfg, args), "start_horizon": args.warmup,
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (BF16 scoring operands %.1f GB, alpha set %.0f MB)"
+                         % (2.0 * cfg["r"] * n_pad * cfg["m"] * cfg["z"] / 1e9, cfg["r"] * cfg["n"] * 4 / 1e6)},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "plain_fp32": plain,
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "step_breakdown_ms": {k: last[k] for k in ("msDedup", "msScore", "msRescore", "msAssemble", "msTotal",
+                                                   "msGemm")},
+        "unique_alphas": [s["uniqueAlphas"] for s in stats],
+        "rows_rescored": last["rowsMultiCand"], "pairs_full_exact": last["rowsOverflow"],
+        "mdp_vi": mdp,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

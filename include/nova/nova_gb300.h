@@ -1,0 +1,85 @@
+/*
+ * nova-gb300: additive entry points (no counterpart in the reference).
+ *
+ * The reference's own entry points keep their exact semantics; everything
+ * here is new and optional. All functions are synchronous and return NOVA_*
+ * status codes.
+ */
+#ifndef NOVA_GB300_H
+#define NOVA_GB300_H
+
+#include <nova/nova_abi.h>
+#include <nova/mdp/mdp.h>
+#include <nova/mdp/algorithms/mdp_vi_gpu.h>
+#include <nova/mdp/policies/mdp_value_function.h>
+#include <nova/pomdp/pomdp.h>
+#include <nova/pomdp/algorithms/pomdp_pbvi_gpu.h>
+
+NOVA_NS_BEGIN
+
+/* Belief-scoring modes of the PBVI / Perseus backup.
+ *  NOVA_SCORING_EXACT: every candidate alpha is scored in FP32 in the
+ *      reference's operation order (bit-identical to pomdp_pbvi_cpu.cpp:37-103).
+ *  NOVA_SCORING_BF16: tcgen05 tensor cores score all alphas in BF16 (FP32
+ *      accumulate); every alpha within a proven error bound of the best is
+ *      re-scored in the exact FP32 order, so the argmax equals EXACT's. */
+#define NOVA_SCORING_EXACT 0u
+#define NOVA_SCORING_BF16  1u
+
+/* Select the scoring mode used by later pomdp_pbvi_update_gpu calls on this
+ * solver struct (default NOVA_SCORING_BF16 where the shapes allow it). */
+NOVA_API int pomdp_pbvi_set_scoring_gpu(POMDPPBVIGPU *pbvi, unsigned int mode);
+
+/* Per-update counters of the last pomdp_pbvi_update_gpu on this solver. */
+typedef struct NovaPBVIStats {
+    unsigned int horizon;          /* currentHorizon after the update */
+    unsigned int scoring;          /* mode actually used */
+    unsigned int uniqueAlphas;     /* distinct rows of the input Gamma */
+    unsigned int rowsMultiCand;    /* (belief, action, obs) rows re-scored exactly */
+    unsigned int rowsOverflow;     /* (belief, action) pairs scored exactly in full */
+    unsigned int candidates;       /* total alphas re-scored in FP32 */
+    float msDedup, msScore, msRescore, msAssemble, msTotal;
+    float msGemm;                  /* the tensor-core scoring kernel alone (0 if not run) */
+    unsigned int launches;         /* kernels this library launched for the update */
+} NovaPBVIStats;
+
+NOVA_API int pomdp_pbvi_get_stats_gpu(const POMDPPBVIGPU *pbvi, NovaPBVIStats *stats);
+
+/* V(b) = max_i Gamma_i . b over the solver's current device Gamma (the one
+ * get_policy would return), reduced in FP64 on the device. b is a dense host
+ * array of n floats; *a receives pi of the maximising alpha (lowest index on
+ * ties). Replaces, for device-resident policies, the host evaluation in
+ * pomdp_alpha_vectors.cpp:52-79. */
+NOVA_API int pomdp_pbvi_value_gpu(const POMDP *pomdp, const POMDPPBVIGPU *pbvi,
+        const float *b, double *Vb, unsigned int *a);
+
+/* Value iteration until the Bellman residual max_s |V'(s) - V(s)|, computed
+ * in FP64 on the device after every sweep, drops below tol, or maxSweeps
+ * sweeps ran. The reference's VI has no convergence test (mdp_vi_gpu.cu:163-221
+ * runs exactly `horizon` sweeps). The policy is filled as by
+ * mdp_vi_get_policy_gpu. */
+NOVA_API int mdp_vi_execute_until_converged_gpu(const MDP *mdp, MDPVIGPU *vi,
+        MDPValueFunction *policy, double tol, unsigned int maxSweeps,
+        unsigned int *sweeps, double *residual);
+
+/* Residual max_s |V'(s) - V(s)| in FP64 of the last sweep made by
+ * mdp_vi_update_gpu on this solver. */
+NOVA_API int mdp_vi_residual_gpu(const MDP *mdp, const MDPVIGPU *vi, double *residual);
+
+/* Library self-description: 1 if the library was built for sm_103a and a
+ * device is present, 0 otherwise; *deviceError receives (and clears) the
+ * device-side error word that bounded waits set instead of hanging. */
+NOVA_API int nova_gb300_device_status(unsigned int *deviceError);
+
+/* Number of kernels this library has launched since it was loaded. */
+NOVA_API unsigned long long nova_gb300_kernel_launches(void);
+
+/* Test hook: make the count-th future call of a CUDA wrapper of the given
+ * kind fail on the host, without calling CUDA (kind 1 = device allocation,
+ * 2 = host-to-device copy, 3 = device-to-host copy, 4 = kernel launch).
+ * count 0 disarms it. */
+NOVA_API void nova_gb300_inject_fault(unsigned int kind, unsigned int count);
+
+NOVA_NS_END
+
+#endif

@@ -1,0 +1,1104 @@
+// nova-gb300: the point-based backup on the GB300, exact-order path, and
+// the PBVI entry points (device buffers: pomdp_pbvi_*_gpu; host buffers:
+// pomdp_pbvi_*_cpu).
+//
+// What one backup computes (pomdp_pbvi_cpu.cpp:37-162): for every belief i
+// and action a,
+//     j*(i,a,o) = argmax_j  sum_k B[i,k] * gamma * sum_l O(a,S,o) T(s_k,a,l) Gamma_j(S)
+//     alpha_a   = R(.,a) + sum_o gamma * sum_l O T Gamma_{j*}(S)
+//     a*(i)     = argmax_a  alpha_a . b_i ;   Gamma'_i = alpha_{a*},  pi_i = a*
+// with the reference's sentinels (-1e10) and strict '>' (lowest index wins).
+//
+// Kernels (all FP32 with every product and sum rounded separately, in the
+// reference's order, so results are bit-identical to the CPU path):
+//   * tables_*          step-invariant successor lengths and coefficients
+//                       C = fl(O(a,S,o) * T(s,a,l)) in two layouts
+//   * dedup_*           bitwise-identical alpha rows collapse to the lowest
+//                       index (they score identically, and lowest j wins)
+//   * exact_score       per (i,a): all observations x all unique alphas, lanes
+//                       over alphas reading the transposed alpha table
+//                       (coalesced), coefficients broadcast from shared memory
+//   * action_value      per (i,a): alpha_a on the belief support and its value
+//   * assemble          per belief: action argmax, full alpha_{a*} over n states
+// The tensor-core scoring (pbvi_tc.cu) replaces exact_score for rows whose
+// argmax it can prove and hands the rest back to exact_score.
+
+#include "pbvi.h"
+
+#include <vector>
+#include <algorithm>
+
+#include <nova/constants.h>
+#include <nova/pomdp/algorithms/pomdp_pbvi_cpu.h>
+#include <nova/pomdp/algorithms/pomdp_pbvi_gpu.h>
+#include <nova/pomdp/policies/pomdp_alpha_vectors.h>
+
+using nova::POMDP;
+using nova::POMDPPBVICPU;
+using nova::POMDPPBVIGPU;
+using nova::POMDPAlphaVectors;
+using nova::NovaPBVIStats;
+
+namespace nova_gb300 {
+
+constexpr unsigned kNone = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// Step-invariant tables
+// ---------------------------------------------------------------------------
+
+__global__ void tables_len_kernel(unsigned rows, unsigned width, const int *__restrict__ idx,
+                                  unsigned *__restrict__ len) {
+    const unsigned row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= rows) return;
+    unsigned L = width;
+    for (unsigned l = 0; l < width; l++) {
+        if (idx[(size_t)row * width + l] < 0) { L = l; break; }
+    }
+    len[row] = L;
+}
+
+// C1[a][s][l][o] and C3[a][o][s][l] = fl(O(a,S(s,a,l),o) * T(s,a,l)), 0 past the row end.
+__global__ void tables_coef_kernel(DevModel md, const unsigned *__restrict__ succLen, float *__restrict__ C1,
+                                   float *__restrict__ C3) {
+    const size_t total = (size_t)md.m * md.n * md.ns * md.z;
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const unsigned o = (unsigned)(e % md.z);
+        size_t t = e / md.z;
+        const unsigned l = (unsigned)(t % md.ns);
+        t /= md.ns;
+        const unsigned s = (unsigned)(t % md.n);
+        const unsigned a = (unsigned)(t / md.n);
+        float c = 0.0f;
+        if (l < succLen[(size_t)s * md.m + a]) {
+            const size_t row = ((size_t)s * md.m + a) * md.ns + l;
+            const int sp = md.S[row];
+            c = fmul(md.O[((size_t)a * md.n + sp) * md.z + o], md.T[row]);
+        }
+        C1[e] = c;
+        C3[(((size_t)a * md.z + o) * md.n + s) * md.ns + l] = c;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Dedup of alpha rows
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+    x ^= x >> 30; x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27; x *= 0x94d049bb133111ebull;
+    x ^= x >> 31;
+    return x;
+}
+
+__global__ void dedup_hash_kernel(const float *__restrict__ G, unsigned n, unsigned long long *__restrict__ hash) {
+    const unsigned j = blockIdx.x;
+    const unsigned *row = reinterpret_cast<const unsigned *>(G + (size_t)j * n);
+    unsigned long long h = 0;
+    for (unsigned s = threadIdx.x; s < n; s += blockDim.x)
+        h += mix64(((unsigned long long)row[s] << 20) ^ (0x9e3779b97f4a7c15ull * (s + 1)));
+    __shared__ unsigned long long red[32];
+    for (int off = 16; off > 0; off >>= 1) h += __shfl_xor_sync(0xffffffffu, h, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = h;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (unsigned w = 0; w < (blockDim.x + 31) / 32; w++) t += red[w];
+        hash[j] = t;
+    }
+}
+
+__device__ bool rows_equal(const float *G, unsigned n, unsigned j1, unsigned j2) {
+    const unsigned *a = reinterpret_cast<const unsigned *>(G + (size_t)j1 * n);
+    const unsigned *b = reinterpret_cast<const unsigned *>(G + (size_t)j2 * n);
+    for (unsigned s = 0; s < n; s++)
+        if (a[s] != b[s]) return false;
+    return true;
+}
+
+__global__ void dedup_rep_kernel(const unsigned long long *__restrict__ hash, const float *__restrict__ G,
+                                 unsigned n, unsigned rows, unsigned *__restrict__ rep) {
+    __shared__ unsigned long long tile[256];
+    const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned long long myh = j < rows ? hash[j] : 0ull;
+    unsigned r = j;
+    bool found = false;
+    const unsigned last = min(rows, (blockIdx.x + 1) * blockDim.x);  // no candidate beyond this block
+    for (unsigned t0 = 0; t0 < last; t0 += 256) {
+        __syncthreads();
+        if (t0 + threadIdx.x < rows) tile[threadIdx.x] = hash[t0 + threadIdx.x];
+        __syncthreads();
+        if (j < rows && !found) {
+            const unsigned lim = min(256u, j > t0 ? j - t0 : 0u);
+            for (unsigned q = 0; q < lim; q++) {
+                if (tile[q] == myh && rows_equal(G, n, t0 + q, j)) { r = t0 + q; found = true; break; }
+            }
+        }
+    }
+    if (j < rows) rep[j] = r;
+}
+
+// Single-block stream compaction of the rows that are their own representative.
+__global__ void __launch_bounds__(1024) dedup_compact_kernel(const unsigned *__restrict__ rep, unsigned rows,
+                                                             unsigned *__restrict__ uniqJ, unsigned *__restrict__ nU) {
+    __shared__ unsigned warpSums[32];
+    __shared__ unsigned carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (unsigned base = 0; base < rows; base += blockDim.x) {
+        const unsigned j = base + threadIdx.x;
+        const unsigned flag = (j < rows && rep[j] == j) ? 1u : 0u;
+        // inclusive warp scan
+        unsigned v = flag;
+        const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        for (int off = 1; off < 32; off <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, v, off);
+            if (lane >= (unsigned)off) v += y;
+        }
+        if (lane == 31) warpSums[warp] = v;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned w = lane < (blockDim.x >> 5) ? warpSums[lane] : 0u;
+            for (int off = 1; off < 32; off <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, w, off);
+                if (lane >= (unsigned)off) w += y;
+            }
+            warpSums[lane] = w;  // inclusive
+        }
+        __syncthreads();
+        const unsigned before = carry + (warp > 0 ? warpSums[warp - 1] : 0u) + v - flag;
+        if (flag) uniqJ[before] = j;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warpSums[(blockDim.x >> 5) - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *nU = carry;
+}
+
+// Gt[s][u] = G[uniqJ[u]][s]
+__global__ void gather_transpose_kernel(const float *__restrict__ G, unsigned n, const unsigned *__restrict__ uniqJ,
+                                        unsigned nU, float *__restrict__ Gt, size_t gtCols) {
+    __shared__ float tile[32][33];
+    const unsigned u0 = blockIdx.x * 32, s0 = blockIdx.y * 32;
+    for (unsigned k = threadIdx.y; k < 32; k += blockDim.y) {
+        const unsigned u = u0 + k, s = s0 + threadIdx.x;
+        tile[k][threadIdx.x] = (u < nU && s < n) ? G[(size_t)uniqJ[u] * n + s] : 0.0f;
+    }
+    __syncthreads();
+    for (unsigned k = threadIdx.y; k < 32; k += blockDim.y) {
+        const unsigned s = s0 + k, u = u0 + threadIdx.x;
+        if (s < n && u < gtCols) Gt[(size_t)s * gtCols + u] = tile[threadIdx.x][k];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Exact scoring: value(i,a,o,u) in the order of pomdp_pbvi_cpu.cpp:50-83
+// ---------------------------------------------------------------------------
+
+// Better-than for the argmax: strictly larger value, or equal value and
+// lower index. NaN is never better (the reference's `value > bestValue`).
+__device__ __forceinline__ bool better(float v1, unsigned u1, float v2, unsigned u2) {
+    return v1 > v2 || (v1 == v2 && u1 < u2);
+}
+
+template <int ZC>
+__global__ void __launch_bounds__(128) exact_score_kernel(DevModel md, const unsigned *__restrict__ succLen,
+        const unsigned *__restrict__ suppLen, const float *__restrict__ C1, const float *__restrict__ Gt,
+        size_t gtCols, unsigned nU, const unsigned *__restrict__ items, unsigned nItems, unsigned splits,
+        unsigned splitLen, float *__restrict__ partV, unsigned *__restrict__ partU) {
+    extern __shared__ float smem[];
+    float *Cs = smem;                                           // [ns][ZC]
+    int *Ss = reinterpret_cast<int *>(Cs + (size_t)md.ns * ZC); // [ns]
+    __shared__ float redV[4][ZC];
+    __shared__ unsigned redU[4][ZC];
+    __shared__ float runV[ZC];
+    __shared__ unsigned runU[ZC];
+
+    const unsigned tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned split = blockIdx.y;
+    const unsigned uBegin = split * splitLen;
+    const unsigned uEnd = min(nU, uBegin + splitLen);
+    const float gamma = md.gamma;
+
+    for (unsigned w = blockIdx.x; w < nItems; w += gridDim.x) {
+        const unsigned ia = items[w];
+        const unsigned i = ia / md.m, a = ia % md.m;
+        const unsigned Li = suppLen[i];
+        for (unsigned o0 = 0; o0 < md.z; o0 += ZC) {
+            if (tid < ZC) { runV[tid] = NOVA_FLT_MIN; runU[tid] = kNone; }
+            for (unsigned u0 = uBegin; u0 < uEnd; u0 += blockDim.x) {
+                const unsigned u = u0 + tid;
+                const bool valid = u < uEnd;
+                float score[ZC];
+#pragma unroll
+                for (int q = 0; q < ZC; q++) score[q] = 0.0f;
+                for (unsigned k = 0; k < Li; k++) {
+                    const int s = md.Z[(size_t)i * md.rz + k];
+                    const float b = md.B[(size_t)i * md.rz + k];
+                    const unsigned Ls = succLen[(size_t)s * md.m + a];
+                    __syncthreads();
+                    const float *crow = C1 + (((size_t)a * md.n + s) * md.ns) * md.z + o0;
+                    for (unsigned e = tid; e < Ls * ZC; e += blockDim.x) {
+                        const unsigned l = e / ZC, q = e % ZC;
+                        Cs[e] = (o0 + q < md.z) ? crow[(size_t)l * md.z + q] : 0.0f;
+                    }
+                    for (unsigned e = tid; e < Ls; e += blockDim.x) Ss[e] = md.S[((size_t)s * md.m + a) * md.ns + e];
+                    __syncthreads();
+                    if (valid) {
+                        float vt[ZC];
+#pragma unroll
+                        for (int q = 0; q < ZC; q++) vt[q] = 0.0f;
+                        for (unsigned l = 0; l < Ls; l++) {
+                            const float g = Gt[(size_t)Ss[l] * gtCols + u];
+#pragma unroll
+                            for (int q = 0; q < ZC; q++) vt[q] = fadd(vt[q], fmul(Cs[l * ZC + q], g));
+                        }
+#pragma unroll
+                        for (int q = 0; q < ZC; q++) score[q] = fadd(score[q], fmul(fmul(vt[q], gamma), b));
+                    }
+                }
+                // Block argmax per observation over this chunk of alphas.
+#pragma unroll
+                for (int q = 0; q < ZC; q++) {
+                    float v = valid ? score[q] : NOVA_FLT_MIN;
+                    unsigned uu = valid ? u : kNone;
+                    if (!(v > NOVA_FLT_MIN)) { v = NOVA_FLT_MIN; uu = kNone; }
+                    for (int off = 16; off > 0; off >>= 1) {
+                        const float v2 = __shfl_xor_sync(0xffffffffu, v, off);
+                        const unsigned u2 = __shfl_xor_sync(0xffffffffu, uu, off);
+                        if (better(v2, u2, v, uu)) { v = v2; uu = u2; }
+                    }
+                    if (lane == 0) { redV[warp][q] = v; redU[warp][q] = uu; }
+                }
+                __syncthreads();
+                if (tid < ZC) {
+                    float v = runV[tid];
+                    unsigned uu = runU[tid];
+                    for (unsigned ww = 0; ww < blockDim.x / 32; ww++)
+                        if (redU[ww][tid] != kNone && better(redV[ww][tid], redU[ww][tid], v, uu)) {
+                            v = redV[ww][tid]; uu = redU[ww][tid];
+                        }
+                    runV[tid] = v; runU[tid] = uu;
+                }
+                __syncthreads();
+            }
+            if (tid < ZC && o0 + tid < md.z) {
+                const size_t p = ((size_t)w * md.z + o0 + tid) * splits + split;
+                partV[p] = runV[tid];
+                partU[p] = runU[tid];
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Merge split partials in alpha order; map unique index -> original j.
+// When no alpha beats the -1e10 sentinel the reference keeps the previous
+// observation's choice (bestj outlives the o loop, pomdp_pbvi_cpu.cpp:43-45);
+// for the first observation it is undefined there and 0 here.
+__global__ void exact_finalize_kernel(DevModel md, const unsigned *__restrict__ items, unsigned nItems,
+                                      unsigned splits, const float *__restrict__ partV,
+                                      const unsigned *__restrict__ partU, const unsigned *__restrict__ uniqJ,
+                                      unsigned *__restrict__ jstar) {
+    const unsigned w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nItems) return;
+    const unsigned ia = items[w];
+    unsigned prev = 0;
+    for (unsigned o = 0; o < md.z; o++) {
+        float v = NOVA_FLT_MIN;
+        unsigned uu = kNone;
+        for (unsigned sp = 0; sp < splits; sp++) {
+            const size_t p = ((size_t)w * md.z + o) * splits + sp;
+            if (partU[p] != kNone && better(partV[p], partU[p], v, uu)) { v = partV[p]; uu = partU[p]; }
+        }
+        const unsigned j = uu == kNone ? prev : uniqJ[uu];
+        jstar[(size_t)ia * md.z + o] = j;
+        prev = j;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Action values and assembly (pomdp_pbvi_cpu.cpp:88-101 and :128-157)
+// ---------------------------------------------------------------------------
+
+// gamma * sum_l C3 * G_j(S) for state s under action a, observation o, in the
+// reference order (products left to right, sums sequential).
+__device__ __forceinline__ float projected(const DevModel &md, const float *__restrict__ C3,
+                                           const unsigned *__restrict__ succLen, const float *__restrict__ Gj,
+                                           unsigned a, unsigned o, unsigned s) {
+    const unsigned Ls = succLen[(size_t)s * md.m + a];
+    const float *c = C3 + (((size_t)a * md.z + o) * md.n + s) * md.ns;
+    const int *sp = md.S + ((size_t)s * md.m + a) * md.ns;
+    float vt = 0.0f;
+    for (unsigned l = 0; l < Ls; l++) vt = fadd(vt, fmul(c[l], Gj[sp[l]]));
+    return fmul(vt, md.gamma);
+}
+
+// One warp per (belief, action) item: alpha_a on the belief support, then
+// value = sum_k alpha_a(s_k) * b_k in support order.
+__global__ void action_value_kernel(DevModel md, const unsigned *__restrict__ succLen,
+                                    const unsigned *__restrict__ suppLen, const float *__restrict__ C3,
+                                    const float *__restrict__ G, const unsigned *__restrict__ jstar,
+                                    const unsigned *__restrict__ items, unsigned nItems,
+                                    float *__restrict__ actVal) {
+    const unsigned warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    if (warpGlobal >= nItems) return;
+    const unsigned ia = items ? items[warpGlobal] : warpGlobal;
+    const unsigned i = ia / md.m, a = ia % md.m;
+    const unsigned Li = suppLen[i];
+    float value = 0.0f;
+    for (unsigned k0 = 0; k0 < Li; k0 += 32) {
+        const unsigned k = k0 + lane;
+        float p = 0.0f;
+        if (k < Li) {
+            const int s = md.Z[(size_t)i * md.rz + k];
+            float alpha = md.R[(size_t)s * md.m + a];
+            for (unsigned o = 0; o < md.z; o++) {
+                const unsigned j = jstar[(size_t)ia * md.z + o];
+                alpha = fadd(alpha, projected(md, C3, succLen, G + (size_t)j * md.n, a, o, (unsigned)s));
+            }
+            p = fmul(alpha, md.B[(size_t)i * md.rz + k]);
+        }
+        const unsigned cnt = min(32u, Li - k0);
+        for (unsigned t = 0; t < cnt; t++) value = fadd(value, __shfl_sync(0xffffffffu, p, t));
+    }
+    if (lane == 0) actVal[ia] = value;
+}
+
+// One block per belief: action argmax (strict '>' from -1e10, lowest action
+// on ties), then the full alpha of the best action over all n states. A
+// belief whose every action fails to beat the sentinel keeps its old row
+// and action, as in the reference.
+__global__ void assemble_kernel(DevModel md, const unsigned *__restrict__ succLen, const float *__restrict__ C3,
+                                const float *__restrict__ G, const unsigned *__restrict__ jstar,
+                                const float *__restrict__ actVal, unsigned beliefBegin, float *__restrict__ dst,
+                                unsigned *__restrict__ pi, float *__restrict__ rowOut, unsigned *__restrict__ actionOut) {
+    const unsigned i = beliefBegin + blockIdx.x;
+    __shared__ unsigned bestA;
+    extern __shared__ unsigned jsh[];  // [z]
+    if (threadIdx.x == 0) {
+        float best = NOVA_FLT_MIN;
+        unsigned ba = kNone;
+        for (unsigned a = 0; a < md.m; a++) {
+            const float v = actVal[(size_t)i * md.m + a];
+            if (v > best) { best = v; ba = a; }
+        }
+        bestA = ba;
+        if (actionOut) *actionOut = ba;
+    }
+    __syncthreads();
+    const unsigned a = bestA;
+    if (a == kNone) return;
+    if (pi && threadIdx.x == 0) pi[i] = a;
+    float *out = rowOut ? rowOut : dst + (size_t)i * md.n;
+    const unsigned *js = jstar + ((size_t)i * md.m + a) * md.z;
+    for (unsigned o = threadIdx.x; o < md.z; o += blockDim.x) jsh[o] = js[o];
+    __syncthreads();
+    for (unsigned s = threadIdx.x; s < md.n; s += blockDim.x) {
+        float alpha = md.R[(size_t)s * md.m + a];
+        for (unsigned o = 0; o < md.z; o++)
+            alpha = fadd(alpha, projected(md, C3, succLen, G + (size_t)jsh[o] * md.n, a, o, s));
+        out[s] = alpha;
+    }
+}
+
+__global__ void iota_items_kernel(unsigned *items, unsigned count, unsigned first) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < count) items[t] = first + t;
+}
+
+// ---------------------------------------------------------------------------
+// V(b) in FP64 (pomdp_alpha_vectors.cpp:52-79 reduced in double)
+// ---------------------------------------------------------------------------
+
+__global__ void row_dot_fp64_kernel(const float *__restrict__ G, unsigned n, const float *__restrict__ b,
+                                    double *__restrict__ out) {
+    const unsigned j = blockIdx.x;
+    double acc = 0.0;
+    for (unsigned s = threadIdx.x; s < n; s += blockDim.x) acc += (double)G[(size_t)j * n + s] * (double)b[s];
+    __shared__ double red[32];
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (unsigned w = 0; w < (blockDim.x + 31) / 32; w++) t += red[w];
+        out[j] = t;
+    }
+}
+
+__global__ void argmax_fp64_kernel(const double *__restrict__ v, unsigned rows, const unsigned *__restrict__ pi,
+                                   double *__restrict__ outV, unsigned *__restrict__ outA) {
+    double best = (double)NOVA_FLT_MIN;
+    unsigned bi = kNone;
+    for (unsigned j = threadIdx.x; j < rows; j += blockDim.x)
+        if (v[j] > best || (v[j] == best && bi != kNone && j < bi)) { best = v[j]; bi = j; }
+    __shared__ double sv[256];
+    __shared__ unsigned si[256];
+    sv[threadIdx.x] = best; si[threadIdx.x] = bi;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (unsigned t = 1; t < blockDim.x; t++) {
+            if (si[t] == kNone) continue;
+            if (si[0] == kNone || sv[t] > sv[0] || (sv[t] == sv[0] && si[t] < si[0])) { sv[0] = sv[t]; si[0] = si[t]; }
+        }
+        *outV = sv[0];
+        *outA = si[0] == kNone ? 0u : pi[si[0]];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// BackupEngine
+// ---------------------------------------------------------------------------
+
+BackupEngine::~BackupEngine() {
+    cudaDeviceSynchronize();
+    if (tc) tc_release(tc);
+    cudaFree(succLen); cudaFree(suppLen); cudaFree(C1); cudaFree(C3);
+    cudaFree(hash); cudaFree(rep); cudaFree(uniqJ); cudaFree(nUniqueDev); cudaFree(Gt);
+    cudaFree(jstar); cudaFree(actVal); cudaFree(partV); cudaFree(partU); cudaFree(items); cudaFree(itemCount);
+    cudaFree(dotScratch); cudaFree(bDense); cudaFree(resultA); cudaFree(resultV); cudaFree(rowScratch);
+    cudaFree(vnb); cudaFree(vnp1b); cudaFree(btilde);
+    if (eventsMade)
+        for (auto &e : ev) cudaEventDestroy(e);
+}
+
+int BackupEngine::build(const DevModel &model, const char *fn) {
+    md = model;
+    int rc;
+    // Work queued by earlier synchronous copies must be complete before the
+    // tables read the model.
+    if ((rc = sync_device(fn)) != NOVA_SUCCESS) return rc;
+    const size_t nm = (size_t)md.n * md.m;
+    const size_t coef = nm * md.ns * md.z;
+    if ((rc = dev_alloc(&succLen, nm, fn, "the successor lengths")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&suppLen, md.r, fn, "the belief support lengths")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&C1, coef, fn, "the projection coefficients")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&C3, coef, fn, "the projection coefficients (successor-major)")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&hash, md.r, fn, "the alpha hashes")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&rep, md.r, fn, "the alpha representatives")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&uniqJ, md.r, fn, "the unique alphas")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&nUniqueDev, 1, fn, "the unique alpha count")) != NOVA_SUCCESS) return rc;
+    gtCols = round_up(md.r, 32);
+    if ((rc = dev_alloc(&Gt, (size_t)md.n * gtCols, fn, "the transposed alphas")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&jstar, (size_t)md.r * md.m * md.z, fn, "the chosen alphas")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&actVal, (size_t)md.r * md.m, fn, "the action values")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&items, (size_t)md.r * md.m, fn, "the work list")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&itemCount, 1, fn, "the work list count")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&dotScratch, md.r, fn, "the FP64 values")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&bDense, md.n, fn, "the belief")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&resultA, 1, fn, "the action")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&resultV, 1, fn, "the value")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&rowScratch, md.n, fn, "the alpha row")) != NOVA_SUCCESS) return rc;
+    if (!eventsMade) {
+        for (auto &e : ev) cudaEventCreate(&e);
+        eventsMade = true;
+    }
+    tables_len_kernel<<<ceil_div(nm, 256), 256>>>((unsigned)nm, md.ns, md.S, succLen);
+    if ((rc = check_launch(fn, "successor lengths")) != NOVA_SUCCESS) return rc;
+    tables_len_kernel<<<ceil_div(md.r, 256), 256>>>(md.r, md.rz, md.Z, suppLen);
+    if ((rc = check_launch(fn, "support lengths")) != NOVA_SUCCESS) return rc;
+    tables_coef_kernel<<<std::min<size_t>(ceil_div(coef, 256), 65535u * 8u), 256>>>(md, succLen, C1, C3);
+    if ((rc = check_launch(fn, "projection coefficients")) != NOVA_SUCCESS) return rc;
+    return sync_device(fn);
+}
+
+int BackupEngine::dedup(const float *src, unsigned rows, unsigned *nUnique, const char *fn) {
+    int rc;
+    if (rows == 0) { *nUnique = 0; return NOVA_SUCCESS; }
+    dedup_hash_kernel<<<rows, 128, 0, stream>>>(src, md.n, hash);
+    if ((rc = check_launch(fn, "alpha hash")) != NOVA_SUCCESS) return rc;
+    dedup_rep_kernel<<<ceil_div(rows, 256), 256, 0, stream>>>(hash, src, md.n, rows, rep);
+    if ((rc = check_launch(fn, "alpha dedup")) != NOVA_SUCCESS) return rc;
+    dedup_compact_kernel<<<1, 1024, 0, stream>>>(rep, rows, uniqJ, nUniqueDev);
+    if ((rc = check_launch(fn, "alpha compaction")) != NOVA_SUCCESS) return rc;
+    unsigned h = 0;
+    if (cudaMemcpyAsync(&h, nUniqueDev, sizeof(unsigned), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+            cudaStreamSynchronize(stream) != cudaSuccess) {
+        cudaGetLastError();
+        NOVA_ERR(fn, "Failed to read the number of unique alpha-vectors.");
+        return NOVA_ERROR_MEMCPY_TO_HOST;
+    }
+    *nUnique = h;
+    // Transposed unique alphas for the exact scan.
+    dim3 grid(ceil_div(std::max(h, 1u), 32), ceil_div(md.n, 32));
+    gather_transpose_kernel<<<grid, dim3(32, 8), 0, stream>>>(src, md.n, uniqJ, h, Gt, gtCols);
+    return check_launch(fn, "alpha transpose");
+}
+
+template <int ZC>
+static void launch_exact(BackupEngine &e, const unsigned *items, unsigned nItems, unsigned nU, unsigned splits,
+                         unsigned splitLen, unsigned grid) {
+    const size_t smem = (size_t)e.md.ns * ZC * sizeof(float) + (size_t)e.md.ns * sizeof(int);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(exact_score_kernel<ZC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    exact_score_kernel<ZC><<<dim3(grid, splits), 128, smem, e.stream>>>(e.md, e.succLen, e.suppLen, e.C1, e.Gt,
+            e.gtCols, nU, items, nItems, splits, splitLen, e.partV, e.partU);
+}
+
+int BackupEngine::exact_score(const unsigned *itemList, unsigned nItems, unsigned nU, const char *fn) {
+    if (nItems == 0) return NOVA_SUCCESS;
+    int rc;
+    // Split the alpha range so that the grid covers the device.
+    const unsigned target = 152u * 8u;
+    unsigned splits = 1;
+    if (nItems < target) splits = std::min(ceil_div(target, nItems), std::max(1u, ceil_div(nU, 128)));
+    splits = std::max(1u, std::min(splits, 1024u));
+    const unsigned splitLen = (unsigned)round_up(ceil_div(std::max(nU, 1u), splits), 128);
+    splits = std::max(1u, ceil_div(std::max(nU, 1u), splitLen));
+    const size_t need = (size_t)nItems * md.z * splits;
+    if (need > partCap) {
+        cudaFree(partV); cudaFree(partU);
+        partV = nullptr; partU = nullptr; partCap = 0;
+        if ((rc = dev_alloc(&partV, need, fn, "the partial maxima")) != NOVA_SUCCESS) return rc;
+        if ((rc = dev_alloc(&partU, need, fn, "the partial arg-maxima")) != NOVA_SUCCESS) return rc;
+        partCap = need;
+    }
+    const unsigned grid = std::min(nItems, 65535u);
+    const size_t smem32 = (size_t)md.ns * 32 * sizeof(float) + md.ns * sizeof(int);
+    if (md.z >= 16 && smem32 <= 200 * 1024) launch_exact<32>(*this, itemList, nItems, nU, splits, splitLen, grid);
+    else if (md.z >= 4 && (size_t)md.ns * 8 * 4 <= 200 * 1024) launch_exact<8>(*this, itemList, nItems, nU, splits, splitLen, grid);
+    else if ((size_t)md.ns * 2 * 4 <= 200 * 1024) launch_exact<2>(*this, itemList, nItems, nU, splits, splitLen, grid);
+    else {
+        NOVA_ERR(fn, "Too many successors per state for the exact scoring kernel.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    if ((rc = check_launch(fn, "exact belief scoring")) != NOVA_SUCCESS) return rc;
+    exact_finalize_kernel<<<ceil_div(nItems, 128), 128, 0, stream>>>(md, itemList, nItems, splits, partV, partU,
+                                                                      uniqJ, jstar);
+    return check_launch(fn, "exact belief scoring (merge)");
+}
+
+int BackupEngine::fill_items(unsigned first, unsigned count, const char *fn) {
+    if (count == 0) return NOVA_SUCCESS;
+    iota_items_kernel<<<ceil_div(count, 256), 256, 0, stream>>>(items, count, first);
+    return check_launch(fn, "work list");
+}
+
+int BackupEngine::assemble(const float *src, float *dst, unsigned *pi, int onlyBelief, float *dstRowOverride,
+                           unsigned *actionOut, const char *fn) {
+    int rc;
+    const unsigned firstBelief = onlyBelief >= 0 ? (unsigned)onlyBelief : 0u;
+    const unsigned nBeliefs = onlyBelief >= 0 ? 1u : md.r;
+    const unsigned nItems = nBeliefs * md.m;
+    const unsigned *itemList = nullptr;
+    if (onlyBelief >= 0) {
+        iota_items_kernel<<<ceil_div(nItems, 256), 256, 0, stream>>>(items, nItems, firstBelief * md.m);
+        if ((rc = check_launch(fn, "work list")) != NOVA_SUCCESS) return rc;
+        itemList = items;
+    }
+    action_value_kernel<<<ceil_div((size_t)nItems * 32, 256), 256, 0, stream>>>(md, succLen, suppLen, C3, src, jstar,
+                                                                                itemList, nItems, actVal);
+    if ((rc = check_launch(fn, "action values")) != NOVA_SUCCESS) return rc;
+    assemble_kernel<<<nBeliefs, 256, md.z * sizeof(unsigned), stream>>>(md, succLen, C3, src, jstar, actVal,
+                                                                         firstBelief, dst, pi, dstRowOverride,
+                                                                         actionOut);
+    return check_launch(fn, "alpha assembly");
+}
+
+int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsigned *pi, const char *fn) {
+    int rc;
+    memset(&stats, 0, sizeof(stats));
+    const unsigned long long launches0 = launch_count();
+    cudaEventRecord(ev[0], stream);
+    unsigned nU = 0;
+    if ((rc = dedup(src, rGamma, &nU, fn)) != NOVA_SUCCESS) return rc;
+    stats.uniqueAlphas = nU;
+    cudaEventRecord(ev[1], stream);
+    const unsigned allItems = md.r * md.m;
+    bool done = false;
+    if (scoring == NOVA_SCORING_BF16 && tc_supported(md) && nU >= 2) {
+        unsigned nOverflow = 0;
+        rc = tc_score(*this, src, nU, &nOverflow, fn);
+        if (rc != NOVA_SUCCESS) return rc;
+        cudaEventRecord(ev[2], stream);
+        stats.scoring = NOVA_SCORING_BF16;
+        stats.rowsOverflow = nOverflow;
+        if ((rc = exact_score(items, nOverflow, nU, fn)) != NOVA_SUCCESS) return rc;
+        done = true;
+    }
+    if (!done) {
+        iota_items_kernel<<<ceil_div(allItems, 256), 256, 0, stream>>>(items, allItems, 0);
+        if ((rc = check_launch(fn, "work list")) != NOVA_SUCCESS) return rc;
+        cudaEventRecord(ev[2], stream);
+        stats.scoring = NOVA_SCORING_EXACT;
+        if ((rc = exact_score(items, allItems, nU, fn)) != NOVA_SUCCESS) return rc;
+    }
+    cudaEventRecord(ev[3], stream);
+    if ((rc = assemble(src, dst, pi, -1, nullptr, nullptr, fn)) != NOVA_SUCCESS) return rc;
+    cudaEventRecord(ev[4], stream);
+    if (cudaEventSynchronize(ev[4]) != cudaSuccess) {
+        cudaGetLastError();
+        return sync_device(fn);
+    }
+    cudaEventElapsedTime(&stats.msDedup, ev[0], ev[1]);
+    cudaEventElapsedTime(&stats.msScore, ev[1], ev[2]);
+    cudaEventElapsedTime(&stats.msRescore, ev[2], ev[3]);
+    cudaEventElapsedTime(&stats.msAssemble, ev[3], ev[4]);
+    cudaEventElapsedTime(&stats.msTotal, ev[0], ev[4]);
+    stats.launches = (unsigned)(launch_count() - launches0);
+    const unsigned derr = tc_device_error();
+    if (derr != 0) {
+        NOVA_ERR(fn, "A device-side wait timed out; results of this update are invalid.");
+        return NOVA_ERROR_KERNEL_EXECUTION;
+    }
+    return NOVA_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// Solver workspaces
+// ---------------------------------------------------------------------------
+
+struct PbviGpuWorkspace : Workspace {
+    BackupEngine eng;
+    bool built = false;
+    const void *modelKey[6] = {};   // device model pointers the tables were built from
+    float *d_Gamma = nullptr, *d_GammaPrime = nullptr;
+    unsigned *d_pi = nullptr;
+    ~PbviGpuWorkspace() override {
+        cudaDeviceSynchronize();
+        cudaFree(d_Gamma); cudaFree(d_GammaPrime); cudaFree(d_pi);
+    }
+};
+
+struct PbviCpuWorkspace : Workspace {
+    BackupEngine eng;
+    bool built = false;
+    int *S = nullptr; float *T = nullptr, *O = nullptr, *R = nullptr; int *Z = nullptr; float *B = nullptr;
+    float *Gamma = nullptr, *GammaPrime = nullptr;
+    unsigned *pi = nullptr;
+    float *hostGamma = nullptr, *hostGammaPrime = nullptr;
+    unsigned *hostPi = nullptr;
+    ~PbviCpuWorkspace() override {
+        cudaDeviceSynchronize();
+        cudaFree(S); cudaFree(T); cudaFree(O); cudaFree(R); cudaFree(Z); cudaFree(B);
+        cudaFree(Gamma); cudaFree(GammaPrime); cudaFree(pi);
+    }
+};
+
+static DevModel device_model(const POMDP *p) {
+    DevModel md;
+    md.n = p->n; md.ns = p->ns; md.m = p->m; md.z = p->z; md.r = p->r; md.rz = p->rz; md.gamma = p->gamma;
+    md.S = p->d_S; md.T = p->d_T; md.O = p->d_O; md.R = p->d_R; md.Z = p->d_Z; md.B = p->d_B;
+    return md;
+}
+
+// Upload a host POMDP into device arrays owned by a workspace.
+template <typename W>
+static int upload_model(W *ws, const POMDP *p, DevModel *md, const char *fn) {
+    const size_t nms = (size_t)p->n * p->m * p->ns, mnz = (size_t)p->m * p->n * p->z, nm = (size_t)p->n * p->m,
+                 rrz = (size_t)p->r * p->rz;
+    int rc;
+    if ((rc = dev_alloc(&ws->S, nms, fn, "the successor states")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&ws->T, nms, fn, "the state transitions")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&ws->O, mnz, fn, "the observation transitions")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&ws->R, nm, fn, "the rewards")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&ws->Z, rrz, fn, "the non-zero belief states")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&ws->B, rrz, fn, "the belief points")) != NOVA_SUCCESS) return rc;
+    if ((rc = h2d(ws->S, p->S, nms * sizeof(int), fn, "the successor states")) != NOVA_SUCCESS) return rc;
+    if ((rc = h2d(ws->T, p->T, nms * sizeof(float), fn, "the state transitions")) != NOVA_SUCCESS) return rc;
+    if ((rc = h2d(ws->O, p->O, mnz * sizeof(float), fn, "the observation transitions")) != NOVA_SUCCESS) return rc;
+    if ((rc = h2d(ws->R, p->R, nm * sizeof(float), fn, "the rewards")) != NOVA_SUCCESS) return rc;
+    if ((rc = h2d(ws->Z, p->Z, rrz * sizeof(int), fn, "the non-zero belief states")) != NOVA_SUCCESS) return rc;
+    if ((rc = h2d(ws->B, p->B, rrz * sizeof(float), fn, "the belief points")) != NOVA_SUCCESS) return rc;
+    md->n = p->n; md->ns = p->ns; md->m = p->m; md->z = p->z; md->r = p->r; md->rz = p->rz; md->gamma = p->gamma;
+    md->S = ws->S; md->T = ws->T; md->O = ws->O; md->R = ws->R; md->Z = ws->Z; md->B = ws->B;
+    return NOVA_SUCCESS;
+}
+
+// Shared validation of pomdp_pbvi_cpu.cpp:192-200 / pomdp_pbvi_gpu.cu:266-274.
+static bool pomdp_shape_invalid(const POMDP *p) {
+    return p == nullptr || p->n == 0 || p->ns == 0 || p->m == 0 || p->z == 0 || p->r == 0 || p->rz == 0 ||
+           p->gamma < 0.0f || p->gamma > 1.0f || p->horizon < 1;
+}
+
+}  // namespace nova_gb300
+
+using namespace nova_gb300;
+
+// ===========================================================================
+// Device-buffer PBVI (pomdp_pbvi_gpu.cu)
+// ===========================================================================
+
+static PbviGpuWorkspace *pbvi_gpu_ws(const POMDPPBVIGPU *pbvi) {
+    std::lock_guard<std::mutex> lock(registry_mutex());
+    return find_workspace<PbviGpuWorkspace>(pbvi);
+}
+
+extern "C" int pomdp_pbvi_uninitialize_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi) {
+    (void)pomdp;
+    if (pbvi == nullptr) {
+        NOVA_ERR("pomdp_pbvi_uninitialize_gpu", "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    pbvi->currentHorizon = 0;
+    int result = NOVA_SUCCESS;
+    {
+        std::lock_guard<std::mutex> lock(registry_mutex());
+        auto *ws = find_workspace<PbviGpuWorkspace>(pbvi);
+        if (ws != nullptr) {
+            if (pbvi->d_Gamma == ws->d_Gamma) pbvi->d_Gamma = nullptr;
+            if (pbvi->d_GammaPrime == ws->d_GammaPrime) pbvi->d_GammaPrime = nullptr;
+            if (pbvi->d_pi == ws->d_pi) pbvi->d_pi = nullptr;
+            registry().erase(pbvi);
+        }
+    }
+    // Fields this library did not allocate are freed as the reference does
+    // (pomdp_pbvi_gpu.cu:312-358).
+    float **fields[3] = {&pbvi->d_Gamma, &pbvi->d_GammaPrime, &pbvi->d_alphaBA};
+    for (float **f : fields) {
+        if (*f != nullptr && dev_free(*f, "pomdp_pbvi_uninitialize_gpu", "the alpha-vectors") != NOVA_SUCCESS)
+            result = NOVA_ERROR_DEVICE_FREE;
+        *f = nullptr;
+    }
+    if (pbvi->d_pi != nullptr && dev_free(pbvi->d_pi, "pomdp_pbvi_uninitialize_gpu", "pi") != NOVA_SUCCESS)
+        result = NOVA_ERROR_DEVICE_FREE;
+    pbvi->d_pi = nullptr;
+    return result;
+}
+
+extern "C" int pomdp_pbvi_initialize_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi) {
+    static const char *fn = "pomdp_pbvi_initialize_gpu";
+    if (pomdp == nullptr || pbvi == nullptr || pomdp->n == 0 || pomdp->r == 0 || pbvi->GammaInitial == nullptr) {
+        NOVA_ERR(fn, "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    pbvi->currentHorizon = 0;
+    unsigned scoring = NOVA_SCORING_BF16;
+    {
+        std::lock_guard<std::mutex> lock(registry_mutex());
+        auto *old = find_workspace<PbviGpuWorkspace>(pbvi);
+        if (old != nullptr) {
+            scoring = old->eng.scoring;
+            if (pbvi->d_Gamma == old->d_Gamma) pbvi->d_Gamma = nullptr;
+            if (pbvi->d_GammaPrime == old->d_GammaPrime) pbvi->d_GammaPrime = nullptr;
+            if (pbvi->d_pi == old->d_pi) pbvi->d_pi = nullptr;
+            registry().erase(pbvi);
+        }
+    }
+    std::unique_ptr<PbviGpuWorkspace> ws(new PbviGpuWorkspace());
+    ws->eng.scoring = scoring;
+    const size_t rn = (size_t)pomdp->r * pomdp->n;
+    int rc;
+    if ((rc = dev_alloc(&ws->d_Gamma, rn, fn, "Gamma")) != NOVA_SUCCESS) return rc;
+    if ((rc = h2d(ws->d_Gamma, pbvi->GammaInitial, rn * sizeof(float), fn, "Gamma")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&ws->d_GammaPrime, rn, fn, "Gamma (prime)")) != NOVA_SUCCESS) return rc;
+    if ((rc = h2d(ws->d_GammaPrime, pbvi->GammaInitial, rn * sizeof(float), fn, "Gamma (prime)")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&ws->d_pi, pomdp->r, fn, "pi")) != NOVA_SUCCESS) return rc;
+    if (cudaMemset(ws->d_pi, 0, pomdp->r * sizeof(unsigned)) != cudaSuccess) {
+        cudaGetLastError();
+        NOVA_ERR(fn, "Failed to clear pi.");
+        return NOVA_ERROR_MEMCPY_TO_DEVICE;
+    }
+    pbvi->d_Gamma = ws->d_Gamma;
+    pbvi->d_GammaPrime = ws->d_GammaPrime;
+    pbvi->d_pi = ws->d_pi;
+    std::lock_guard<std::mutex> lock(registry_mutex());
+    registry()[pbvi] = std::move(ws);
+    return NOVA_SUCCESS;
+}
+
+// Tables are built on first use and rebuilt if the device model changed.
+static int ensure_built(PbviGpuWorkspace *ws, const POMDP *pomdp, const char *fn) {
+    const void *key[6] = {pomdp->d_S, pomdp->d_T, pomdp->d_O, pomdp->d_R, pomdp->d_Z, pomdp->d_B};
+    if (ws->built && memcmp(key, ws->modelKey, sizeof(key)) == 0 && ws->eng.md.r == pomdp->r &&
+            ws->eng.md.n == pomdp->n)
+        return NOVA_SUCCESS;
+    if (ws->built) {
+        const unsigned scoring = ws->eng.scoring;
+        ws->eng.~BackupEngine();
+        new (&ws->eng) BackupEngine();
+        ws->eng.scoring = scoring;
+        ws->built = false;
+    }
+    int rc = ws->eng.build(device_model(pomdp), fn);
+    if (rc != NOVA_SUCCESS) return rc;
+    memcpy(ws->modelKey, key, sizeof(key));
+    ws->built = true;
+    return NOVA_SUCCESS;
+}
+
+extern "C" int pomdp_pbvi_update_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi) {
+    static const char *fn = "pomdp_pbvi_update_gpu";
+    if (pomdp_shape_invalid(pomdp) || pbvi == nullptr || pomdp->d_S == nullptr || pomdp->d_T == nullptr ||
+            pomdp->d_O == nullptr || pomdp->d_R == nullptr || pomdp->d_Z == nullptr || pomdp->d_B == nullptr ||
+            pbvi->d_Gamma == nullptr || pbvi->d_GammaPrime == nullptr || pbvi->d_pi == nullptr) {
+        NOVA_ERR(fn, "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    PbviGpuWorkspace *ws = pbvi_gpu_ws(pbvi);
+    if (ws == nullptr) {
+        NOVA_ERR(fn, "The solver is not initialized (call pomdp_pbvi_initialize_gpu).");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    int rc = ensure_built(ws, pomdp, fn);
+    if (rc != NOVA_SUCCESS) return rc;
+    const bool even = (pbvi->currentHorizon % 2u) == 0u;
+    const float *src = even ? pbvi->d_Gamma : pbvi->d_GammaPrime;
+    float *dst = even ? pbvi->d_GammaPrime : pbvi->d_Gamma;
+    rc = ws->eng.backup_all(src, pomdp->r, dst, pbvi->d_pi, fn);
+    if (rc != NOVA_SUCCESS) return rc;
+    pbvi->currentHorizon++;
+    ws->eng.stats.horizon = pbvi->currentHorizon;
+    return NOVA_SUCCESS;
+}
+
+extern "C" int pomdp_pbvi_get_policy_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi, POMDPAlphaVectors *policy) {
+    static const char *fn = "pomdp_pbvi_get_policy_gpu";
+    if (pomdp == nullptr || pbvi == nullptr || policy == nullptr) {
+        NOVA_ERR(fn, "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    if (pomdp_alpha_vectors_initialize(policy, pomdp->n, pomdp->m, pomdp->r) != NOVA_SUCCESS) {
+        NOVA_ERR(fn, "Could not create the policy.");
+        return NOVA_ERROR_POLICY_CREATION;
+    }
+    const float *src = (pbvi->currentHorizon % 2u == 0u) ? pbvi->d_Gamma : pbvi->d_GammaPrime;
+    int rc = d2h(policy->Gamma, src, (size_t)pomdp->r * pomdp->n * sizeof(float), fn, "Gamma");
+    if (rc != NOVA_SUCCESS) return rc;
+    return d2h(policy->pi, pbvi->d_pi, pomdp->r * sizeof(unsigned), fn, "pi");
+}
+
+extern "C" int pomdp_pbvi_execute_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi, POMDPAlphaVectors *policy) {
+    static const char *fn = "pomdp_pbvi_execute_gpu";
+    if (pomdp_shape_invalid(pomdp) || pomdp->d_S == nullptr || pomdp->d_T == nullptr || pomdp->d_O == nullptr ||
+            pomdp->d_R == nullptr || pomdp->d_Z == nullptr || pomdp->d_B == nullptr || pbvi == nullptr ||
+            pbvi->GammaInitial == nullptr || policy == nullptr) {
+        NOVA_ERR(fn, "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    if (pbvi->numThreads % 32 != 0) {
+        NOVA_ERR(fn, "Invalid number of threads.");
+        return NOVA_ERROR_INVALID_CUDA_PARAM;
+    }
+    int rc = pomdp_pbvi_initialize_gpu(pomdp, pbvi);
+    if (rc != NOVA_SUCCESS) return rc;
+    while (pbvi->currentHorizon < pomdp->horizon) {
+        rc = pomdp_pbvi_update_gpu(pomdp, pbvi);
+        if (rc != NOVA_SUCCESS) return rc;
+    }
+    rc = pomdp_pbvi_get_policy_gpu(pomdp, pbvi, policy);
+    if (rc != NOVA_SUCCESS) return rc;
+    return pomdp_pbvi_uninitialize_gpu(pomdp, pbvi);
+}
+
+extern "C" int pomdp_pbvi_set_scoring_gpu(POMDPPBVIGPU *pbvi, unsigned int mode) {
+    if (pbvi == nullptr || (mode != NOVA_SCORING_EXACT && mode != NOVA_SCORING_BF16)) {
+        NOVA_ERR("pomdp_pbvi_set_scoring_gpu", "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    PbviGpuWorkspace *ws = pbvi_gpu_ws(pbvi);
+    if (ws == nullptr) {
+        NOVA_ERR("pomdp_pbvi_set_scoring_gpu", "The solver is not initialized.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    ws->eng.scoring = mode;
+    return NOVA_SUCCESS;
+}
+
+extern "C" int pomdp_pbvi_get_stats_gpu(const POMDPPBVIGPU *pbvi, NovaPBVIStats *stats) {
+    if (pbvi == nullptr || stats == nullptr) {
+        NOVA_ERR("pomdp_pbvi_get_stats_gpu", "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    PbviGpuWorkspace *ws = pbvi_gpu_ws(pbvi);
+    if (ws == nullptr) {
+        NOVA_ERR("pomdp_pbvi_get_stats_gpu", "The solver is not initialized.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    *stats = ws->eng.stats;
+    return NOVA_SUCCESS;
+}
+
+extern "C" int pomdp_pbvi_value_gpu(const POMDP *pomdp, const POMDPPBVIGPU *pbvi, const float *b, double *Vb,
+                                    unsigned int *a) {
+    static const char *fn = "pomdp_pbvi_value_gpu";
+    if (pomdp == nullptr || pbvi == nullptr || b == nullptr || Vb == nullptr || a == nullptr ||
+            pbvi->d_Gamma == nullptr || pbvi->d_GammaPrime == nullptr || pbvi->d_pi == nullptr) {
+        NOVA_ERR(fn, "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    PbviGpuWorkspace *ws = pbvi_gpu_ws(pbvi);
+    if (ws == nullptr) {
+        NOVA_ERR(fn, "The solver is not initialized.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    int rc = ensure_built(ws, pomdp, fn);
+    if (rc != NOVA_SUCCESS) return rc;
+    BackupEngine &e = ws->eng;
+    const float *G = (pbvi->currentHorizon % 2u == 0u) ? pbvi->d_Gamma : pbvi->d_GammaPrime;
+    if ((rc = h2d(e.bDense, b, pomdp->n * sizeof(float), fn, "the belief")) != NOVA_SUCCESS) return rc;
+    row_dot_fp64_kernel<<<pomdp->r, 256, 0, e.stream>>>(G, pomdp->n, e.bDense, e.dotScratch);
+    if ((rc = check_launch(fn, "FP64 belief values")) != NOVA_SUCCESS) return rc;
+    argmax_fp64_kernel<<<1, 256, 0, e.stream>>>(e.dotScratch, pomdp->r, pbvi->d_pi, e.resultV, e.resultA);
+    if ((rc = check_launch(fn, "FP64 belief argmax")) != NOVA_SUCCESS) return rc;
+    if ((rc = sync_device(fn)) != NOVA_SUCCESS) return rc;
+    if ((rc = d2h(Vb, e.resultV, sizeof(double), fn, "the value")) != NOVA_SUCCESS) return rc;
+    return d2h(a, e.resultA, sizeof(unsigned), fn, "the action");
+}
+
+// ===========================================================================
+// Host-buffer PBVI (pomdp_pbvi_cpu.cpp): same engine, host arrays
+// ===========================================================================
+
+static PbviCpuWorkspace *pbvi_cpu_ws(const POMDPPBVICPU *pbvi) {
+    std::lock_guard<std::mutex> lock(registry_mutex());
+    return find_workspace<PbviCpuWorkspace>(pbvi);
+}
+
+extern "C" int pomdp_pbvi_uninitialize_cpu(const POMDP *pomdp, POMDPPBVICPU *pbvi) {
+    (void)pomdp;
+    if (pbvi == nullptr) {
+        NOVA_ERR("pomdp_pbvi_uninitialize_cpu", "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    pbvi->currentHorizon = 0;
+    {
+        std::lock_guard<std::mutex> lock(registry_mutex());
+        registry().erase(pbvi);
+    }
+    delete[] pbvi->Gamma; pbvi->Gamma = nullptr;
+    delete[] pbvi->GammaPrime; pbvi->GammaPrime = nullptr;
+    delete[] pbvi->pi; pbvi->pi = nullptr;
+    return NOVA_SUCCESS;
+}
+
+extern "C" int pomdp_pbvi_initialize_cpu(const POMDP *pomdp, POMDPPBVICPU *pbvi) {
+    static const char *fn = "pomdp_pbvi_initialize_cpu";
+    if (pomdp == nullptr || pbvi == nullptr || pomdp->n == 0 || pomdp->r == 0 || pbvi->GammaInitial == nullptr) {
+        NOVA_ERR(fn, "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    pbvi->currentHorizon = 0;
+    unsigned scoring = NOVA_SCORING_BF16;
+    {
+        std::lock_guard<std::mutex> lock(registry_mutex());
+        auto *old = find_workspace<PbviCpuWorkspace>(pbvi);
+        if (old != nullptr) {
+            scoring = old->eng.scoring;
+            if (pbvi->Gamma == old->hostGamma) { delete[] pbvi->Gamma; pbvi->Gamma = nullptr; }
+            if (pbvi->GammaPrime == old->hostGammaPrime) { delete[] pbvi->GammaPrime; pbvi->GammaPrime = nullptr; }
+            if (pbvi->pi == old->hostPi) { delete[] pbvi->pi; pbvi->pi = nullptr; }
+            registry().erase(pbvi);
+        }
+    }
+    const size_t rn = (size_t)pomdp->r * pomdp->n;
+    // Host arrays as pomdp_pbvi_cpu.cpp:165-183.
+    pbvi->Gamma = new float[rn];
+    pbvi->GammaPrime = new float[rn];
+    pbvi->pi = new unsigned int[pomdp->r];
+    memcpy(pbvi->Gamma, pbvi->GammaInitial, rn * sizeof(float));
+    memcpy(pbvi->GammaPrime, pbvi->GammaInitial, rn * sizeof(float));
+    for (unsigned i = 0; i < pomdp->r; i++) pbvi->pi[i] = 0;
+    std::unique_ptr<PbviCpuWorkspace> ws(new PbviCpuWorkspace());
+    ws->eng.scoring = scoring;
+    ws->hostGamma = pbvi->Gamma; ws->hostGammaPrime = pbvi->GammaPrime; ws->hostPi = pbvi->pi;
+    std::lock_guard<std::mutex> lock(registry_mutex());
+    registry()[pbvi] = std::move(ws);
+    return NOVA_SUCCESS;
+}
+
+// The model is uploaded at the first update after initialize (the struct may
+// be initialized before its arrays are filled) and reused afterwards.
+static int pbvi_cpu_prepare(PbviCpuWorkspace *ws, const POMDP *pomdp, const char *fn) {
+    if (ws->built) return NOVA_SUCCESS;
+    if (pomdp->S == nullptr || pomdp->T == nullptr || pomdp->O == nullptr || pomdp->R == nullptr ||
+            pomdp->Z == nullptr || pomdp->B == nullptr) {
+        NOVA_ERR(fn, "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    DevModel md;
+    int rc = upload_model(ws, pomdp, &md, fn);
+    if (rc != NOVA_SUCCESS) return rc;
+    const size_t rn = (size_t)pomdp->r * pomdp->n;
+    if ((rc = dev_alloc(&ws->Gamma, rn, fn, "Gamma")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&ws->GammaPrime, rn, fn, "Gamma (prime)")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&ws->pi, pomdp->r, fn, "pi")) != NOVA_SUCCESS) return rc;
+    if ((rc = ws->eng.build(md, fn)) != NOVA_SUCCESS) return rc;
+    ws->built = true;
+    return NOVA_SUCCESS;
+}
+
+// One backup with host arrays as the source of truth: upload the input set,
+// the output set (rows a belief does not improve keep their contents) and
+// pi; back up on the device; download the output set and pi.
+static int pbvi_cpu_step(PbviCpuWorkspace *ws, const POMDP *pomdp, POMDPPBVICPU *pbvi, const char *fn) {
+    const size_t rn = (size_t)pomdp->r * pomdp->n;
+    const bool even = (pbvi->currentHorizon % 2u) == 0u;
+    float *hsrc = even ? pbvi->Gamma : pbvi->GammaPrime;
+    float *hdst = even ? pbvi->GammaPrime : pbvi->Gamma;
+    int rc;
+    if ((rc = h2d(ws->Gamma, hsrc, rn * sizeof(float), fn, "Gamma")) != NOVA_SUCCESS) return rc;
+    if ((rc = h2d(ws->GammaPrime, hdst, rn * sizeof(float), fn, "Gamma (prime)")) != NOVA_SUCCESS) return rc;
+    if ((rc = h2d(ws->pi, pbvi->pi, pomdp->r * sizeof(unsigned), fn, "pi")) != NOVA_SUCCESS) return rc;
+    if ((rc = ws->eng.backup_all(ws->Gamma, pomdp->r, ws->GammaPrime, ws->pi, fn)) != NOVA_SUCCESS) return rc;
+    if ((rc = d2h(hdst, ws->GammaPrime, rn * sizeof(float), fn, "Gamma (prime)")) != NOVA_SUCCESS) return rc;
+    if ((rc = d2h(pbvi->pi, ws->pi, pomdp->r * sizeof(unsigned), fn, "pi")) != NOVA_SUCCESS) return rc;
+    pbvi->currentHorizon++;
+    return NOVA_SUCCESS;
+}
+
+extern "C" int pomdp_pbvi_update_cpu(const POMDP *pomdp, POMDPPBVICPU *pbvi) {
+    static const char *fn = "pomdp_pbvi_update_cpu";
+    if (pomdp_shape_invalid(pomdp) || pbvi == nullptr || pbvi->Gamma == nullptr || pbvi->GammaPrime == nullptr ||
+            pbvi->pi == nullptr) {
+        NOVA_ERR(fn, "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    PbviCpuWorkspace *ws = pbvi_cpu_ws(pbvi);
+    if (ws == nullptr) {
+        NOVA_ERR(fn, "The solver is not initialized (call pomdp_pbvi_initialize_cpu).");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    int rc = pbvi_cpu_prepare(ws, pomdp, fn);
+    if (rc != NOVA_SUCCESS) return rc;
+    return pbvi_cpu_step(ws, pomdp, pbvi, fn);
+}
+
+extern "C" int pomdp_pbvi_get_policy_cpu(const POMDP *pomdp, POMDPPBVICPU *pbvi, POMDPAlphaVectors *policy) {
+    static const char *fn = "pomdp_pbvi_get_policy_cpu";
+    if (pomdp == nullptr || pbvi == nullptr || policy == nullptr) {
+        NOVA_ERR(fn, "Invalid arguments. Policy must be undefined.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    if (pomdp_alpha_vectors_initialize(policy, pomdp->n, pomdp->m, pomdp->r) != NOVA_SUCCESS) {
+        NOVA_ERR(fn, "Could not create the policy.");
+        return NOVA_ERROR_POLICY_CREATION;
+    }
+    const float *src = (pbvi->currentHorizon % 2u == 0u) ? pbvi->Gamma : pbvi->GammaPrime;
+    memcpy(policy->Gamma, src, (size_t)pomdp->r * pomdp->n * sizeof(float));
+    memcpy(policy->pi, pbvi->pi, pomdp->r * sizeof(unsigned));
+    return NOVA_SUCCESS;
+}
+
+extern "C" int pomdp_pbvi_execute_cpu(const POMDP *pomdp, POMDPPBVICPU *pbvi, POMDPAlphaVectors *policy) {
+    static const char *fn = "pomdp_pbvi_execute_cpu";
+    if (pomdp_shape_invalid(pomdp) || pomdp->S == nullptr || pomdp->T == nullptr || pomdp->O == nullptr ||
+            pomdp->R == nullptr || pomdp->Z == nullptr || pomdp->B == nullptr || pbvi == nullptr ||
+            pbvi->GammaInitial == nullptr || policy == nullptr) {
+        NOVA_ERR(fn, "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    int rc = pomdp_pbvi_initialize_cpu(pomdp, pbvi);
+    if (rc != NOVA_SUCCESS) return rc;
+    PbviCpuWorkspace *ws = pbvi_cpu_ws(pbvi);
+    if ((rc = pbvi_cpu_prepare(ws, pomdp, fn)) != NOVA_SUCCESS) return rc;
+    // The whole horizon runs on the device; the sets come back once.
+    const size_t rn = (size_t)pomdp->r * pomdp->n;
+    if ((rc = h2d(ws->Gamma, pbvi->Gamma, rn * sizeof(float), fn, "Gamma")) != NOVA_SUCCESS) return rc;
+    if ((rc = h2d(ws->GammaPrime, pbvi->GammaPrime, rn * sizeof(float), fn, "Gamma (prime)")) != NOVA_SUCCESS) return rc;
+    if ((rc = h2d(ws->pi, pbvi->pi, pomdp->r * sizeof(unsigned), fn, "pi")) != NOVA_SUCCESS) return rc;
+    while (pbvi->currentHorizon < pomdp->horizon) {
+        const bool even = (pbvi->currentHorizon % 2u) == 0u;
+        rc = ws->eng.backup_all(even ? ws->Gamma : ws->GammaPrime, pomdp->r, even ? ws->GammaPrime : ws->Gamma,
+                                ws->pi, fn);
+        if (rc != NOVA_SUCCESS) return rc;
+        pbvi->currentHorizon++;
+    }
+    if ((rc = d2h(pbvi->Gamma, ws->Gamma, rn * sizeof(float), fn, "Gamma")) != NOVA_SUCCESS) return rc;
+    if ((rc = d2h(pbvi->GammaPrime, ws->GammaPrime, rn * sizeof(float), fn, "Gamma (prime)")) != NOVA_SUCCESS) return rc;
+    if ((rc = d2h(pbvi->pi, ws->pi, pomdp->r * sizeof(unsigned), fn, "pi")) != NOVA_SUCCESS) return rc;
+    rc = pomdp_pbvi_get_policy_cpu(pomdp, pbvi, policy);
+    if (rc != NOVA_SUCCESS) return rc;
+    return pomdp_pbvi_uninitialize_cpu(pomdp, pbvi);
+}

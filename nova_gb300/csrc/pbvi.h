@@ -1,0 +1,94 @@
+// nova-gb300 internal: the point-based backup engine shared by PBVI and
+// Perseus (device buffers, step-invariant tables, per-step scratch) and the
+// interface between the exact-order kernels (pbvi.cu) and the tensor-core
+// scoring path (pbvi_tc.cu).
+#pragma once
+
+#include "common.h"
+
+#include <nova/pomdp/pomdp.h>
+#include <nova/nova_gb300.h>
+
+namespace nova_gb300 {
+
+using nova::NovaPBVIStats;
+
+// Device view of a POMDP model. All arrays are device pointers with the
+// reference layouts: S,T [n][m][ns]; O [m][n][z]; R [n][m]; Z,B [r][rz].
+struct DevModel {
+    unsigned n, ns, m, z, r, rz;
+    float gamma;
+    const int *S;
+    const float *T;
+    const float *O;
+    const float *R;
+    const int *Z;
+    const float *B;
+};
+
+struct TcState;  // tensor-core scoring state (pbvi_tc.cu)
+
+// Exact-order kernel workspace and tables.
+struct BackupEngine {
+    DevModel md{};
+    // Step-invariant tables (built once per model):
+    unsigned *succLen = nullptr;   // [n*m]  successors before the first negative entry of row (s,a)
+    unsigned *suppLen = nullptr;   // [r]    support entries before the first negative state of belief i
+    float *C1 = nullptr;           // [m][n][ns][z]  fl(O[a,S(s,a,l),o] * T[s,a,l]); 0 past the row end
+    float *C3 = nullptr;           // [m][z][n][ns]  same values, successor-contiguous
+    // Per-step scratch:
+    unsigned long long *hash = nullptr;  // [r] row hash of the input Gamma
+    unsigned *rep = nullptr;             // [r] lowest index with a bitwise-identical row
+    unsigned *uniqJ = nullptr;           // [r] unique index -> lowest original index
+    unsigned *nUniqueDev = nullptr;      // device scalar
+    float *Gt = nullptr;                 // [n][gtCols] transposed unique alphas
+    size_t gtCols = 0;
+    unsigned *jstar = nullptr;           // [r][m][z] chosen alpha per (belief, action, observation)
+    float *actVal = nullptr;             // [r][m] value of each action's assembled alpha at the belief
+    float *partV = nullptr;              // [items][z][splits] split-scan partial maxima
+    unsigned *partU = nullptr;
+    size_t partCap = 0;
+    unsigned *items = nullptr;           // [r*m] work list (belief*m + action)
+    unsigned *itemCount = nullptr;       // device scalar
+    double *dotScratch = nullptr;        // [r] FP64 V(b) row values
+    float *bDense = nullptr;             // [n]
+    unsigned *resultA = nullptr;         // [1]
+    double *resultV = nullptr;           // [1]
+    float *rowScratch = nullptr;         // [n] single-belief alpha (Perseus)
+    float *vnb = nullptr, *vnp1b = nullptr;  // [r] Perseus values over V_n and V_{n+1}
+    unsigned *btilde = nullptr;          // [r] Perseus compacted belief list
+    cudaStream_t stream = 0;
+    cudaEvent_t ev[6] = {};
+    bool eventsMade = false;
+    unsigned scoring = NOVA_SCORING_BF16;
+    NovaPBVIStats stats{};
+    TcState *tc = nullptr;
+
+    ~BackupEngine();
+    int build(const DevModel &model, const char *fn);
+    // One backup of every belief (PBVI): Gamma rows [0, rGamma) -> dst, pi.
+    int backup_all(const float *src, unsigned rGamma, float *dst, unsigned *pi, const char *fn);
+    // Dedup of Gamma rows [0, rows); returns the number of unique rows.
+    int dedup(const float *src, unsigned rows, unsigned *nUnique, const char *fn);
+    // Exact scoring of the listed (belief, action) items over the unique rows.
+    int exact_score(const unsigned *items, unsigned nItems, unsigned nU, const char *fn);
+    // Work list of `count` consecutive items starting at `first`.
+    int fill_items(unsigned first, unsigned count, const char *fn);
+    // Action values and best-action assembly for all beliefs (or one).
+    int assemble(const float *src, float *dst, unsigned *pi, int onlyBelief, float *dstRowOverride,
+                 unsigned *actionOut, const char *fn);
+};
+
+// Tensor-core scoring (pbvi_tc.cu). tc_supported: the shapes fit the GEMM.
+bool tc_supported(const DevModel &md);
+// Builds the BF16 operand tables once; returns NOVA_SUCCESS or an error.
+int tc_build(BackupEngine &eng, const char *fn);
+// Scores every (belief, action, observation) row against the nU unique rows
+// of src (gathered through eng.uniqJ), writes eng.jstar for rows whose argmax
+// is proven, and appends the (belief, action) items that need the exact full
+// scan to eng.items / *nOverflow.
+int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nOverflow, const char *fn);
+void tc_release(TcState *tc);
+unsigned tc_device_error();
+
+}  // namespace nova_gb300

@@ -1,0 +1,105 @@
+"""MDP model object (python/nova/mdp.py:40-305), without the file loader and
+the legacy `solve` (use MDPValueIterationCPU / MDPValueIterationGPU)."""
+import ctypes as ct
+
+import numpy as np
+
+from . import nova_mdp as nm
+from .pomdp import _fill
+
+
+class MDP(nm.NovaMDP):
+    """ A Markov Decision Process (MDP) object. """
+
+    def __init__(self):
+        self.n = int(0)
+        self.ns = int(0)
+        self.m = int(0)
+        self.gamma = float(0.9)
+        self.horizon = int(1)
+        self.epsilon = float(0.01)
+        self.s0 = int(0)
+        self.ng = int(0)
+        self.goals = ct.POINTER(ct.c_uint)()
+        self.S = ct.POINTER(ct.c_int)()
+        self.T = ct.POINTER(ct.c_float)()
+        self.R = ct.POINTER(ct.c_float)()
+        self.d_goals = ct.POINTER(ct.c_uint)()
+        self.d_S = ct.POINTER(ct.c_int)()
+        self.d_T = ct.POINTER(ct.c_float)()
+        self.d_R = ct.POINTER(ct.c_float)()
+        self.Rmin = None
+        self.Rmax = None
+        self.cpuIsInitialized = False
+        self.gpuIsInitialized = False
+
+    def __del__(self):
+        self.uninitialize_gpu()
+        self.uninitialize()
+
+    def initialize(self, n, ns, m, gamma, horizon, epsilon, s0, ng):
+        """ Allocate the MDP's arrays (mdp_initialize_cpu). """
+        if self.cpuIsInitialized:
+            return
+        result = nm._nova.mdp_initialize_cpu(self, n, ns, m, gamma, horizon, epsilon, s0, ng)
+        if result != 0:
+            print("Failed to initialize the MDP.")
+            raise Exception()
+        self.cpuIsInitialized = True
+
+    def uninitialize(self):
+        if not self.cpuIsInitialized:
+            return
+        result = nm._nova.mdp_uninitialize_cpu(self)
+        if result != 0:
+            print("Failed to uninitialize the MDP.")
+            raise Exception()
+        self.cpuIsInitialized = False
+
+    def initialize_gpu(self):
+        """ Upload S, T, R (and goals) to the GPU (python/nova/mdp.py:119-136). """
+        if self.gpuIsInitialized:
+            return
+        result = nm._nova.mdp_initialize_successors_gpu(self)
+        result += nm._nova.mdp_initialize_state_transitions_gpu(self)
+        result += nm._nova.mdp_initialize_rewards_gpu(self)
+        if self.ng > 0:
+            result += nm._nova.mdp_initialize_goals_gpu(self)
+        if result != 0:
+            print("Failed to initialize the 'nova' library's GPU variables for the MDP.")
+            raise Exception()
+        self.gpuIsInitialized = True
+
+    def uninitialize_gpu(self):
+        if not self.gpuIsInitialized:
+            return
+        result = nm._nova.mdp_uninitialize_successors_gpu(self)
+        result += nm._nova.mdp_uninitialize_state_transitions_gpu(self)
+        result += nm._nova.mdp_uninitialize_rewards_gpu(self)
+        if self.ng > 0:
+            result += nm._nova.mdp_uninitialize_goals_gpu(self)
+        if result != 0:
+            print("Failed to uninitialize the 'nova' library's GPU variables for the MDP.")
+            raise Exception()
+        self.gpuIsInitialized = False
+
+    def set_arrays(self, S, T, R, goals=None):
+        """ Copy numpy arrays (nova layouts) into the allocated C arrays. """
+        _fill(self.S, S, np.int32)
+        _fill(self.T, T, np.float32)
+        _fill(self.R, R, np.float32)
+        if goals is not None and self.ng > 0:
+            _fill(self.goals, goals, np.uint32)
+        R = np.asarray(R, dtype=np.float32)
+        self.Rmin = float(R.min())
+        self.Rmax = float(R.max())
+
+    @classmethod
+    def from_arrays(cls, model, epsilon=0.0001, s0=0, ng=0):
+        p = cls()
+        p.initialize(model["n"], model["ns"], model["m"], model["gamma"], model["horizon"], epsilon, s0, ng)
+        p.set_arrays(model["S"], model["T"], model["R"], model.get("goals"))
+        return p
+
+    def load(self, filename, filetype='cassandra', scalarize=lambda x: x[0]):
+        raise NotImplementedError("nova-gb300 does not parse MDP files; fill the arrays with set_arrays()")

@@ -1,0 +1,149 @@
+"""POMDP model object (python/nova/pomdp.py:40-402).
+
+Same class, fields and methods as the reference wrapper. Arrays are owned by
+the C library (pomdp_initialize_cpu allocates them); `set_arrays` fills them
+from numpy in one copy per array instead of the reference's element loop.
+File loading and belief-set expansion are not part of this library.
+"""
+import ctypes as ct
+
+import numpy as np
+
+from . import nova_pomdp as npm
+
+
+def _fill(ptr, values, ctype):
+    values = np.ascontiguousarray(values, dtype=ctype)
+    ct.memmove(ptr, values.ctypes.data, values.nbytes)
+
+
+class POMDP(npm.NovaPOMDP):
+    """ A Partially Observable Markov Decision Process (POMDP) object. """
+
+    def __init__(self):
+        self.n = int(0)
+        self.ns = int(0)
+        self.m = int(0)
+        self.z = int(0)
+        self.r = int(0)
+        self.rz = int(0)
+        self.gamma = float(0.9)
+        self.horizon = int(1)
+        self.S = ct.POINTER(ct.c_int)()
+        self.T = ct.POINTER(ct.c_float)()
+        self.O = ct.POINTER(ct.c_float)()
+        self.R = ct.POINTER(ct.c_float)()
+        self.Z = ct.POINTER(ct.c_int)()
+        self.B = ct.POINTER(ct.c_float)()
+        self.d_S = ct.POINTER(ct.c_int)()
+        self.d_T = ct.POINTER(ct.c_float)()
+        self.d_O = ct.POINTER(ct.c_float)()
+        self.d_R = ct.POINTER(ct.c_float)()
+        self.d_Z = ct.POINTER(ct.c_int)()
+        self.d_B = ct.POINTER(ct.c_float)()
+        self.Rmin = None
+        self.Rmax = None
+        self.cpuIsInitialized = False
+        self.gpuIsInitialized = False
+
+    def __del__(self):
+        self.uninitialize_gpu()
+        self.uninitialize()
+
+    def initialize(self, n, ns, m, z, r, rz, gamma, horizon):
+        """ Allocate the POMDP's arrays (pomdp_initialize_cpu). """
+        if self.cpuIsInitialized:
+            return
+        result = npm._nova.pomdp_initialize_cpu(self, n, ns, m, z, r, rz, gamma, horizon)
+        if result != 0:
+            print("Failed to initialize the POMDP.")
+            raise Exception()
+        self.cpuIsInitialized = True
+
+    def uninitialize(self):
+        """ Free the POMDP's arrays (pomdp_uninitialize_cpu). """
+        if not self.cpuIsInitialized:
+            return
+        result = npm._nova.pomdp_uninitialize_cpu(self)
+        if result != 0:
+            print("Failed to uninitialize the POMDP.")
+            raise Exception()
+        self.cpuIsInitialized = False
+
+    def initialize_gpu(self):
+        """ Upload the arrays to the GPU (pomdp_initialize_gpu). """
+        if self.gpuIsInitialized:
+            return
+        result = npm._nova.pomdp_initialize_gpu(self)
+        if result != 0:
+            print("Failed to initialize the 'nova' library's GPU variables for the POMDP.")
+            raise Exception()
+        self.gpuIsInitialized = True
+
+    def uninitialize_gpu(self):
+        """ Free the GPU copies (pomdp_uninitialize_gpu). """
+        if not self.gpuIsInitialized:
+            return
+        result = npm._nova.pomdp_uninitialize_gpu(self)
+        if result != 0:
+            print("Failed to uninitialize the 'nova' library's GPU variables for the POMDP.")
+            raise Exception()
+        self.gpuIsInitialized = False
+
+    def set_arrays(self, S, T, O, R, Z, B, Rmin=None, Rmax=None):
+        """ Copy numpy arrays (nova layouts) into the allocated C arrays. """
+        _fill(self.S, S, np.int32)
+        _fill(self.T, T, np.float32)
+        _fill(self.O, O, np.float32)
+        _fill(self.R, R, np.float32)
+        _fill(self.Z, Z, np.int32)
+        _fill(self.B, B, np.float32)
+        R = np.asarray(R, dtype=np.float32)
+        self.Rmin = float(R.min()) if Rmin is None else Rmin
+        self.Rmax = float(R.max()) if Rmax is None else Rmax
+
+    @classmethod
+    def from_arrays(cls, model):
+        """ Build a POMDP from a dict with n, ns, m, z, r, rz, gamma, horizon, S, T, O, R, Z, B. """
+        p = cls()
+        p.initialize(model["n"], model["ns"], model["m"], model["z"], model["r"], model["rz"], model["gamma"],
+                     model["horizon"])
+        p.set_arrays(model["S"], model["T"], model["O"], model["R"], model["Z"], model["B"])
+        return p
+
+    def load(self, filename, filetype='cassandra', scalarize=lambda x: x[0]):
+        """ Not provided: model files are parsed outside this library (see set_arrays). """
+        raise NotImplementedError("nova-gb300 does not parse POMDP files; fill the arrays with set_arrays()")
+
+    def expand(self, method='random', numBeliefsToAdd=1000, pemaPolicy=None, pemaAlgorithm=None):
+        """ Not provided: belief-set expansion is outside this library. """
+        raise NotImplementedError("nova-gb300 does not expand belief sets; pass Z/B with set_arrays()")
+
+    def sigma_approximate(self, numDesiredNonZeroValues=1):
+        """ Not provided: sigma-approximation is outside this library. """
+        raise NotImplementedError("nova-gb300 does not provide the sigma approximation")
+
+    def belief_update(self, b, a, o):
+        """ Belief update b' = normalise(O(a,.,o) * T(.,a,.)^T b) (pomdp_belief_update_cpu). """
+        b = (ct.c_float * self.n)(*np.asarray(b, dtype=np.float32).ravel())
+        bp = ct.POINTER(ct.c_float)()
+        result = npm._nova.pomdp_belief_update_cpu(self, b, int(a), int(o), ct.byref(bp))
+        if result != 0:
+            print("Failed to perform a belief update on the CPU.")
+            raise Exception()
+        out = np.array([bp[s] for s in range(self.n)], dtype=np.float32)
+        return out
+
+    def __str__(self):
+        def arr(ptr, count, shape):
+            return np.array([ptr[i] for i in range(count)]).reshape(shape)
+        result = "n:       %d\nns:      %d\nm:       %d\nz:       %d\nr:       %d\nrz:      %d\n" \
+                 "horizon: %d\ngamma:   %s\n" % (self.n, self.ns, self.m, self.z, self.r, self.rz, self.horizon,
+                                                 str(self.gamma))
+        result += "S(s, a, s'):\n%s\n\n" % str(arr(self.S, self.n * self.m * self.ns, (self.n, self.m, self.ns)))
+        result += "T(s, a, s'):\n%s\n\n" % str(arr(self.T, self.n * self.m * self.ns, (self.n, self.m, self.ns)))
+        result += "O(a, s', o):\n%s\n\n" % str(arr(self.O, self.m * self.n * self.z, (self.m, self.n, self.z)))
+        result += "R(s, a):\n%s\n\n" % str(arr(self.R, self.n * self.m, (self.n, self.m)))
+        result += "Z(i, s):\n%s\n\n" % str(arr(self.Z, self.r * self.rz, (self.r, self.rz)))
+        result += "B(i, s):\n%s\n\n" % str(arr(self.B, self.r * self.rz, (self.r, self.rz)))
+        return result

@@ -1,0 +1,152 @@
+"""PBVI solver objects (python/nova/pomdp_pbvi.py:38-214).
+
+POMDPPBVICPU keeps nova's host-buffer contract and POMDPPBVIGPU its
+device-buffer contract; in this library both run the backup on the GB300.
+"""
+import ctypes as ct
+
+import numpy as np
+
+from . import pomdp
+from . import pomdp_alpha_vectors as pav
+from . import nova_pomdp_pbvi as npp
+
+
+def _initial_gamma(p, GammaInitial):
+    """nova's default: Rmin / (1 - gamma) everywhere, or 0 when gamma == 1."""
+    if GammaInitial is None:
+        if p.gamma < 1.0:
+            rmin = p.Rmin if p.Rmin is not None else float(
+                np.ctypeslib.as_array(p.R, shape=(p.n * p.m,)).min())
+            GammaInitial = np.full(p.r * p.n, np.float32(rmin) / (np.float32(1.0) - np.float32(p.gamma)),
+                                   dtype=np.float32)
+        else:
+            GammaInitial = np.zeros(p.r * p.n, dtype=np.float32)
+    GammaInitial = np.ascontiguousarray(np.asarray(GammaInitial, dtype=np.float32).ravel())
+    buf = (ct.c_float * (p.r * p.n))()
+    ct.memmove(buf, GammaInitial.ctypes.data, GammaInitial.nbytes)
+    return buf
+
+
+class POMDPPBVICPU(npp.NovaPOMDPPBVICPU):
+    """ The point-based value iteration solver (host buffers). """
+
+    def __init__(self, pomdpObject, GammaInitial=None):
+        self.pomdp = pomdpObject
+        self.pomdpPtr = ct.POINTER(pomdp.POMDP)(self.pomdp)
+        self._GammaInitialBuf = _initial_gamma(self.pomdp, GammaInitial)
+        self.GammaInitial = ct.cast(self._GammaInitialBuf, ct.POINTER(ct.c_float))
+        self.currentHorizon = int(0)
+        self.Gamma = ct.POINTER(ct.c_float)()
+        self.GammaPrime = ct.POINTER(ct.c_float)()
+        self.pi = ct.POINTER(ct.c_uint)()
+        result = npp._nova.pomdp_pbvi_initialize_cpu(self.pomdpPtr, self)
+        if result != 0:
+            print("Failed to initialize the PBVI (CPU) algorithm.")
+            raise Exception()
+
+    def __del__(self):
+        result = npp._nova.pomdp_pbvi_uninitialize_cpu(self.pomdpPtr, self)
+        if result != 0:
+            print("Failed to free the PBVI (CPU) algorithm.")
+            raise Exception()
+
+    def update(self):
+        """ One backup of every belief (pomdp_pbvi_update_cpu). """
+        result = npp._nova.pomdp_pbvi_update_cpu(self.pomdpPtr, self)
+        if result != 0:
+            raise RuntimeError("pomdp_pbvi_update_cpu failed with code %d" % result)
+
+    def solve(self):
+        """ Solve the POMDP; returns the POMDPAlphaVectors policy. """
+        policy = pav.POMDPAlphaVectors()
+        result = npp._nova.pomdp_pbvi_execute_cpu(self.pomdpPtr, self, policy)
+        if result != 0:
+            print("Failed to execute the 'nova' library's CPU POMDP solver.")
+            raise Exception()
+        return policy
+
+    def get_policy(self):
+        policy = pav.POMDPAlphaVectors()
+        result = npp._nova.pomdp_pbvi_get_policy_cpu(self.pomdpPtr, self, policy)
+        if result != 0:
+            raise RuntimeError("pomdp_pbvi_get_policy_cpu failed with code %d" % result)
+        return policy
+
+    def __str__(self):
+        return "currentHorizon: %i\n\n" % self.currentHorizon
+
+
+class POMDPPBVIGPU(npp.NovaPOMDPPBVIGPU):
+    """ The point-based value iteration solver (device buffers). """
+
+    def __init__(self, pomdpObject, numThreads=1024, GammaInitial=None):
+        self.pomdp = pomdpObject
+        self.pomdpPtr = ct.POINTER(pomdp.POMDP)(self.pomdp)
+        self._GammaInitialBuf = _initial_gamma(self.pomdp, GammaInitial)
+        self.GammaInitial = ct.cast(self._GammaInitialBuf, ct.POINTER(ct.c_float))
+        self.currentHorizon = int(0)
+        self.numThreads = numThreads
+        self.d_Gamma = ct.POINTER(ct.c_float)()
+        self.d_GammaPrime = ct.POINTER(ct.c_float)()
+        self.d_pi = ct.POINTER(ct.c_uint)()
+        self.d_alphaBA = ct.POINTER(ct.c_float)()
+        result = npp._nova.pomdp_pbvi_initialize_gpu(self.pomdpPtr, self)
+        if result != 0:
+            print("Failed to initialize the PBVI (GPU) algorithm.")
+            raise Exception()
+
+    def __del__(self):
+        result = npp._nova.pomdp_pbvi_uninitialize_gpu(self.pomdpPtr, self)
+        if result != 0:
+            print("Failed to free the PBVI (GPU) algorithm.")
+            raise Exception()
+
+    def set_scoring(self, mode):
+        """ npp.SCORING_EXACT or npp.SCORING_BF16 (pomdp_pbvi_set_scoring_gpu). """
+        result = npp._nova.pomdp_pbvi_set_scoring_gpu(self, int(mode))
+        if result != 0:
+            raise RuntimeError("pomdp_pbvi_set_scoring_gpu failed with code %d" % result)
+
+    def update(self):
+        """ One backup of every belief (pomdp_pbvi_update_gpu). """
+        result = npp._nova.pomdp_pbvi_update_gpu(self.pomdpPtr, self)
+        if result != 0:
+            raise RuntimeError("pomdp_pbvi_update_gpu failed with code %d" % result)
+
+    def stats(self):
+        s = npp.NovaPBVIStats()
+        result = npp._nova.pomdp_pbvi_get_stats_gpu(self, ct.byref(s))
+        if result != 0:
+            raise RuntimeError("pomdp_pbvi_get_stats_gpu failed with code %d" % result)
+        return {name: getattr(s, name) for name, _ in s._fields_}
+
+    def value(self, b):
+        """ FP64 V(b) and action over the current device alpha set (pomdp_pbvi_value_gpu). """
+        b = np.ascontiguousarray(np.asarray(b, dtype=np.float32).ravel())
+        Vb = ct.c_double(0.0)
+        a = ct.c_uint(0)
+        result = npp._nova.pomdp_pbvi_value_gpu(self.pomdpPtr, self, b.ctypes.data_as(ct.POINTER(ct.c_float)),
+                                                ct.byref(Vb), ct.byref(a))
+        if result != 0:
+            raise RuntimeError("pomdp_pbvi_value_gpu failed with code %d" % result)
+        return Vb.value, a.value
+
+    def solve(self):
+        """ Solve the POMDP; returns the POMDPAlphaVectors policy. """
+        policy = pav.POMDPAlphaVectors()
+        result = npp._nova.pomdp_pbvi_execute_gpu(self.pomdpPtr, self, policy)
+        if result != 0:
+            print("Failed to execute the 'nova' library's GPU POMDP solver.")
+            raise Exception()
+        return policy
+
+    def get_policy(self):
+        policy = pav.POMDPAlphaVectors()
+        result = npp._nova.pomdp_pbvi_get_policy_gpu(self.pomdpPtr, self, policy)
+        if result != 0:
+            raise RuntimeError("pomdp_pbvi_get_policy_gpu failed with code %d" % result)
+        return policy
+
+    def __str__(self):
+        return "currentHorizon: %i\n\nnumThreads: %i\n\n" % (self.currentHorizon, self.numThreads)

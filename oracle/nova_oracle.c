@@ -1,0 +1,540 @@
+/*
+ * nova-gb300 ORACLE -- test infrastructure only.
+ *
+ * A plain-C restatement of kylewray/nova's CPU algorithms for the hot path,
+ * used as the parity checker by tests/, __graft_entry__.smoke() and the CPU
+ * baseline leg of bench.py. Nothing in the product library links or calls it.
+ *
+ * Parity is pinned: tests/test_oracle.py checks every function here bit for
+ * bit against fixtures produced by the reference itself (its CPU sources
+ * compiled by oracle/Makefile into oracle/_ref, run by
+ * tests/golden/make_golden.py) and against the reference's unit-test values.
+ *
+ * Arithmetic is IEEE FP32 with every product and sum rounded separately
+ * (build with -ffp-contract=off): the reference is built by g++ for x86-64
+ * without FMA, and these functions reproduce its operation order exactly.
+ */
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+
+#define ORACLE_FLT_MIN (-1e+10f)   /* nova's FLT_MIN, include/nova/constants.h:34 */
+
+/* ------------------------------------------------------------------------ */
+/* PBVI, the reference's own loop structure                                  */
+/* ------------------------------------------------------------------------ */
+
+/* Follows pomdp_pbvi_update_compute_best_alpha_cpu, pomdp_pbvi_cpu.cpp:37-103.
+ * bestj persists across observations (it is declared outside the o loop) and
+ * is never assigned when no alpha beats the -1e10 sentinel; here it starts
+ * at 0 in every call (the product library does the same). */
+static void pbvi_best_alpha(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned rG, unsigned rz, float gamma,
+                            const int *S, const float *T, const float *O, const int *Z, const float *B,
+                            const float *Gamma, unsigned i, unsigned a, float *alpha, unsigned *bestjState,
+                            unsigned *jstarOut) {
+    unsigned bestj = 0;
+    (void)bestjState;
+    for (unsigned o = 0; o < z; o++) {
+        float bestValue = ORACLE_FLT_MIN;
+        for (unsigned j = 0; j < rG; j++) {
+            float value = 0.0f;
+            for (unsigned k = 0; k < rz; k++) {
+                int s = Z[i * rz + k];
+                if (s < 0) break;
+                float Vtk = 0.0f;
+                for (unsigned l = 0; l < ns; l++) {
+                    int sp = S[s * m * ns + a * ns + l];
+                    if (sp < 0) break;
+                    float ot = O[a * n * z + sp * z + o] * T[s * m * ns + a * ns + l];
+                    float p = ot * Gamma[j * n + sp];
+                    Vtk = Vtk + p;
+                }
+                Vtk = Vtk * gamma;
+                float q = Vtk * B[i * rz + k];
+                value = value + q;
+            }
+            if (value > bestValue) {
+                bestj = j;
+                bestValue = value;
+            }
+        }
+        if (jstarOut) jstarOut[o] = bestj;
+        for (unsigned s = 0; s < n; s++) {
+            float Vtk = 0.0f;
+            for (unsigned l = 0; l < ns; l++) {
+                int sp = S[s * m * ns + a * ns + l];
+                if (sp < 0) break;
+                float ot = O[a * n * z + sp * z + o] * T[s * m * ns + a * ns + l];
+                float p = ot * Gamma[bestj * n + sp];
+                Vtk = Vtk + p;
+            }
+            Vtk = Vtk * gamma;
+            alpha[s] = alpha[s] + Vtk;
+        }
+    }
+}
+
+/* Follows pomdp_pbvi_update_step_cpu, pomdp_pbvi_cpu.cpp:106-162: one backup
+ * of beliefs [i0, i1) against Gamma (r rows), writing GammaPrime rows and
+ * pi. Rows/actions of beliefs that no action improves are left untouched. */
+void oracle_pbvi_update_range(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz, float gamma,
+                              const int *S, const float *T, const float *O, const float *R, const int *Z,
+                              const float *B, const float *Gamma, float *GammaPrime, unsigned *pi, unsigned i0,
+                              unsigned i1) {
+    float *alpha = (float *)malloc(sizeof(float) * n);
+    unsigned bestjState = 0;
+    for (unsigned i = i0; i < i1; i++) {
+        float bestValue = ORACLE_FLT_MIN;
+        for (unsigned a = 0; a < m; a++) {
+            for (unsigned s = 0; s < n; s++) alpha[s] = R[s * m + a];
+            pbvi_best_alpha(n, ns, m, z, r, rz, gamma, S, T, O, Z, B, Gamma, i, a, alpha, &bestjState, NULL);
+            float value = 0.0f;
+            for (unsigned k = 0; k < rz; k++) {
+                int s = Z[i * rz + k];
+                if (s < 0) break;
+                float q = alpha[s] * B[i * rz + k];
+                value = value + q;
+            }
+            if (value > bestValue) {
+                memcpy(&GammaPrime[i * n], alpha, n * sizeof(float));
+                pi[i] = a;
+                bestValue = value;
+            }
+        }
+    }
+    free(alpha);
+}
+
+void oracle_pbvi_update(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz, float gamma,
+                        const int *S, const float *T, const float *O, const float *R, const int *Z, const float *B,
+                        const float *Gamma, float *GammaPrime, unsigned *pi) {
+    oracle_pbvi_update_range(n, ns, m, z, r, rz, gamma, S, T, O, R, Z, B, Gamma, GammaPrime, pi, 0, r);
+}
+
+/* Follows pomdp_pbvi_execute_cpu / update_cpu / get_policy_cpu
+ * (pomdp_pbvi_cpu.cpp:186-300): horizon steps with the parity swap; the
+ * result (GammaOut, piOut) is what get_policy returns. */
+void oracle_pbvi_solve(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz, float gamma,
+                       unsigned horizon, const int *S, const float *T, const float *O, const float *R, const int *Z,
+                       const float *B, const float *GammaInitial, float *GammaOut, unsigned *piOut) {
+    float *G = (float *)malloc(sizeof(float) * r * n);
+    float *Gp = (float *)malloc(sizeof(float) * r * n);
+    memcpy(G, GammaInitial, sizeof(float) * r * n);
+    memcpy(Gp, GammaInitial, sizeof(float) * r * n);
+    for (unsigned i = 0; i < r; i++) piOut[i] = 0;
+    for (unsigned h = 0; h < horizon; h++) {
+        if (h % 2 == 0) oracle_pbvi_update(n, ns, m, z, r, rz, gamma, S, T, O, R, Z, B, G, Gp, piOut);
+        else oracle_pbvi_update(n, ns, m, z, r, rz, gamma, S, T, O, R, Z, B, Gp, G, piOut);
+    }
+    memcpy(GammaOut, (horizon % 2 == 0) ? G : Gp, sizeof(float) * r * n);
+    free(G);
+    free(Gp);
+}
+
+/* ------------------------------------------------------------------------ */
+/* PBVI, factored: the same values, projection hoisted out of the belief loop */
+/* ------------------------------------------------------------------------ */
+
+/* Proj[j][s] = gamma * sum_l fl(O*T) * Gamma[j][S] for fixed (a, o), exactly
+ * the Vtk of pomdp_pbvi_cpu.cpp:66-74 and :89-98 (same operands, same order),
+ * so scores built from it are bit-identical to the loop form above. Cost is
+ * O(r*n*ns + r*r*rz) per (a, o) instead of O(r*r*rz*ns + n*ns). */
+static void project(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned rG, float gamma, const int *S,
+                    const float *T, const float *O, const float *Gamma, unsigned a, unsigned o, float *Proj) {
+    for (unsigned j = 0; j < rG; j++) {
+        const float *g = Gamma + (size_t)j * n;
+        float *out = Proj + (size_t)j * n;
+        for (unsigned s = 0; s < n; s++) {
+            float Vtk = 0.0f;
+            for (unsigned l = 0; l < ns; l++) {
+                int sp = S[s * m * ns + a * ns + l];
+                if (sp < 0) break;
+                float ot = O[a * n * z + sp * z + o] * T[s * m * ns + a * ns + l];
+                float p = ot * g[sp];
+                Vtk = Vtk + p;
+            }
+            out[s] = Vtk * gamma;
+        }
+    }
+}
+
+/* Bit-identical to oracle_pbvi_update for beliefs [i0, i1); jstarOut
+ * (optional, [r][m][z]) receives the chosen alpha per (belief, action, obs). */
+void oracle_pbvi_update_factored(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz,
+                                 float gamma, const int *S, const float *T, const float *O, const float *R,
+                                 const int *Z, const float *B, const float *Gamma, float *GammaPrime, unsigned *pi,
+                                 unsigned i0, unsigned i1, unsigned *jstarOut) {
+    float *Proj = (float *)malloc(sizeof(float) * (size_t)r * n);
+    float *alphaAll = (float *)malloc(sizeof(float) * (size_t)(i1 - i0) * m * n);
+    unsigned *jbest = (unsigned *)malloc(sizeof(unsigned) * (size_t)(i1 - i0) * m);
+    for (unsigned i = i0; i < i1; i++)
+        for (unsigned a = 0; a < m; a++) {
+            float *alpha = alphaAll + ((size_t)(i - i0) * m + a) * n;
+            for (unsigned s = 0; s < n; s++) alpha[s] = R[s * m + a];
+        }
+    /* bestj is carried across observations within one (i, a), from 0. */
+    for (size_t t = 0; t < (size_t)(i1 - i0) * m; t++) jbest[t] = 0;
+    for (unsigned a = 0; a < m; a++) {
+        for (unsigned o = 0; o < z; o++) {
+            project(n, ns, m, z, r, gamma, S, T, O, Gamma, a, o, Proj);
+            for (unsigned i = i0; i < i1; i++) {
+                float bestValue = ORACLE_FLT_MIN;
+                unsigned bestj = jbest[(size_t)(i - i0) * m + a];
+                for (unsigned j = 0; j < r; j++) {
+                    const float *pj = Proj + (size_t)j * n;
+                    float value = 0.0f;
+                    for (unsigned k = 0; k < rz; k++) {
+                        int s = Z[i * rz + k];
+                        if (s < 0) break;
+                        float q = pj[s] * B[i * rz + k];
+                        value = value + q;
+                    }
+                    if (value > bestValue) {
+                        bestj = j;
+                        bestValue = value;
+                    }
+                }
+                jbest[(size_t)(i - i0) * m + a] = bestj;
+                if (jstarOut) jstarOut[((size_t)i * m + a) * z + o] = bestj;
+                float *alpha = alphaAll + ((size_t)(i - i0) * m + a) * n;
+                const float *pj = Proj + (size_t)bestj * n;
+                for (unsigned s = 0; s < n; s++) alpha[s] = alpha[s] + pj[s];
+            }
+        }
+    }
+    for (unsigned i = i0; i < i1; i++) {
+        float bestValue = ORACLE_FLT_MIN;
+        for (unsigned a = 0; a < m; a++) {
+            const float *alpha = alphaAll + ((size_t)(i - i0) * m + a) * n;
+            float value = 0.0f;
+            for (unsigned k = 0; k < rz; k++) {
+                int s = Z[i * rz + k];
+                if (s < 0) break;
+                float q = alpha[s] * B[i * rz + k];
+                value = value + q;
+            }
+            if (value > bestValue) {
+                memcpy(&GammaPrime[(size_t)i * n], alpha, n * sizeof(float));
+                pi[i] = a;
+                bestValue = value;
+            }
+        }
+    }
+    free(Proj);
+    free(alphaAll);
+    free(jbest);
+}
+
+/* FP64 restatement of the same backup (factored form, all arithmetic in
+ * double, same argmax rules): the reference solution for V(b0) error. */
+void oracle_pbvi_update_f64(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz, double gamma,
+                            const int *S, const double *T, const double *O, const double *R, const int *Z,
+                            const double *B, const double *Gamma, double *GammaPrime, unsigned *pi) {
+    double *Proj = (double *)malloc(sizeof(double) * (size_t)r * n);
+    double *alphaAll = (double *)malloc(sizeof(double) * (size_t)r * m * n);
+    for (unsigned i = 0; i < r; i++)
+        for (unsigned a = 0; a < m; a++)
+            for (unsigned s = 0; s < n; s++) alphaAll[((size_t)i * m + a) * n + s] = R[s * m + a];
+    for (unsigned a = 0; a < m; a++) {
+        for (unsigned o = 0; o < z; o++) {
+            for (unsigned j = 0; j < r; j++) {
+                for (unsigned s = 0; s < n; s++) {
+                    double v = 0.0;
+                    for (unsigned l = 0; l < ns; l++) {
+                        int sp = S[s * m * ns + a * ns + l];
+                        if (sp < 0) break;
+                        v += O[a * n * z + sp * z + o] * T[s * m * ns + a * ns + l] * Gamma[(size_t)j * n + sp];
+                    }
+                    Proj[(size_t)j * n + s] = v * gamma;
+                }
+            }
+            for (unsigned i = 0; i < r; i++) {
+                double bestValue = -1e10;
+                unsigned bestj = 0;
+                for (unsigned j = 0; j < r; j++) {
+                    double value = 0.0;
+                    for (unsigned k = 0; k < rz; k++) {
+                        int s = Z[i * rz + k];
+                        if (s < 0) break;
+                        value += Proj[(size_t)j * n + s] * B[i * rz + k];
+                    }
+                    if (value > bestValue) { bestj = j; bestValue = value; }
+                }
+                double *alpha = alphaAll + ((size_t)i * m + a) * n;
+                for (unsigned s = 0; s < n; s++) alpha[s] += Proj[(size_t)bestj * n + s];
+            }
+        }
+    }
+    for (unsigned i = 0; i < r; i++) {
+        double bestValue = -1e10;
+        for (unsigned a = 0; a < m; a++) {
+            const double *alpha = alphaAll + ((size_t)i * m + a) * n;
+            double value = 0.0;
+            for (unsigned k = 0; k < rz; k++) {
+                int s = Z[i * rz + k];
+                if (s < 0) break;
+                value += alpha[s] * B[i * rz + k];
+            }
+            if (value > bestValue) {
+                memcpy(&GammaPrime[(size_t)i * n], alpha, n * sizeof(double));
+                pi[i] = a;
+                bestValue = value;
+            }
+        }
+    }
+    free(Proj);
+    free(alphaAll);
+}
+
+/* ------------------------------------------------------------------------ */
+/* V(b) (pomdp_alpha_vectors.cpp:52-79)                                       */
+/* ------------------------------------------------------------------------ */
+
+void oracle_alpha_value(unsigned n, unsigned r, const float *Gamma, const unsigned *pi, const float *b, float *Vb,
+                        unsigned *a) {
+    float best = ORACLE_FLT_MIN;
+    unsigned act = 0;
+    for (unsigned i = 0; i < r; i++) {
+        float V = 0.0f;
+        for (unsigned s = 0; s < n; s++) {
+            float p = Gamma[i * n + s] * b[s];
+            V = V + p;
+        }
+        if (best < V) {
+            best = V;
+            act = pi[i];
+        }
+    }
+    *Vb = best;
+    *a = act;
+}
+
+/* ------------------------------------------------------------------------ */
+/* MDP value iteration (mdp_vi_cpu.cpp:36-63, 185-196)                        */
+/* ------------------------------------------------------------------------ */
+
+void oracle_mdp_vi_sweep(unsigned n, unsigned ns, unsigned m, float gamma, const int *S, const float *T,
+                         const float *R, const float *V, float *VPrime, unsigned *pi) {
+    for (unsigned s = 0; s < n; s++) {
+        VPrime[s] = -1e+10f;
+        for (unsigned a = 0; a < m; a++) {
+            float Qsa = R[s * m + a];
+            for (unsigned i = 0; i < ns; i++) {
+                int sp = S[s * m * ns + a * ns + i];
+                if (sp < 0) break;
+                float gt = gamma * T[s * m * ns + a * ns + i];
+                float p = gt * V[sp];
+                Qsa = Qsa + p;
+            }
+            if (a == 0 || Qsa > VPrime[s]) {
+                VPrime[s] = Qsa;
+                pi[s] = a;
+            }
+        }
+    }
+}
+
+/* Sweeps with the parity swap; V/pi out as mdp_vi_get_policy_cpu returns. */
+void oracle_mdp_vi_solve(unsigned n, unsigned ns, unsigned m, float gamma, unsigned horizon, const int *S,
+                         const float *T, const float *R, const float *VInitial, float *VOut, unsigned *piOut) {
+    float *V = (float *)malloc(sizeof(float) * n);
+    float *Vp = (float *)malloc(sizeof(float) * n);
+    for (unsigned s = 0; s < n; s++) {
+        V[s] = VInitial ? VInitial[s] : 0.0f;
+        Vp[s] = V[s];
+        piOut[s] = 0;
+    }
+    for (unsigned h = 0; h < horizon; h++) {
+        if (h % 2 == 0) oracle_mdp_vi_sweep(n, ns, m, gamma, S, T, R, V, Vp, piOut);
+        else oracle_mdp_vi_sweep(n, ns, m, gamma, S, T, R, Vp, V, piOut);
+    }
+    memcpy(VOut, (horizon % 2 == 0) ? V : Vp, sizeof(float) * n);
+    free(V);
+    free(Vp);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Perseus (pomdp_perseus_cpu.cpp:37-461)                                    */
+/* ------------------------------------------------------------------------ */
+
+static float b_dot_alpha(unsigned rz, const int *Z, const float *B, unsigned bIndex, const float *alpha) {
+    float acc = 0.0f;
+    for (unsigned j = 0; j < rz; j++) {
+        int s = Z[bIndex * rz + j];
+        if (s < 0) break;
+        float p = B[bIndex * rz + j] * alpha[s];
+        acc = acc + p;
+    }
+    return acc;
+}
+
+static void compute_Vb(unsigned n, unsigned rz, const int *Z, const float *B, unsigned bIndex, const float *Gamma,
+                       unsigned rGamma, float *Vnb, unsigned *idx) {
+    *Vnb = ORACLE_FLT_MIN;
+    for (unsigned i = 0; i < rGamma; i++) {
+        float d = b_dot_alpha(rz, Z, B, bIndex, &Gamma[i * n]);
+        if (*Vnb < d) {
+            *Vnb = d;
+            *idx = i;
+        }
+    }
+}
+
+/* State of one Perseus solve, laid out like POMDPPerseusCPU. */
+typedef struct {
+    unsigned currentHorizon, rGamma, rGammaPrime, rTilde;
+    unsigned *BTilde;
+    float *Gamma, *GammaPrime;
+    unsigned *pi, *piPrime;
+} OraclePerseus;
+
+/* One update (pomdp_perseus_update_cpu). Returns 9 (NOVA_CONVERGED), 0, or
+ * 11 (out of memory). With an empty V_n the reference's best-alpha index is
+ * unassigned; row 0 is used. */
+int oracle_perseus_update(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz, float gamma,
+                          const int *S, const float *T, const float *O, const float *R, const int *Z, const float *B,
+                          OraclePerseus *per) {
+    float *Gamma, *GammaPrime;
+    unsigned *rGamma, *rGammaPrime, *pi, *piPrime;
+    if (per->currentHorizon % 2 == 0) {
+        Gamma = per->Gamma; GammaPrime = per->GammaPrime; rGamma = &per->rGamma; rGammaPrime = &per->rGammaPrime;
+        pi = per->pi; piPrime = per->piPrime;
+    } else {
+        Gamma = per->GammaPrime; GammaPrime = per->Gamma; rGamma = &per->rGammaPrime; rGammaPrime = &per->rGamma;
+        pi = per->piPrime; piPrime = per->pi;
+    }
+    unsigned bTildeIndex = (unsigned)((float)rand() / (float)RAND_MAX * (float)(per->rTilde));
+    if (bTildeIndex >= r) bTildeIndex = r - 1;
+    unsigned bIndex = per->BTilde[bTildeIndex];
+
+    /* pomdp_perseus_update_step_cpu (:140-180) */
+    float *alpha = (float *)malloc(sizeof(float) * n);
+    float *best = (float *)malloc(sizeof(float) * n);
+    unsigned alphaAction = 0;
+    float bestValue = ORACLE_FLT_MIN;
+    unsigned bestjState = 0;
+    for (unsigned a = 0; a < m; a++) {
+        for (unsigned s = 0; s < n; s++) alpha[s] = R[s * m + a];
+        if (*rGamma == 0) {
+            /* no alpha to maximise over: add the projection of row 0 */
+            for (unsigned o = 0; o < z; o++)
+                for (unsigned s = 0; s < n; s++) {
+                    float Vtk = 0.0f;
+                    for (unsigned l = 0; l < ns; l++) {
+                        int sp = S[s * m * ns + a * ns + l];
+                        if (sp < 0) break;
+                        float ot = O[a * n * z + sp * z + o] * T[s * m * ns + a * ns + l];
+                        float p = ot * Gamma[sp];
+                        Vtk = Vtk + p;
+                    }
+                    Vtk = Vtk * gamma;
+                    alpha[s] = alpha[s] + Vtk;
+                }
+        } else {
+            pbvi_best_alpha(n, ns, m, z, *rGamma, rz, gamma, S, T, O, Z, B, Gamma, bIndex, a, alpha, &bestjState,
+                            NULL);
+        }
+        float value = b_dot_alpha(rz, Z, B, bIndex, alpha);
+        if (value > bestValue) {
+            memcpy(best, alpha, n * sizeof(float));
+            alphaAction = a;
+            bestValue = value;
+        }
+    }
+    float bDotAlpha = b_dot_alpha(rz, Z, B, bIndex, best);
+    float Vnb = 0.0f;
+    unsigned alphaPrimeIndex = 0;
+    compute_Vb(n, rz, Z, B, bIndex, Gamma, *rGamma, &Vnb, &alphaPrimeIndex);
+    if (*rGammaPrime + 1 > r) {
+        free(alpha); free(best);
+        return 11;
+    }
+    if (bDotAlpha >= Vnb) {
+        memcpy(&GammaPrime[(*rGammaPrime) * n], best, n * sizeof(float));
+        piPrime[*rGammaPrime] = alphaAction;
+    } else {
+        memcpy(&GammaPrime[(*rGammaPrime) * n], &Gamma[alphaPrimeIndex * n], n * sizeof(float));
+        piPrime[*rGammaPrime] = pi[alphaPrimeIndex];
+    }
+    (*rGammaPrime)++;
+    free(alpha);
+    free(best);
+
+    per->rTilde = 0;
+    for (unsigned i = 0; i < r; i++) {
+        unsigned action = 0;
+        float vn = 0.0f, vn1 = 0.0f;
+        compute_Vb(n, rz, Z, B, i, Gamma, *rGamma, &vn, &action);
+        compute_Vb(n, rz, Z, B, i, GammaPrime, *rGammaPrime, &vn1, &action);
+        if (vn1 < vn) per->BTilde[per->rTilde++] = i;
+    }
+    if (per->rTilde == 0) {
+        per->currentHorizon++;
+        *rGamma = 0;
+        per->rTilde = r;
+        for (unsigned i = 0; i < r; i++) per->BTilde[i] = i;
+        return 9;
+    }
+    return 0;
+}
+
+/* Full solve (pomdp_perseus_execute_cpu, :222-270). The caller seeds
+ * srand() first. Writes the policy rows into GammaOut (capacity r*n) and
+ * returns the number of rows, or -1 on error. */
+int oracle_perseus_solve(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz, float gamma,
+                         unsigned horizon, const int *S, const float *T, const float *O, const float *R, const int *Z,
+                         const float *B, const float *GammaInitial, float *GammaOut, unsigned *piOut) {
+    OraclePerseus per;
+    per.currentHorizon = 0; per.rGamma = 0; per.rGammaPrime = 0; per.rTilde = r;
+    per.BTilde = (unsigned *)malloc(sizeof(unsigned) * r);
+    per.Gamma = (float *)malloc(sizeof(float) * r * n);
+    per.GammaPrime = (float *)malloc(sizeof(float) * r * n);
+    per.pi = (unsigned *)calloc(r, sizeof(unsigned));
+    per.piPrime = (unsigned *)calloc(r, sizeof(unsigned));
+    memcpy(per.Gamma, GammaInitial, sizeof(float) * r * n);
+    memcpy(per.GammaPrime, GammaInitial, sizeof(float) * r * n);
+    for (unsigned i = 0; i < r; i++) per.BTilde[i] = i;
+    int rows = 0;
+    while (per.currentHorizon < horizon) {
+        int rc = 0;
+        while (rc != 9) {
+            rc = oracle_perseus_update(n, ns, m, z, r, rz, gamma, S, T, O, R, Z, B, &per);
+            if (rc != 9 && rc != 0) { rows = -1; goto done; }
+        }
+    }
+    if (per.currentHorizon % 2 == 0) {
+        rows = (int)per.rGamma;
+        memcpy(GammaOut, per.Gamma, sizeof(float) * per.rGamma * n);
+        memcpy(piOut, per.pi, sizeof(unsigned) * per.rGamma);
+    } else {
+        rows = (int)per.rGammaPrime;
+        memcpy(GammaOut, per.GammaPrime, sizeof(float) * per.rGammaPrime * n);
+        memcpy(piOut, per.piPrime, sizeof(unsigned) * per.rGammaPrime);
+    }
+done:
+    free(per.BTilde); free(per.Gamma); free(per.GammaPrime); free(per.pi); free(per.piPrime);
+    return rows;
+}
+
+void oracle_srand(unsigned seed) { srand(seed); }
+
+/* One (belief, action) pair of nova's backup in the loop form (the inner
+ * body of pomdp_pbvi_update_step_cpu, pomdp_pbvi_cpu.cpp:128-145): fills
+ * alphaOut (n) and returns its value at the belief. A belief backup is m of
+ * these plus an argmax; the CPU baseline times them in bounded samples. */
+float oracle_pbvi_belief_action(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz,
+                                float gamma, const int *S, const float *T, const float *O, const float *R,
+                                const int *Z, const float *B, const float *Gamma, unsigned i, unsigned a,
+                                float *alphaOut) {
+    unsigned state = 0;
+    for (unsigned s = 0; s < n; s++) alphaOut[s] = R[s * m + a];
+    pbvi_best_alpha(n, ns, m, z, r, rz, gamma, S, T, O, Z, B, Gamma, i, a, alphaOut, &state, NULL);
+    float value = 0.0f;
+    for (unsigned k = 0; k < rz; k++) {
+        int s = Z[i * rz + k];
+        if (s < 0) break;
+        float q = alphaOut[s] * B[i * rz + k];
+        value = value + q;
+    }
+    return value;
+}

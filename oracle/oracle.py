@@ -1,0 +1,375 @@
+"""ORACLE -- test infrastructure only (tests/, __graft_entry__.smoke(), the CPU
+baseline leg of bench.py). The product library never imports this module.
+
+Two CPU implementations of nova's hot-path algorithms, behind one numpy API:
+
+* the C restatement in oracle/nova_oracle.c (`liboracle`), built by
+  oracle/Makefile wherever the tests run (x86 here, Arm on the GPU machine);
+* the reference itself: nova's own CPU sources compiled by `make -C oracle ref`
+  into oracle/_ref/libnova_ref.so, called through nova's own C API
+  (pomdp_pbvi_execute_cpu, mdp_vi_execute_cpu, ...). It exists only where the
+  reference sources are present; `ref_available()` says whether it loaded.
+
+The restatement is pinned bit for bit to the reference by tests/test_oracle.py
+and by the fixtures in tests/golden/ (made by tests/golden/make_golden.py from
+the reference).
+"""
+import ctypes as ct
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libnova_ref.so")
+REF_DIR = os.environ.get("NOVA_REFERENCE_DIR", "/root/reference")
+
+_F = ct.POINTER(ct.c_float)
+_I = ct.POINTER(ct.c_int)
+_U = ct.POINTER(ct.c_uint)
+_D = ct.POINTER(ct.c_double)
+
+_oracle = None
+_ref = None
+
+
+def build(with_ref=None):
+    """Build liboracle.so (and the reference library when its sources exist)."""
+    if with_ref is None:
+        with_ref = os.path.isdir(os.path.join(REF_DIR, "src"))
+    target = "ref" if with_ref else "all"
+    subprocess.run(["make", "-s", "-C", HERE, target, "REF_DIR=" + REF_DIR], check=True,
+                   stdout=subprocess.DEVNULL)
+
+
+def lib():
+    global _oracle
+    if _oracle is None:
+        if not os.path.exists(ORACLE_SO) or os.path.getmtime(ORACLE_SO) < os.path.getmtime(
+                os.path.join(HERE, "nova_oracle.c")):
+            build(with_ref=False)
+        _oracle = ct.CDLL(ORACLE_SO)
+        L = _oracle
+        L.oracle_pbvi_update_range.argtypes = [ct.c_uint] * 6 + [ct.c_float, _I, _F, _F, _F, _I, _F, _F, _F, _U,
+                                                                 ct.c_uint, ct.c_uint]
+        L.oracle_pbvi_update.argtypes = [ct.c_uint] * 6 + [ct.c_float, _I, _F, _F, _F, _I, _F, _F, _F, _U]
+        L.oracle_pbvi_solve.argtypes = [ct.c_uint] * 6 + [ct.c_float, ct.c_uint, _I, _F, _F, _F, _I, _F, _F, _F, _U]
+        L.oracle_pbvi_update_factored.argtypes = [ct.c_uint] * 6 + [ct.c_float, _I, _F, _F, _F, _I, _F, _F, _F, _U,
+                                                                    ct.c_uint, ct.c_uint, _U]
+        L.oracle_pbvi_update_f64.argtypes = [ct.c_uint] * 6 + [ct.c_double, _I, _D, _D, _D, _I, _D, _D, _D, _U]
+        L.oracle_alpha_value.argtypes = [ct.c_uint, ct.c_uint, _F, _U, _F, _F, _U]
+        L.oracle_mdp_vi_sweep.argtypes = [ct.c_uint, ct.c_uint, ct.c_uint, ct.c_float, _I, _F, _F, _F, _F, _U]
+        L.oracle_mdp_vi_solve.argtypes = [ct.c_uint, ct.c_uint, ct.c_uint, ct.c_float, ct.c_uint, _I, _F, _F, _F,
+                                          _F, _U]
+        L.oracle_perseus_solve.argtypes = [ct.c_uint] * 6 + [ct.c_float, ct.c_uint, _I, _F, _F, _F, _I, _F, _F,
+                                                             _F, _U]
+        L.oracle_perseus_solve.restype = ct.c_int
+        L.oracle_srand.argtypes = [ct.c_uint]
+        L.oracle_pbvi_belief_action.argtypes = [ct.c_uint] * 6 + [ct.c_float, _I, _F, _F, _F, _I, _F, _F, ct.c_uint,
+                                                                  ct.c_uint, _F]
+        L.oracle_pbvi_belief_action.restype = ct.c_float
+    return _oracle
+
+
+def ref_available():
+    return ref_lib() is not None
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_SO) and os.path.isdir(os.path.join(REF_DIR, "src")):
+            try:
+                build(with_ref=True)
+            except Exception:
+                return None
+        if not os.path.exists(REF_SO):
+            return None
+        _ref = ct.CDLL(REF_SO)
+    return _ref
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+def _arrays(model):
+    S = np.ascontiguousarray(model["S"], dtype=np.int32)
+    T = np.ascontiguousarray(model["T"], dtype=np.float32)
+    O = np.ascontiguousarray(model["O"], dtype=np.float32)
+    R = np.ascontiguousarray(model["R"], dtype=np.float32)
+    Z = np.ascontiguousarray(model["Z"], dtype=np.int32)
+    B = np.ascontiguousarray(model["B"], dtype=np.float32)
+    return S, T, O, R, Z, B
+
+
+def _dims(model):
+    return (model["n"], model["ns"], model["m"], model["z"], model["r"], model["rz"])
+
+
+# ---------------------------------------------------------------------------
+# Restatement (liboracle)
+# ---------------------------------------------------------------------------
+
+def pbvi_solve(model, horizon=None, GammaInitial=None):
+    """nova's PBVI CPU solve (loop form); returns (Gamma [r,n], pi [r])."""
+    L = lib()
+    S, T, O, R, Z, B = _arrays(model)
+    n, ns, m, z, r, rz = _dims(model)
+    G0 = np.ascontiguousarray(model["GammaInitial"] if GammaInitial is None else GammaInitial, dtype=np.float32)
+    Gout = np.empty((r, n), np.float32)
+    pi = np.empty(r, np.uint32)
+    L.oracle_pbvi_solve(n, ns, m, z, r, rz, model["gamma"], model["horizon"] if horizon is None else horizon,
+                        _p(S, _I), _p(T, _F), _p(O, _F), _p(R, _F), _p(Z, _I), _p(B, _F), _p(G0, _F),
+                        _p(Gout, _F), _p(pi, _U))
+    return Gout, pi
+
+
+def pbvi_update(model, Gamma, GammaPrime, pi, i0=0, i1=None, factored=True, jstar=None):
+    """One backup of beliefs [i0, i1) in place into GammaPrime/pi (bit-identical forms)."""
+    L = lib()
+    S, T, O, R, Z, B = _arrays(model)
+    n, ns, m, z, r, rz = _dims(model)
+    i1 = r if i1 is None else i1
+    G = np.ascontiguousarray(Gamma, dtype=np.float32)
+    assert GammaPrime.dtype == np.float32 and GammaPrime.flags.c_contiguous
+    assert pi.dtype == np.uint32 and pi.flags.c_contiguous
+    if factored:
+        js = _p(jstar, _U) if jstar is not None else None
+        L.oracle_pbvi_update_factored(n, ns, m, z, r, rz, model["gamma"], _p(S, _I), _p(T, _F), _p(O, _F),
+                                      _p(R, _F), _p(Z, _I), _p(B, _F), _p(G, _F), _p(GammaPrime, _F), _p(pi, _U),
+                                      i0, i1, js)
+    else:
+        L.oracle_pbvi_update_range(n, ns, m, z, r, rz, model["gamma"], _p(S, _I), _p(T, _F), _p(O, _F),
+                                   _p(R, _F), _p(Z, _I), _p(B, _F), _p(G, _F), _p(GammaPrime, _F), _p(pi, _U),
+                                   i0, i1)
+
+
+def pbvi_update_f64(model, Gamma):
+    """FP64 backup of every belief; returns (GammaPrime [r,n] float64, pi)."""
+    L = lib()
+    n, ns, m, z, r, rz = _dims(model)
+    S = np.ascontiguousarray(model["S"], dtype=np.int32)
+    Z = np.ascontiguousarray(model["Z"], dtype=np.int32)
+    T, O, R, B = (np.ascontiguousarray(model[k], dtype=np.float64) for k in ("T", "O", "R", "B"))
+    G = np.ascontiguousarray(Gamma, dtype=np.float64)
+    Gp = G.copy()
+    pi = np.zeros(r, np.uint32)
+    L.oracle_pbvi_update_f64(n, ns, m, z, r, rz, float(model["gamma"]), _p(S, _I), _p(T, _D), _p(O, _D),
+                             _p(R, _D), _p(Z, _I), _p(B, _D), _p(G, _D), _p(Gp, _D), _p(pi, _U))
+    return Gp, pi
+
+
+def pbvi_belief_action_sampler(model, Gamma):
+    """A callable (i, a) -> value running one (belief, action) pair of nova's
+    loop-form backup against Gamma (the unit the CPU baseline times). The
+    ctypes call releases the GIL, so threads run in parallel."""
+    L = lib()
+    S, T, O, R, Z, B = _arrays(model)
+    n, ns, m, z, r, rz = _dims(model)
+    G = np.ascontiguousarray(Gamma, dtype=np.float32)
+    keep = (S, T, O, R, Z, B, G)
+    ptrs = (_p(S, _I), _p(T, _F), _p(O, _F), _p(R, _F), _p(Z, _I), _p(B, _F), _p(G, _F))
+
+    def run(i, a):
+        out = np.empty(n, np.float32)
+        _ = keep
+        return L.oracle_pbvi_belief_action(n, ns, m, z, G.shape[0], rz, model["gamma"], *ptrs, i, a,
+                                           _p(out, _F))
+    return run
+
+
+def alpha_value(Gamma, pi, b):
+    """nova's V(b) (FP32, strict '<'); returns (V, action)."""
+    L = lib()
+    G = np.ascontiguousarray(Gamma, dtype=np.float32)
+    p = np.ascontiguousarray(pi, dtype=np.uint32)
+    bb = np.ascontiguousarray(b, dtype=np.float32)
+    V = ct.c_float(0)
+    a = ct.c_uint(0)
+    L.oracle_alpha_value(G.shape[1], G.shape[0], _p(G, _F), _p(p, _U), _p(bb, _F), ct.byref(V), ct.byref(a))
+    return V.value, a.value
+
+
+def mdp_vi_solve(model, horizon=None, VInitial=None):
+    """nova's VI CPU solve; returns (V [n], pi [n])."""
+    L = lib()
+    S = np.ascontiguousarray(model["S"], dtype=np.int32)
+    T = np.ascontiguousarray(model["T"], dtype=np.float32)
+    R = np.ascontiguousarray(model["R"], dtype=np.float32)
+    n = model["n"]
+    V = np.empty(n, np.float32)
+    pi = np.empty(n, np.uint32)
+    V0 = None if VInitial is None else np.ascontiguousarray(VInitial, dtype=np.float32)
+    L.oracle_mdp_vi_solve(n, model["ns"], model["m"], model["gamma"],
+                          model["horizon"] if horizon is None else horizon, _p(S, _I), _p(T, _F), _p(R, _F),
+                          _p(V0, _F) if V0 is not None else None, _p(V, _F), _p(pi, _U))
+    return V, pi
+
+
+def mdp_vi_sweep(model, V):
+    """One Bellman sweep; returns (V', pi)."""
+    L = lib()
+    S = np.ascontiguousarray(model["S"], dtype=np.int32)
+    T = np.ascontiguousarray(model["T"], dtype=np.float32)
+    R = np.ascontiguousarray(model["R"], dtype=np.float32)
+    Vin = np.ascontiguousarray(V, dtype=np.float32)
+    n = model["n"]
+    Vp = np.empty(n, np.float32)
+    pi = np.empty(n, np.uint32)
+    L.oracle_mdp_vi_sweep(n, model["ns"], model["m"], model["gamma"], _p(S, _I), _p(T, _F), _p(R, _F),
+                          _p(Vin, _F), _p(Vp, _F), _p(pi, _U))
+    return Vp, pi
+
+
+def perseus_solve(model, seed, horizon=None, GammaInitial=None):
+    """nova's Perseus CPU solve after srand(seed); returns (Gamma rows, pi)."""
+    L = lib()
+    S, T, O, R, Z, B = _arrays(model)
+    n, ns, m, z, r, rz = _dims(model)
+    G0 = np.ascontiguousarray(model["GammaInitial"] if GammaInitial is None else GammaInitial, dtype=np.float32)
+    Gout = np.zeros((r, n), np.float32)
+    pi = np.zeros(r, np.uint32)
+    L.oracle_srand(seed)
+    rows = L.oracle_perseus_solve(n, ns, m, z, r, rz, model["gamma"], model["horizon"] if horizon is None else horizon,
+                                  _p(S, _I), _p(T, _F), _p(O, _F), _p(R, _F), _p(Z, _I), _p(B, _F), _p(G0, _F),
+                                  _p(Gout, _F), _p(pi, _U))
+    if rows < 0:
+        raise RuntimeError("oracle Perseus failed")
+    return Gout[:rows].copy(), pi[:rows].copy()
+
+
+# ---------------------------------------------------------------------------
+# The reference itself (oracle/_ref/libnova_ref.so), through nova's C API
+# ---------------------------------------------------------------------------
+
+class _RefPOMDP(ct.Structure):
+    _fields_ = [("n", ct.c_uint), ("ns", ct.c_uint), ("m", ct.c_uint), ("z", ct.c_uint), ("r", ct.c_uint),
+                ("rz", ct.c_uint), ("gamma", ct.c_float), ("horizon", ct.c_uint),
+                ("S", _I), ("T", _F), ("O", _F), ("R", _F), ("Z", _I), ("B", _F),
+                ("d_S", _I), ("d_T", _F), ("d_O", _F), ("d_R", _F), ("d_Z", _I), ("d_B", _F)]
+
+
+class _RefMDP(ct.Structure):
+    _fields_ = [("n", ct.c_uint), ("ns", ct.c_uint), ("m", ct.c_uint), ("gamma", ct.c_float),
+                ("horizon", ct.c_uint), ("epsilon", ct.c_float), ("s0", ct.c_uint), ("ng", ct.c_uint),
+                ("goals", _U), ("S", _I), ("T", _F), ("R", _F), ("d_goals", _U), ("d_S", _I), ("d_T", _F),
+                ("d_R", _F)]
+
+
+class _RefAlpha(ct.Structure):
+    _fields_ = [("n", ct.c_uint), ("m", ct.c_uint), ("r", ct.c_uint), ("Gamma", _F), ("pi", _U)]
+
+
+class _RefVF(ct.Structure):
+    _fields_ = [("n", ct.c_uint), ("m", ct.c_uint), ("r", ct.c_uint), ("S", _U), ("V", _F), ("pi", _U)]
+
+
+class _RefPBVI(ct.Structure):
+    _fields_ = [("GammaInitial", _F), ("currentHorizon", ct.c_uint), ("Gamma", _F), ("GammaPrime", _F), ("pi", _U)]
+
+
+class _RefPerseus(ct.Structure):
+    _fields_ = [("GammaInitial", _F), ("currentHorizon", ct.c_uint), ("rGamma", ct.c_uint),
+                ("rGammaPrime", ct.c_uint), ("rTilde", ct.c_uint), ("BTilde", _U), ("Gamma", _F),
+                ("GammaPrime", _F), ("pi", _U), ("piPrime", _U)]
+
+
+class _RefVI(ct.Structure):
+    _fields_ = [("VInitial", _F), ("currentHorizon", ct.c_uint), ("V", _F), ("VPrime", _F), ("pi", _U)]
+
+
+def _ref_pomdp(model, keep):
+    S, T, O, R, Z, B = _arrays(model)
+    keep.extend([S, T, O, R, Z, B])
+    p = _RefPOMDP()
+    p.n, p.ns, p.m, p.z, p.r, p.rz = _dims(model)
+    p.gamma = model["gamma"]
+    p.horizon = model["horizon"]
+    p.S, p.T, p.O, p.R, p.Z, p.B = _p(S, _I), _p(T, _F), _p(O, _F), _p(R, _F), _p(Z, _I), _p(B, _F)
+    return p
+
+
+def ref_pbvi_solve(model, horizon=None):
+    """Reference pomdp_pbvi_execute_cpu; returns (Gamma, pi)."""
+    L = ref_lib()
+    keep = []
+    p = _ref_pomdp(model, keep)
+    if horizon is not None:
+        p.horizon = horizon
+    G0 = np.ascontiguousarray(model["GammaInitial"], dtype=np.float32)
+    alg = _RefPBVI()
+    alg.GammaInitial = _p(G0, _F)
+    pol = _RefAlpha()
+    rc = L.pomdp_pbvi_execute_cpu(ct.byref(p), ct.byref(alg), ct.byref(pol))
+    if rc != 0:
+        raise RuntimeError("reference pomdp_pbvi_execute_cpu failed: %d" % rc)
+    G = np.ctypeslib.as_array(pol.Gamma, shape=(pol.r * pol.n,)).reshape(pol.r, pol.n).copy()
+    pi = np.ctypeslib.as_array(pol.pi, shape=(pol.r,)).copy().astype(np.uint32)
+    L.pomdp_alpha_vectors_uninitialize(ct.byref(pol))
+    return G, pi
+
+
+def ref_perseus_solve(model, seed, horizon=None):
+    """Reference pomdp_perseus_execute_cpu after srand(seed); returns (Gamma, pi)."""
+    L = ref_lib()
+    keep = []
+    p = _ref_pomdp(model, keep)
+    if horizon is not None:
+        p.horizon = horizon
+    G0 = np.ascontiguousarray(model["GammaInitial"], dtype=np.float32)
+    alg = _RefPerseus()
+    alg.GammaInitial = _p(G0, _F)
+    pol = _RefAlpha()
+    lib().oracle_srand(seed)  # same libc rand() state as the reference library
+    rc = L.pomdp_perseus_execute_cpu(ct.byref(p), ct.byref(alg), ct.byref(pol))
+    if rc != 0:
+        raise RuntimeError("reference pomdp_perseus_execute_cpu failed: %d" % rc)
+    G = np.ctypeslib.as_array(pol.Gamma, shape=(pol.r * pol.n,)).reshape(pol.r, pol.n).copy()
+    pi = np.ctypeslib.as_array(pol.pi, shape=(pol.r,)).copy().astype(np.uint32)
+    L.pomdp_alpha_vectors_uninitialize(ct.byref(pol))
+    return G, pi
+
+
+def ref_mdp_vi_solve(model, horizon=None, VInitial=None):
+    """Reference mdp_vi_execute_cpu; returns (V, pi)."""
+    L = ref_lib()
+    S = np.ascontiguousarray(model["S"], dtype=np.int32)
+    T = np.ascontiguousarray(model["T"], dtype=np.float32)
+    R = np.ascontiguousarray(model["R"], dtype=np.float32)
+    mdp = _RefMDP()
+    mdp.n, mdp.ns, mdp.m = model["n"], model["ns"], model["m"]
+    mdp.gamma = model["gamma"]
+    mdp.horizon = model["horizon"] if horizon is None else horizon
+    mdp.S, mdp.T, mdp.R = _p(S, _I), _p(T, _F), _p(R, _F)
+    alg = _RefVI()
+    V0 = None
+    if VInitial is not None:
+        V0 = np.ascontiguousarray(VInitial, dtype=np.float32)
+        alg.VInitial = _p(V0, _F)
+    pol = _RefVF()
+    rc = L.mdp_vi_execute_cpu(ct.byref(mdp), ct.byref(alg), ct.byref(pol))
+    if rc != 0:
+        raise RuntimeError("reference mdp_vi_execute_cpu failed: %d" % rc)
+    V = np.ctypeslib.as_array(pol.V, shape=(pol.n,)).copy()
+    pi = np.ctypeslib.as_array(pol.pi, shape=(pol.n,)).copy().astype(np.uint32)
+    L.mdp_value_function_uninitialize(ct.byref(pol))
+    return V, pi
+
+
+def ref_alpha_value(Gamma, pi, b):
+    """Reference pomdp_alpha_vectors_value_and_action; returns (V, action)."""
+    L = ref_lib()
+    G = np.ascontiguousarray(Gamma, dtype=np.float32)
+    p = np.ascontiguousarray(pi, dtype=np.uint32)
+    bb = np.ascontiguousarray(b, dtype=np.float32)
+    pol = _RefAlpha()
+    pol.n, pol.m, pol.r = G.shape[1], int(p.max()) + 1, G.shape[0]
+    pol.Gamma, pol.pi = _p(G, _F), _p(p, _U)
+    V = ct.c_float(0)
+    a = ct.c_uint(0)
+    rc = L.pomdp_alpha_vectors_value_and_action(ct.byref(pol), _p(bb, _F), ct.byref(V), ct.byref(a))
+    if rc != 0:
+        raise RuntimeError("reference value_and_action failed: %d" % rc)
+    return V.value, a.value

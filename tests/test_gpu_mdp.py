@@ -1,0 +1,107 @@
+"""MDP value iteration on the GB300 through the C ABI."""
+import ctypes as ct
+
+import numpy as np
+import pytest
+
+from conftest import load_golden, bits, MDP_GOLDENS
+from oracle import oracle as orc
+from nova_gb300 import synth
+from nova_gb300.mdp import MDP
+from nova_gb300.mdp_vi import MDPValueIterationGPU, MDPValueIterationCPU
+from nova_gb300 import nova_mdp_vi as nmvi
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_solve(model, VInitial=None):
+    m = MDP.from_arrays(model)
+    m.initialize_gpu()
+    alg = MDPValueIterationGPU(m, Vinitial=VInitial if VInitial is not None else np.zeros(model["n"], np.float32))
+    pol = alg.solve()
+    return pol.V_array(), pol.pi_array()
+
+
+@pytest.mark.parametrize("name", MDP_GOLDENS)
+def test_execute_gpu_matches_reference(name):
+    g = load_golden(name)
+    V, pi = gpu_solve(g, g.get("VInitial"))
+    np.testing.assert_array_equal(bits(V), bits(g["out_V"]))
+    np.testing.assert_array_equal(pi, g["out_pi"])
+
+
+@pytest.mark.parametrize("name", MDP_GOLDENS)
+def test_execute_cpu_api_matches_reference(name):
+    g = load_golden(name)
+    m = MDP.from_arrays(g)
+    alg = MDPValueIterationCPU(m, Vinitial=g.get("VInitial", np.zeros(g["n"], np.float32)))
+    pol = alg.solve()
+    np.testing.assert_array_equal(bits(pol.V_array()), bits(g["out_V"]))
+    np.testing.assert_array_equal(pol.pi_array(), g["out_pi"])
+
+
+def three_state():
+    S = np.array([[[0, 1], [0, -1]], [[1, -1], [2, -1]], [[2, -1], [2, -1]]], np.int32)
+    T = np.array([[[0.5, 0.5], [1.0, 0.0]], [[1.0, 0.0], [1.0, 0.0]], [[1.0, 0.0], [1.0, 0.0]]], np.float32)
+    R = np.array([[-1.0, -2.0], [-1.0, -2.0], [0.0, 0.0]], np.float32)
+    return dict(n=3, ns=2, m=2, gamma=0.9, horizon=5, S=S, T=T, R=R, goals=np.array([2], np.uint32))
+
+
+def test_reference_unit_values_gpu():
+    # mdp_vi_gpu_tests.cpp:226-228 (V = -3.303775, -2.0, 0.0; pi = 0, 1)
+    V, pi = gpu_solve(three_state())
+    np.testing.assert_allclose(V, [-3.303775, -2.0, 0.0], atol=1e-5)
+    assert pi[0] == 0 and pi[1] == 1
+    simple = dict(n=1, ns=1, m=1, gamma=0.9, horizon=3, S=np.array([[[0]]], np.int32),
+                  T=np.array([[[1.0]]], np.float32), R=np.array([[1.0]], np.float32))
+    V, pi = gpu_solve(simple)
+    assert abs(V[0] - 2.71) < 1e-5
+
+
+def test_update_cpu_per_step_host_arrays():
+    """mdp_vi_cpu_tests.cpp:444-479: V and V' after each update, read from the struct."""
+    mm = three_state()
+    m = MDP.from_arrays(mm)
+    alg = MDPValueIterationCPU(m, Vinitial=np.zeros(3, np.float32))
+    f = nmvi._nova
+    expect = [([0, 0, 0], [-1, -1, 0]), ([-1.9, -1.9, 0], [-1, -1, 0]), ([-1.9, -1.9, 0], [-2.71, -2.0, 0])]
+    for h, (v, vp) in enumerate(expect):
+        assert f.mdp_vi_update_cpu(alg.mdpPtr, alg) == 0
+        assert alg.currentHorizon == h + 1
+        np.testing.assert_allclose([alg.V[i] for i in range(3)], v, atol=1e-5)
+        np.testing.assert_allclose([alg.Vprime[i] for i in range(3)], vp, atol=1e-5)
+
+
+def test_update_gpu_matches_oracle_sweeps():
+    md = synth.random_mdp(n=5000, m=7, ns=9, gamma=0.97, horizon=30, seed=4)
+    m = MDP.from_arrays(md)
+    m.initialize_gpu()
+    alg = MDPValueIterationGPU(m, Vinitial=np.zeros(md["n"], np.float32))
+    V = np.zeros(md["n"], np.float32)
+    for h in range(5):
+        assert nmvi._nova.mdp_vi_update_gpu(alg.mdpPtr, alg) == 0
+        Vn, pi = orc.mdp_vi_sweep(md, V)
+        resid = ct.c_double(0)
+        assert nmvi._nova.mdp_vi_residual_gpu(alg.mdpPtr, alg, ct.byref(resid)) == 0
+        assert resid.value == np.max(np.abs(Vn.astype(np.float64) - V.astype(np.float64)))
+        V = Vn
+    from nova_gb300 import mdp_value_function as mvf
+    pol = mvf.MDPValueFunction()
+    assert nmvi._nova.mdp_vi_get_policy_gpu(alg.mdpPtr, alg, pol) == 0
+    np.testing.assert_array_equal(bits(pol.V_array()), bits(V))
+    np.testing.assert_array_equal(pol.pi_array(), pi)
+
+
+@pytest.mark.parametrize("m_actions", [1, 3, 8, 33])
+def test_action_counts_and_until_converged(m_actions):
+    md = synth.random_mdp(n=777, m=m_actions, ns=4, gamma=0.9, horizon=400, seed=m_actions)
+    m = MDP.from_arrays(md)
+    m.initialize_gpu()
+    alg = MDPValueIterationGPU(m, Vinitial=np.zeros(md["n"], np.float32))
+    pol, sweeps, resid = alg.solve_until_converged(tol=1e-4, maxSweeps=400)
+    assert resid < 1e-4 and 0 < sweeps < 400
+    V, pi = orc.mdp_vi_solve(md, horizon=sweeps, VInitial=np.zeros(md["n"], np.float32))
+    np.testing.assert_array_equal(bits(pol.V_array()), bits(V))
+    np.testing.assert_array_equal(pol.pi_array(), pi)
+    Vprev, _ = orc.mdp_vi_solve(md, horizon=sweeps - 1, VInitial=np.zeros(md["n"], np.float32))
+    assert resid == np.max(np.abs(V.astype(np.float64) - Vprev.astype(np.float64)))

@@ -1,0 +1,119 @@
+"""PBVI on the GB300 through the C ABI (nova_gb300's ctypes wrapper):
+bit-identical to the reference's outputs (golden fixtures) and to the oracle."""
+import ctypes as ct
+
+import numpy as np
+import pytest
+
+from conftest import load_golden, bits, PBVI_GOLDENS
+from oracle import oracle as orc
+from nova_gb300 import synth
+from nova_gb300.pomdp import POMDP
+from nova_gb300.pomdp_pbvi import POMDPPBVIGPU, POMDPPBVICPU
+from nova_gb300 import nova_pomdp_pbvi as npp
+
+pytestmark = pytest.mark.gpu
+
+MODES = [npp.SCORING_EXACT, npp.SCORING_BF16]
+
+
+def solve_gpu(model, mode, horizon=None):
+    p = POMDP.from_arrays(dict(model, horizon=model["horizon"] if horizon is None else horizon))
+    p.initialize_gpu()
+    alg = POMDPPBVIGPU(p, GammaInitial=model["GammaInitial"])
+    alg.set_scoring(mode)
+    pol = alg.solve()
+    return pol.gamma_array(), pol.pi_array()
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("name", PBVI_GOLDENS)
+def test_execute_gpu_matches_reference(name, mode):
+    g = load_golden(name)
+    G, pi = solve_gpu(g, mode)
+    np.testing.assert_array_equal(bits(G), bits(g["out_Gamma"]))
+    np.testing.assert_array_equal(pi, g["out_pi"])
+
+
+@pytest.mark.parametrize("name", ["pbvi_n64_h5", "pbvi_ragged", "pbvi_tiger"])
+def test_execute_cpu_api_matches_reference(name):
+    g = load_golden(name)
+    p = POMDP.from_arrays(g)
+    alg = POMDPPBVICPU(p, GammaInitial=g["GammaInitial"])
+    pol = alg.solve()
+    np.testing.assert_array_equal(bits(pol.gamma_array()), bits(g["out_Gamma"]))
+    np.testing.assert_array_equal(pol.pi_array(), g["out_pi"])
+
+
+def test_stepwise_update_cpu_api_host_arrays():
+    """update_cpu leaves valid host arrays after every call (the reference's contract)."""
+    g = load_golden("pbvi_ragged")
+    p = POMDP.from_arrays(g)
+    alg = POMDPPBVICPU(p, GammaInitial=g["GammaInitial"])
+    G = g["GammaInitial"].copy()
+    Gp = G.copy()
+    pi = np.zeros(g["r"], np.uint32)
+    r, n = g["r"], g["n"]
+    for h in range(4):
+        alg.update()
+        if h % 2 == 0:
+            orc.pbvi_update(g, G, Gp, pi)
+            host = np.ctypeslib.as_array(alg.GammaPrime, shape=(r * n,)).reshape(r, n)
+            np.testing.assert_array_equal(bits(host), bits(Gp))
+        else:
+            orc.pbvi_update(g, Gp, G, pi)
+            host = np.ctypeslib.as_array(alg.Gamma, shape=(r * n,)).reshape(r, n)
+            np.testing.assert_array_equal(bits(host), bits(G))
+        np.testing.assert_array_equal(np.ctypeslib.as_array(alg.pi, shape=(r,)), pi)
+        assert alg.currentHorizon == h + 1
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("seed", [7, 8])
+def test_random_models_stepwise_against_oracle(seed, mode):
+    """Uneven shapes (n, r, z not multiples of any tile) step by step."""
+    m = synth.random_pomdp(n=173, m=5, z=11, ns=9, r=301, rz=13, gamma=0.93, horizon=6, seed=seed)
+    p = POMDP.from_arrays(m)
+    p.initialize_gpu()
+    alg = POMDPPBVIGPU(p, GammaInitial=m["GammaInitial"])
+    alg.set_scoring(mode)
+    G = m["GammaInitial"].copy()
+    Gp = G.copy()
+    pi = np.zeros(m["r"], np.uint32)
+    for h in range(m["horizon"]):
+        alg.update()
+        if h % 2 == 0:
+            orc.pbvi_update(m, G, Gp, pi)
+        else:
+            orc.pbvi_update(m, Gp, G, pi)
+        pol = alg.get_policy()
+        ref = Gp if h % 2 == 0 else G
+        np.testing.assert_array_equal(bits(pol.gamma_array()), bits(ref))
+        np.testing.assert_array_equal(pol.pi_array(), pi)
+
+
+def test_value_gpu_fp64():
+    g = load_golden("pbvi_n64_h100")
+    p = POMDP.from_arrays(g)
+    p.initialize_gpu()
+    alg = POMDPPBVIGPU(p, GammaInitial=g["GammaInitial"])
+    for _ in range(g["horizon"]):
+        alg.update()
+    b0 = synth.dense_belief(g, 0)
+    V, a = alg.value(b0)
+    G = g["out_Gamma"].astype(np.float64)
+    vals = G @ b0.astype(np.float64)
+    assert abs(V - vals.max()) <= 1e-12 * max(1.0, abs(vals.max()))
+    assert a == g["out_pi"][int(np.argmax(vals))]
+    Vf, af = orc.alpha_value(g["out_Gamma"], g["out_pi"], b0)
+    assert abs(V - Vf) < 1e-5 * max(1.0, abs(Vf))
+
+
+def test_numthreads_must_be_multiple_of_32():
+    g = load_golden("pbvi_tiger")
+    p = POMDP.from_arrays(g)
+    p.initialize_gpu()
+    alg = POMDPPBVIGPU(p, numThreads=33, GammaInitial=g["GammaInitial"])
+    from nova_gb300 import pomdp_alpha_vectors as pav
+    pol = pav.POMDPAlphaVectors()
+    assert npp._nova.pomdp_pbvi_execute_gpu(alg.pomdpPtr, alg, pol) == 2  # NOVA_ERROR_INVALID_CUDA_PARAM

@@ -1,0 +1,142 @@
+"""Host-side behaviour of the C library that needs no GPU: model allocation,
+argument validation and error codes, policy containers, belief update,
+fault injection wiring."""
+import ctypes as ct
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from oracle import oracle as orc
+from nova_gb300 import _lib
+from nova_gb300.pomdp import POMDP
+from nova_gb300.mdp import MDP
+from nova_gb300 import nova_pomdp as npm, nova_pomdp_pbvi as npp, nova_mdp_vi as nmvi
+from nova_gb300 import pomdp_alpha_vectors as pav, mdp_value_function as mvf
+from nova_gb300 import nova_pomdp_perseus as npper
+
+L = _lib.load()
+NOVA_SUCCESS, INVALID_DATA, INVALID_CUDA_PARAM, DEVICE_MALLOC = 0, 1, 2, 3
+
+
+def test_pomdp_initialize_validation_and_defaults():
+    p = npm.NovaPOMDP()
+    assert L.pomdp_initialize_cpu(ct.byref(p), 0, 1, 1, 1, 1, 1, 0.9, 1) == INVALID_DATA
+    assert L.pomdp_initialize_cpu(ct.byref(p), 2, 3, 1, 1, 1, 1, 0.9, 1) == INVALID_DATA  # n < ns
+    assert L.pomdp_initialize_cpu(ct.byref(p), 3, 2, 2, 2, 4, 2, 1.5, 1) == INVALID_DATA  # gamma > 1
+    assert L.pomdp_initialize_cpu(ct.byref(p), 3, 2, 2, 2, 4, 2, 0.9, 10) == NOVA_SUCCESS
+    assert (p.n, p.ns, p.m, p.z, p.r, p.rz, p.horizon) == (3, 2, 2, 2, 4, 2, 10)
+    assert all(p.S[i] == -1 for i in range(3 * 2 * 2)) and all(p.T[i] == 0.0 for i in range(12))
+    assert all(p.Z[i] == 0 for i in range(8))
+    assert not p.d_S and not p.d_B
+    # a second initialize on allocated arrays is rejected (pomdp_model_cpu.cpp:37-38)
+    assert L.pomdp_initialize_cpu(ct.byref(p), 3, 2, 2, 2, 4, 2, 0.9, 10) == INVALID_DATA
+    assert L.pomdp_uninitialize_cpu(ct.byref(p)) == NOVA_SUCCESS
+    assert not p.S and p.n == 0
+
+
+def test_mdp_initialize_validation():
+    m = nmvi.mdp.MDP()
+    assert L.mdp_initialize_cpu(ct.byref(m), 4, 2, 2, 0.9, 5, 0.001, 4, 0) == INVALID_DATA  # s0 >= n
+    assert L.mdp_initialize_cpu(ct.byref(m), 4, 2, 2, 0.9, 5, 0.001, 0, 1) == NOVA_SUCCESS
+    assert m.goals and m.goals[0] == 0
+    assert L.mdp_uninitialize_cpu(ct.byref(m)) == NOVA_SUCCESS
+
+
+def test_alpha_vectors_reference_values_through_library():
+    # pomdp_alpha_vectors_tests.cpp:35-89, through pomdp_alpha_vectors_value_and_action
+    pol = pav.POMDPAlphaVectors()
+    assert L.pomdp_alpha_vectors_initialize(pol, 2, 2, 2) == NOVA_SUCCESS
+    for k, v in enumerate([1.0, 0.0, 0.0, 1.0]):
+        pol.Gamma[k] = v
+    pol.pi[0], pol.pi[1] = 1, 0
+    for b, v, a in (([0.0, 1.0], 1.0, 0), ([1.0, 0.0], 1.0, 1), ([0.25, 0.75], 0.75, 0), ([0.67, 0.33], 0.67, 1)):
+        V, act = pol.value_and_action(np.array(b, np.float32))
+        assert abs(V - v) < 1e-5 and act == a
+    # initialize refuses a policy that already holds arrays
+    assert L.pomdp_alpha_vectors_initialize(pol, 2, 2, 2) == INVALID_DATA
+
+
+def test_alpha_value_matches_oracle_on_fixture():
+    g = load_golden("pbvi_n64_h100")
+    pol = pav.POMDPAlphaVectors()
+    assert L.pomdp_alpha_vectors_initialize(pol, g["n"], g["m"], g["r"]) == NOVA_SUCCESS
+    G = np.ascontiguousarray(g["out_Gamma"])
+    ct.memmove(pol.Gamma, G.ctypes.data, G.nbytes)
+    ct.memmove(pol.pi, g["out_pi"].ctypes.data, g["out_pi"].nbytes)
+    for i in range(5):
+        b = np.zeros(g["n"], np.float32)
+        b[g["Z"][i]] = g["B"][i]
+        assert pol.value_and_action(b) == orc.alpha_value(G, g["out_pi"], b)
+
+
+def test_value_function_dense_and_sparse():
+    vf = mvf.MDPValueFunction()
+    assert L.mdp_value_function_initialize(vf, 5, 2, 0) == NOVA_SUCCESS
+    assert not vf.S and vf.V and vf.pi
+    vf2 = mvf.MDPValueFunction()
+    assert L.mdp_value_function_initialize(vf2, 5, 2, 3) == NOVA_SUCCESS
+    assert vf2.S and vf2.r == 3
+    assert L.mdp_value_function_initialize(vf2, 5, 2, 3) == INVALID_DATA
+
+
+def test_belief_update_and_raw_beliefs():
+    g = load_golden("pbvi_tiger")
+    p = POMDP.from_arrays(g)
+    b = np.array([0.5, 0.5], np.float32)
+    bp = p.belief_update(b, 0, 0)
+    # numpy restatement of pomdp_model_cpu.cpp:89-137 for the tiger 'listen' action
+    expect = np.zeros(2, np.float32)
+    for s in range(2):
+        for l in range(g["ns"]):
+            sp = g["S"][s, 0, l]
+            if sp < 0:
+                break
+            expect[sp] += g["T"][s, 0, l] * b[s]
+    expect *= g["O"][0, :, 0]
+    expect /= expect.sum()
+    np.testing.assert_allclose(bp, expect, rtol=1e-6)
+    r0, rz0 = p.r, p.rz
+    Bnew = np.array([[0.3, 0.7], [1.0, 0.0]], np.float32)
+    assert L.pomdp_add_new_raw_beliefs_cpu(p, 2, Bnew.ctypes.data_as(ct.POINTER(ct.c_float))) == NOVA_SUCCESS
+    assert p.r == r0 + 2 and p.rz == max(rz0, 2)
+    assert [p.Z[(r0) * p.rz + k] for k in range(2)] == [0, 1]
+    assert p.Z[(r0 + 1) * p.rz + 1] == -1
+
+
+def test_execute_validation_before_any_device_work():
+    g = load_golden("pbvi_tiger")
+    p = POMDP.from_arrays(g)
+    pol = pav.POMDPAlphaVectors()
+    alg = npp.NovaPOMDPPBVIGPU()
+    # no device model: invalid data
+    assert L.pomdp_pbvi_execute_gpu(p, ct.byref(alg), pol) == INVALID_DATA
+    # with (never dereferenced) device pointers and a bad numThreads: invalid CUDA parameter
+    fake = ct.cast(ct.c_void_p(0x1000), ct.POINTER(ct.c_int))
+    fakef = ct.cast(ct.c_void_p(0x1000), ct.POINTER(ct.c_float))
+    p.d_S, p.d_Z = fake, fake
+    p.d_T, p.d_O, p.d_R, p.d_B = fakef, fakef, fakef, fakef
+    G0 = (ct.c_float * (g["r"] * g["n"]))()
+    alg.GammaInitial = ct.cast(G0, ct.POINTER(ct.c_float))
+    alg.numThreads = 48
+    assert L.pomdp_pbvi_execute_gpu(p, ct.byref(alg), pol) == INVALID_CUDA_PARAM
+    p.d_S = p.d_Z = ct.POINTER(ct.c_int)()
+    p.d_T = p.d_O = p.d_R = p.d_B = ct.POINTER(ct.c_float)()
+    # CPU-buffer entry points validate too
+    cpu = npp.NovaPOMDPPBVICPU()
+    assert L.pomdp_pbvi_execute_cpu(p, ct.byref(cpu), pol) == INVALID_DATA  # no GammaInitial
+    per = npper.NovaPOMDPPerseusCPU()
+    assert L.pomdp_perseus_execute_cpu(p, ct.byref(per), pol) == INVALID_DATA
+    assert L.pomdp_pbvi_update_gpu(p, ct.byref(alg)) == INVALID_DATA
+    assert L.mdp_vi_execute_gpu(None, None, None) == INVALID_DATA
+
+
+def test_fault_injection_hook_is_wired():
+    """An armed allocation fault fails the next device allocation on the host,
+    before CUDA is called, with the reference's error code."""
+    g = load_golden("pbvi_tiger")
+    p = POMDP.from_arrays(g)
+    L.nova_gb300_inject_fault(1, 1)
+    assert L.pomdp_initialize_successors_gpu(p) == DEVICE_MALLOC
+    assert not p.d_S
+    L.nova_gb300_inject_fault(0, 0)
