@@ -22,12 +22,20 @@ NOVA_NS_BEGIN
  *      reference's operation order (bit-identical to pomdp_pbvi_cpu.cpp:37-103).
  *  NOVA_SCORING_BF16: tcgen05 tensor cores score all alphas in BF16 (FP32
  *      accumulate); every alpha within a proven error bound of the best is
- *      re-scored in the exact FP32 order, so the argmax equals EXACT's. */
+ *      re-scored in the exact FP32 order, so the argmax equals EXACT's.
+ *  NOVA_SCORING_FP16: as BF16 with FP16 operands (per-belief power-of-two
+ *      scaling keeps them in range); the tighter rounding leaves fewer
+ *      alphas to re-score. */
 #define NOVA_SCORING_EXACT 0u
 #define NOVA_SCORING_BF16  1u
+#define NOVA_SCORING_FP16  2u
 
 /* Select the scoring mode used by later pomdp_pbvi_update_gpu calls on this
- * solver struct (default NOVA_SCORING_BF16 where the shapes allow it). */
+ * solver struct. The default is NOVA_SCORING_FP16: at n=4096 with 8192
+ * alphas its proven margin leaves ~2% of rows to the exact scan, BF16's
+ * ~93%. Tensor-core scoring engages once 32 distinct alphas exist and the
+ * projection table fits in device memory; otherwise rows are scored exactly.
+ * All modes give bit-identical results. */
 NOVA_API int pomdp_pbvi_set_scoring_gpu(POMDPPBVIGPU *pbvi, unsigned int mode);
 
 /* Per-update counters of the last pomdp_pbvi_update_gpu on this solver. */
@@ -38,7 +46,7 @@ typedef struct NovaPBVIStats {
     unsigned int rowsMultiCand;    /* (belief, action, obs) rows re-scored exactly */
     unsigned int rowsOverflow;     /* (belief, action) pairs scored exactly in full */
     unsigned int candidates;       /* total alphas re-scored in FP32 */
-    float msDedup, msScore, msRescore, msAssemble, msTotal;
+    float msDedup, msProject, msScore, msRescore, msActions, msAssemble, msTotal;
     float msGemm;                  /* the tensor-core scoring kernel alone (0 if not run) */
     unsigned int launches;         /* kernels this library launched for the update */
 } NovaPBVIStats;

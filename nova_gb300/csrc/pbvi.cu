@@ -449,6 +449,244 @@ __global__ void argmax_fp64_kernel(const double *__restrict__ v, unsigned rows, 
 }
 
 // ---------------------------------------------------------------------------
+// Projection table: Proj[a][o][s][u] = gamma * sum_l fl(O(a,S,o) T(s,a,l)) * alpha_u(S)
+// ---------------------------------------------------------------------------
+
+// The reference recomputes this value (its Vtk after `Vtk *= gamma`,
+// pomdp_pbvi_cpu.cpp:66-74 and :89-98) for every belief that has s in its
+// support; it depends only on (a, o, s, alpha), so it is computed once per
+// update here, with the same operands in the same order (bit-identical).
+// One block per (a, s); threads over alphas read the transposed alpha table
+// coalesced, the coefficients of the row are broadcast from shared memory,
+// and each observation's values are written as one coalesced row segment.
+template <int ZC>
+__global__ void __launch_bounds__(256) proj_kernel(DevModel md, const unsigned *__restrict__ succLen,
+                                                   const float *__restrict__ C1, const float *__restrict__ Gt,
+                                                   size_t gtCols, unsigned nU, float *__restrict__ Proj,
+                                                   size_t uCols) {
+    extern __shared__ float smem[];
+    float *Cs = smem;                                           // [ns][ZC]
+    int *Ss = reinterpret_cast<int *>(Cs + (size_t)md.ns * ZC); // [ns]
+    const unsigned a = blockIdx.x / md.n, s = blockIdx.x % md.n;
+    const unsigned L = succLen[(size_t)s * md.m + a];
+    const float gamma = md.gamma;
+    for (unsigned e = threadIdx.x; e < L; e += blockDim.x) Ss[e] = md.S[((size_t)s * md.m + a) * md.ns + e];
+    for (unsigned o0 = 0; o0 < md.z; o0 += ZC) {
+        __syncthreads();
+        const float *crow = C1 + (((size_t)a * md.n + s) * md.ns) * md.z + o0;
+        for (unsigned e = threadIdx.x; e < L * ZC; e += blockDim.x) {
+            const unsigned l = e / ZC, q = e % ZC;
+            Cs[e] = (o0 + q < md.z) ? crow[(size_t)l * md.z + q] : 0.0f;
+        }
+        __syncthreads();
+        const unsigned zc = min((unsigned)ZC, md.z - o0);
+        float *out = Proj + (((size_t)a * md.z + o0) * md.n + s) * uCols;
+        const size_t oStride = (size_t)md.n * uCols;
+        // Two alphas per thread (u and u + blockDim) share every coefficient read.
+        for (unsigned u0 = 0; u0 < nU; u0 += 2 * blockDim.x) {
+            const unsigned ua = u0 + threadIdx.x, ub = ua + blockDim.x;
+            const bool va = ua < nU, vb = ub < nU;
+            float acc0[ZC], acc1[ZC];
+#pragma unroll
+            for (int q = 0; q < ZC; q++) { acc0[q] = 0.0f; acc1[q] = 0.0f; }
+            for (unsigned l = 0; l < L; l++) {
+                const float *grow = Gt + (size_t)Ss[l] * gtCols;
+                const float g0 = va ? grow[ua] : 0.0f;
+                const float g1 = vb ? grow[ub] : 0.0f;
+                const float4 *c4 = reinterpret_cast<const float4 *>(Cs + l * ZC);
+#pragma unroll
+                for (int q4 = 0; q4 < ZC / 4; q4++) {
+                    const float4 c = c4[q4];
+                    acc0[4 * q4 + 0] = fadd(acc0[4 * q4 + 0], fmul(c.x, g0));
+                    acc1[4 * q4 + 0] = fadd(acc1[4 * q4 + 0], fmul(c.x, g1));
+                    acc0[4 * q4 + 1] = fadd(acc0[4 * q4 + 1], fmul(c.y, g0));
+                    acc1[4 * q4 + 1] = fadd(acc1[4 * q4 + 1], fmul(c.y, g1));
+                    acc0[4 * q4 + 2] = fadd(acc0[4 * q4 + 2], fmul(c.z, g0));
+                    acc1[4 * q4 + 2] = fadd(acc1[4 * q4 + 2], fmul(c.z, g1));
+                    acc0[4 * q4 + 3] = fadd(acc0[4 * q4 + 3], fmul(c.w, g0));
+                    acc1[4 * q4 + 3] = fadd(acc1[4 * q4 + 3], fmul(c.w, g1));
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < ZC; q++) {
+                if ((unsigned)q < zc) {
+                    if (va) out[(size_t)q * oStride + ua] = fmul(acc0[q], gamma);
+                    if (vb) out[(size_t)q * oStride + ub] = fmul(acc1[q], gamma);
+                }
+            }
+        }
+    }
+}
+
+// Exact scan of whole (a*z+o, belief) rows over the unique alphas using the
+// projection table: value(u) = sum_k fl(Proj[ao][s_k][u] * B[i,k]) in
+// support order (pomdp_pbvi_cpu.cpp:50-83), argmax with the lowest index on
+// ties and the -1e10 sentinel. One block per row. The alphas are scanned in
+// column chunks [u0, u1) so that the (a, o) slice being read stays in L2
+// while the rows of that (a, o) (consecutive in the list) use it; a chunk
+// after the first merges with the running best of the earlier ones, which
+// hold lower indices (so ties keep the earlier alpha).
+__global__ void __launch_bounds__(256) scan_rows_kernel(DevModel md, const unsigned *__restrict__ suppLen,
+                                                        const float *__restrict__ Proj, size_t uCols, unsigned u0,
+                                                        unsigned u1, const unsigned *__restrict__ rowList,
+                                                        unsigned nRows, float *__restrict__ runV,
+                                                        unsigned *__restrict__ runU, int first) {
+    extern __shared__ float sh[];
+    float *bk = sh;                                              // [rz]
+    unsigned *sk = reinterpret_cast<unsigned *>(sh + md.rz);     // [rz]
+    __shared__ float redV[8];
+    __shared__ unsigned redU[8];
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (unsigned w = blockIdx.x; w < nRows; w += gridDim.x) {
+        const unsigned row = rowList ? rowList[w] : w;
+        const unsigned ao = row / md.r, i = row % md.r;
+        const unsigned Li = suppLen[i];
+        __syncthreads();
+        for (unsigned k = threadIdx.x; k < Li; k += blockDim.x) {
+            bk[k] = md.B[(size_t)i * md.rz + k];
+            sk[k] = (unsigned)md.Z[(size_t)i * md.rz + k];
+        }
+        __syncthreads();
+        const float *P = Proj + (size_t)ao * md.n * uCols;
+        float best = NOVA_FLT_MIN;
+        unsigned bu = kNone;
+        for (unsigned u = u0 + threadIdx.x; u < u1; u += blockDim.x) {
+            float v = 0.0f;
+            for (unsigned k = 0; k < Li; k++) v = fadd(v, fmul(__ldg(P + (size_t)sk[k] * uCols + u), bk[k]));
+            if (v > best) { best = v; bu = u; }
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            const float v2 = __shfl_xor_sync(0xffffffffu, best, off);
+            const unsigned u2 = __shfl_xor_sync(0xffffffffu, bu, off);
+            if (u2 != kNone && (bu == kNone || better(v2, u2, best, bu))) { best = v2; bu = u2; }
+        }
+        if (lane == 0) { redV[warp] = best; redU[warp] = bu; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (unsigned ww = 1; ww < blockDim.x / 32; ww++)
+                if (redU[ww] != kNone && (bu == kNone || better(redV[ww], redU[ww], best, bu))) {
+                    best = redV[ww]; bu = redU[ww];
+                }
+            if (!first) {
+                const unsigned pu = runU[w];
+                if (pu != kNone && (bu == kNone || !(best > runV[w]))) { best = runV[w]; bu = pu; }
+            }
+            runV[w] = best;
+            runU[w] = bu;
+        }
+    }
+}
+
+// Final choice of each scanned row (kNone where nothing beat the sentinel).
+__global__ void scan_finish_kernel(DevModel md, const unsigned *__restrict__ rowList, unsigned nRows,
+                                   const unsigned *__restrict__ runU, const unsigned *__restrict__ uniqJ,
+                                   unsigned *__restrict__ ustar, unsigned *__restrict__ jstar) {
+    const unsigned w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nRows) return;
+    const unsigned row = rowList ? rowList[w] : w;
+    const unsigned ao = row / md.r, i = row % md.r;
+    const size_t js = ((size_t)i * md.m + ao / md.z) * md.z + ao % md.z;
+    const unsigned bu = runU[w];
+    ustar[js] = bu;
+    jstar[js] = bu == kNone ? kNone : uniqJ[bu];
+}
+
+// Rows with no alpha above the -1e10 sentinel take the previous
+// observation's choice (0 for the first), as the reference's bestj does.
+__global__ void sentinel_fixup_kernel(DevModel md, const unsigned *__restrict__ uniqJ, unsigned *__restrict__ ustar,
+                                      unsigned *__restrict__ jstar) {
+    const unsigned ia = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ia >= md.r * md.m) return;
+    unsigned prevU = 0, prevJ = 0;
+    for (unsigned o = 0; o < md.z; o++) {
+        const size_t js = (size_t)ia * md.z + o;
+        if (jstar[js] == kNone) {
+            // uniqJ[0] == 0: the first row is always its own representative
+            jstar[js] = prevJ;
+            ustar[js] = prevU;
+        }
+        prevJ = jstar[js];
+        prevU = ustar[js];
+    }
+}
+
+// Action values from the projection table (one warp per (belief, action)):
+// alpha_a(s_k) = R(s_k,a) + sum_o Proj[a][o][s_k][u*], value = sum_k alpha * b_k.
+__global__ void action_value_proj_kernel(DevModel md, const unsigned *__restrict__ suppLen,
+                                         const float *__restrict__ Proj, size_t uCols,
+                                         const unsigned *__restrict__ ustar, float *__restrict__ actVal) {
+    const unsigned warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31;
+    if (warpGlobal >= md.r * md.m) return;
+    const unsigned ia = warpGlobal;
+    const unsigned i = ia / md.m, a = ia % md.m;
+    const unsigned Li = suppLen[i];
+    float value = 0.0f;
+    for (unsigned k0 = 0; k0 < Li; k0 += 32) {
+        const unsigned k = k0 + lane;
+        float p = 0.0f;
+        if (k < Li) {
+            const int s = md.Z[(size_t)i * md.rz + k];
+            float alpha = md.R[(size_t)s * md.m + a];
+            for (unsigned o = 0; o < md.z; o++) {
+                const unsigned u = ustar[(size_t)ia * md.z + o];
+                alpha = fadd(alpha, Proj[(((size_t)a * md.z + o) * md.n + s) * uCols + u]);
+            }
+            p = fmul(alpha, md.B[(size_t)i * md.rz + k]);
+        }
+        const unsigned cnt = min(32u, Li - k0);
+        for (unsigned t = 0; t < cnt; t++) value = fadd(value, __shfl_sync(0xffffffffu, p, t));
+    }
+    if (lane == 0) actVal[ia] = value;
+}
+
+// Assembly from the projection table: Gamma'_i(s) = R(s,a*) + sum_o
+// Proj[a*][o][s][u*_o], the reference's alpha for the best action
+// (pomdp_pbvi_cpu.cpp:128-145, 88-101) with its additions in observation
+// order. One block per belief; each thread issues a chunk of independent
+// loads before the sequential additions.
+__global__ void __launch_bounds__(256) assemble_proj_kernel(DevModel md, const float *__restrict__ Proj, size_t uCols,
+                                                            const unsigned *__restrict__ ustar,
+                                                            const float *__restrict__ actVal, float *__restrict__ dst,
+                                                            unsigned *__restrict__ pi) {
+    const unsigned i = blockIdx.x;
+    __shared__ unsigned bestA;
+    extern __shared__ unsigned ush[];  // [z]
+    if (threadIdx.x == 0) {
+        float best = NOVA_FLT_MIN;
+        unsigned ba = kNone;
+        for (unsigned a = 0; a < md.m; a++) {
+            const float v = actVal[(size_t)i * md.m + a];
+            if (v > best) { best = v; ba = a; }
+        }
+        bestA = ba;
+    }
+    __syncthreads();
+    const unsigned a = bestA;
+    if (a == kNone) return;
+    if (threadIdx.x == 0) pi[i] = a;
+    const unsigned *us = ustar + ((size_t)i * md.m + a) * md.z;
+    for (unsigned o = threadIdx.x; o < md.z; o += blockDim.x) ush[o] = us[o];
+    __syncthreads();
+    const float *P = Proj + (size_t)a * md.z * md.n * uCols;
+    const size_t oStride = (size_t)md.n * uCols;
+    for (unsigned s = threadIdx.x; s < md.n; s += blockDim.x) {
+        float alpha = md.R[(size_t)s * md.m + a];
+        const float *Ps = P + (size_t)s * uCols;
+        unsigned o = 0;
+        for (; o + 8 <= md.z; o += 8) {
+            float v[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) v[q] = __ldg(Ps + (size_t)(o + q) * oStride + ush[o + q]);
+#pragma unroll
+            for (int q = 0; q < 8; q++) alpha = fadd(alpha, v[q]);
+        }
+        for (; o < md.z; o++) alpha = fadd(alpha, __ldg(Ps + (size_t)o * oStride + ush[o]));
+        dst[(size_t)i * md.n + s] = alpha;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // BackupEngine
 // ---------------------------------------------------------------------------
 
@@ -460,6 +698,7 @@ BackupEngine::~BackupEngine() {
     cudaFree(jstar); cudaFree(actVal); cudaFree(partV); cudaFree(partU); cudaFree(items); cudaFree(itemCount);
     cudaFree(dotScratch); cudaFree(bDense); cudaFree(resultA); cudaFree(resultV); cudaFree(rowScratch);
     cudaFree(vnb); cudaFree(vnp1b); cudaFree(btilde);
+    cudaFree(Proj); cudaFree(ustar); cudaFree(scanV); cudaFree(scanU);
     if (eventsMade)
         for (auto &e : ev) cudaEventDestroy(e);
 }
@@ -483,6 +722,7 @@ int BackupEngine::build(const DevModel &model, const char *fn) {
     gtCols = round_up(md.r, 32);
     if ((rc = dev_alloc(&Gt, (size_t)md.n * gtCols, fn, "the transposed alphas")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&jstar, (size_t)md.r * md.m * md.z, fn, "the chosen alphas")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&ustar, (size_t)md.r * md.m * md.z, fn, "the chosen unique alphas")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&actVal, (size_t)md.r * md.m, fn, "the action values")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&items, (size_t)md.r * md.m, fn, "the work list")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&itemCount, 1, fn, "the work list count")) != NOVA_SUCCESS) return rc;
@@ -569,6 +809,75 @@ int BackupEngine::exact_score(const unsigned *itemList, unsigned nItems, unsigne
     return check_launch(fn, "exact belief scoring (merge)");
 }
 
+bool BackupEngine::ensure_proj(unsigned nU) {
+    if (projUnavailable) return false;
+    const size_t cols = round_up(std::max(nU, 1u), 32);
+    const size_t need = (size_t)md.m * md.z * md.n * cols;
+    if (need <= projCap) {
+        projCols = cols;
+        return true;
+    }
+    // Capacity for the largest possible alpha set, allocated once.
+    const size_t full = (size_t)md.m * md.z * md.n * round_up(md.r, 32);
+    size_t freeB = 0, totalB = 0;
+    cudaMemGetInfo(&freeB, &totalB);
+    cudaFree(Proj);
+    Proj = nullptr;
+    projCap = 0;
+    if (full * sizeof(float) + (1ull << 30) > freeB || cudaMalloc(&Proj, full * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError();
+        Proj = nullptr;
+        projUnavailable = true;
+        return false;
+    }
+    projCap = full;
+    projCols = cols;
+    return true;
+}
+
+int BackupEngine::project(unsigned nU, const char *fn) {
+    const size_t smem32 = (size_t)md.ns * 32 * sizeof(float) + md.ns * sizeof(int);
+    const unsigned blocks = md.m * md.n;
+    if (md.z >= 16 && smem32 <= 200 * 1024) {
+        if (smem32 > 48 * 1024)
+            cudaFuncSetAttribute(proj_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32);
+        proj_kernel<32><<<blocks, 256, smem32, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj, projCols);
+    } else {
+        const size_t smem8 = (size_t)md.ns * 8 * sizeof(float) + md.ns * sizeof(int);
+        if (smem8 > 48 * 1024)
+            cudaFuncSetAttribute(proj_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem8);
+        proj_kernel<8><<<blocks, 256, smem8, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj, projCols);
+    }
+    return check_launch(fn, "projection table");
+}
+
+int BackupEngine::scan_rows(const unsigned *rowList, unsigned nRows, unsigned nU, const char *fn) {
+    if (nRows == 0) return NOVA_SUCCESS;
+    int rc;
+    if ((size_t)nRows > scanCap) {
+        cudaFree(scanV); cudaFree(scanU);
+        scanV = nullptr; scanU = nullptr; scanCap = 0;
+        if ((rc = dev_alloc(&scanV, nRows, fn, "the scan maxima")) != NOVA_SUCCESS) return rc;
+        if ((rc = dev_alloc(&scanU, nRows, fn, "the scan arg-maxima")) != NOVA_SUCCESS) return rc;
+        scanCap = nRows;
+    }
+    // Column chunk: one (a, o) slice of at most ~48 MB stays L2-resident.
+    size_t chunk = ((48ull << 20) / ((size_t)md.n * sizeof(float))) / 256 * 256;
+    if (chunk < 256) chunk = 256;
+    const unsigned grid = std::min(nRows, 152u * 16u);
+    for (size_t u0 = 0; u0 < std::max(nU, 1u); u0 += chunk) {
+        const unsigned u1 = (unsigned)std::min<size_t>(nU, u0 + chunk);
+        scan_rows_kernel<<<grid, 256, 2 * md.rz * sizeof(float), stream>>>(md, suppLen, Proj, projCols, (unsigned)u0,
+                                                                          u1, rowList, nRows, scanV, scanU,
+                                                                          u0 == 0 ? 1 : 0);
+        if ((rc = check_launch(fn, "exact row scan")) != NOVA_SUCCESS) return rc;
+    }
+    scan_finish_kernel<<<ceil_div(nRows, 256), 256, 0, stream>>>(md, rowList, nRows, scanU, uniqJ, ustar, jstar);
+    if ((rc = check_launch(fn, "exact row scan (finish)")) != NOVA_SUCCESS) return rc;
+    sentinel_fixup_kernel<<<ceil_div((size_t)md.r * md.m, 256), 256, 0, stream>>>(md, uniqJ, ustar, jstar);
+    return check_launch(fn, "sentinel fixup");
+}
+
 int BackupEngine::fill_items(unsigned first, unsigned count, const char *fn) {
     if (count == 0) return NOVA_SUCCESS;
     iota_items_kernel<<<ceil_div(count, 256), 256, 0, stream>>>(items, count, first);
@@ -587,12 +896,21 @@ int BackupEngine::assemble(const float *src, float *dst, unsigned *pi, int onlyB
         if ((rc = check_launch(fn, "work list")) != NOVA_SUCCESS) return rc;
         itemList = items;
     }
-    action_value_kernel<<<ceil_div((size_t)nItems * 32, 256), 256, 0, stream>>>(md, succLen, suppLen, C3, src, jstar,
-                                                                                itemList, nItems, actVal);
+    if (useProjNow && onlyBelief < 0)
+        action_value_proj_kernel<<<ceil_div((size_t)nItems * 32, 256), 256, 0, stream>>>(md, suppLen, Proj, projCols,
+                                                                                         ustar, actVal);
+    else
+        action_value_kernel<<<ceil_div((size_t)nItems * 32, 256), 256, 0, stream>>>(md, succLen, suppLen, C3, src,
+                                                                                    jstar, itemList, nItems, actVal);
     if ((rc = check_launch(fn, "action values")) != NOVA_SUCCESS) return rc;
-    assemble_kernel<<<nBeliefs, 256, md.z * sizeof(unsigned), stream>>>(md, succLen, C3, src, jstar, actVal,
-                                                                         firstBelief, dst, pi, dstRowOverride,
-                                                                         actionOut);
+    if (onlyBelief < 0) cudaEventRecord(ev[6], stream);
+    if (useProjNow && onlyBelief < 0)
+        assemble_proj_kernel<<<nBeliefs, 256, md.z * sizeof(unsigned), stream>>>(md, Proj, projCols, ustar, actVal,
+                                                                                  dst, pi);
+    else
+        assemble_kernel<<<nBeliefs, 256, md.z * sizeof(unsigned), stream>>>(md, succLen, C3, src, jstar, actVal,
+                                                                             firstBelief, dst, pi, dstRowOverride,
+                                                                             actionOut);
     return check_launch(fn, "alpha assembly");
 }
 
@@ -607,20 +925,33 @@ int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsi
     cudaEventRecord(ev[1], stream);
     const unsigned allItems = md.r * md.m;
     bool done = false;
-    if (scoring == NOVA_SCORING_BF16 && tc_supported(md) && nU >= 2) {
-        unsigned nOverflow = 0;
-        rc = tc_score(*this, src, nU, &nOverflow, fn);
-        if (rc != NOVA_SUCCESS) return rc;
-        cudaEventRecord(ev[2], stream);
-        stats.scoring = NOVA_SCORING_BF16;
-        stats.rowsOverflow = nOverflow;
-        if ((rc = exact_score(items, nOverflow, nU, fn)) != NOVA_SUCCESS) return rc;
-        done = true;
-    }
-    if (!done) {
+    // With room for the projection table every exact score is a 64-term
+    // dot product over it: the plain form scans every row over it, and the
+    // tensor-core form re-scores its near-ties and scans its unresolved rows
+    // with it. Without room, every (belief, action) pair is scored from the
+    // alphas directly.
+    useProjNow = ensure_proj(nU);
+    if (useProjNow && (rc = project(nU, fn)) != NOVA_SUCCESS) return rc;
+    const bool wantTc = (scoring == NOVA_SCORING_BF16 || scoring == NOVA_SCORING_FP16) && useProjNow &&
+                        tc_supported(md) && nU >= kTcMinUnique && !tcUnavailable;
+    if (wantTc && tc == nullptr && tc_build(*this, fn) != NOVA_SUCCESS) tcUnavailable = true;
+    cudaEventRecord(ev[2], stream);
+    if (wantTc && tc != nullptr) {
+        unsigned nRows = 0;
+        const unsigned *rowList = nullptr;
+        if ((rc = tc_score(*this, src, nU, &nRows, &rowList, fn)) != NOVA_SUCCESS) return rc;
+        cudaEventRecord(ev[5], stream);
+        stats.scoring = scoring;
+        stats.rowsOverflow = nRows;
+        if ((rc = scan_rows(rowList, nRows, nU, fn)) != NOVA_SUCCESS) return rc;
+    } else if (useProjNow) {
+        cudaEventRecord(ev[5], stream);
+        stats.scoring = NOVA_SCORING_EXACT;
+        if ((rc = scan_rows(nullptr, md.r * md.m * md.z, nU, fn)) != NOVA_SUCCESS) return rc;
+    } else {
         iota_items_kernel<<<ceil_div(allItems, 256), 256, 0, stream>>>(items, allItems, 0);
         if ((rc = check_launch(fn, "work list")) != NOVA_SUCCESS) return rc;
-        cudaEventRecord(ev[2], stream);
+        cudaEventRecord(ev[5], stream);
         stats.scoring = NOVA_SCORING_EXACT;
         if ((rc = exact_score(items, allItems, nU, fn)) != NOVA_SUCCESS) return rc;
     }
@@ -632,9 +963,11 @@ int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsi
         return sync_device(fn);
     }
     cudaEventElapsedTime(&stats.msDedup, ev[0], ev[1]);
-    cudaEventElapsedTime(&stats.msScore, ev[1], ev[2]);
-    cudaEventElapsedTime(&stats.msRescore, ev[2], ev[3]);
-    cudaEventElapsedTime(&stats.msAssemble, ev[3], ev[4]);
+    cudaEventElapsedTime(&stats.msProject, ev[1], ev[2]);
+    cudaEventElapsedTime(&stats.msScore, ev[2], ev[5]);
+    cudaEventElapsedTime(&stats.msRescore, ev[5], ev[3]);
+    cudaEventElapsedTime(&stats.msActions, ev[3], ev[6]);
+    cudaEventElapsedTime(&stats.msAssemble, ev[6], ev[4]);
     cudaEventElapsedTime(&stats.msTotal, ev[0], ev[4]);
     stats.launches = (unsigned)(launch_count() - launches0);
     const unsigned derr = tc_device_error();
@@ -764,7 +1097,7 @@ extern "C" int pomdp_pbvi_initialize_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi)
         return NOVA_ERROR_INVALID_DATA;
     }
     pbvi->currentHorizon = 0;
-    unsigned scoring = NOVA_SCORING_BF16;
+    unsigned scoring = NOVA_SCORING_FP16;
     {
         std::lock_guard<std::mutex> lock(registry_mutex());
         auto *old = find_workspace<PbviGpuWorkspace>(pbvi);
@@ -883,7 +1216,7 @@ extern "C" int pomdp_pbvi_execute_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi, PO
 }
 
 extern "C" int pomdp_pbvi_set_scoring_gpu(POMDPPBVIGPU *pbvi, unsigned int mode) {
-    if (pbvi == nullptr || (mode != NOVA_SCORING_EXACT && mode != NOVA_SCORING_BF16)) {
+    if (pbvi == nullptr || (mode != NOVA_SCORING_EXACT && mode != NOVA_SCORING_BF16 && mode != NOVA_SCORING_FP16)) {
         NOVA_ERR("pomdp_pbvi_set_scoring_gpu", "Invalid arguments.");
         return NOVA_ERROR_INVALID_DATA;
     }
@@ -970,7 +1303,7 @@ extern "C" int pomdp_pbvi_initialize_cpu(const POMDP *pomdp, POMDPPBVICPU *pbvi)
         return NOVA_ERROR_INVALID_DATA;
     }
     pbvi->currentHorizon = 0;
-    unsigned scoring = NOVA_SCORING_BF16;
+    unsigned scoring = NOVA_SCORING_FP16;
     {
         std::lock_guard<std::mutex> lock(registry_mutex());
         auto *old = find_workspace<PbviCpuWorkspace>(pbvi);

@@ -44,6 +44,13 @@ struct BackupEngine {
     float *Gt = nullptr;                 // [n][gtCols] transposed unique alphas
     size_t gtCols = 0;
     unsigned *jstar = nullptr;           // [r][m][z] chosen alpha per (belief, action, observation)
+    unsigned *ustar = nullptr;           // [r][m][z] the same choice as a unique-alpha index
+    float *Proj = nullptr;               // [m][z][n][projCols] exact projections of the unique alphas
+    size_t projCap = 0, projCols = 0;
+    bool projUnavailable = false, useProjNow = false;
+    float *scanV = nullptr;              // running best of the chunked row scan
+    unsigned *scanU = nullptr;
+    size_t scanCap = 0;
     float *actVal = nullptr;             // [r][m] value of each action's assembled alpha at the belief
     float *partV = nullptr;              // [items][z][splits] split-scan partial maxima
     unsigned *partU = nullptr;
@@ -58,11 +65,13 @@ struct BackupEngine {
     float *vnb = nullptr, *vnp1b = nullptr;  // [r] Perseus values over V_n and V_{n+1}
     unsigned *btilde = nullptr;          // [r] Perseus compacted belief list
     cudaStream_t stream = 0;
-    cudaEvent_t ev[6] = {};
+    cudaEvent_t ev[8] = {};
     bool eventsMade = false;
-    unsigned scoring = NOVA_SCORING_BF16;
+    unsigned scoring = NOVA_SCORING_FP16;
     NovaPBVIStats stats{};
     TcState *tc = nullptr;
+    bool tcUnavailable = false;   // tensor-core operands could not be built (memory)
+    static constexpr unsigned kTcMinUnique = 32;
 
     ~BackupEngine();
     int build(const DevModel &model, const char *fn);
@@ -72,6 +81,11 @@ struct BackupEngine {
     int dedup(const float *src, unsigned rows, unsigned *nUnique, const char *fn);
     // Exact scoring of the listed (belief, action) items over the unique rows.
     int exact_score(const unsigned *items, unsigned nItems, unsigned nU, const char *fn);
+    // Projection table for nU unique alphas (false if it does not fit).
+    bool ensure_proj(unsigned nU);
+    int project(unsigned nU, const char *fn);
+    // Exact scan of (a*z+o)*r + i rows over the projection table (all rows if rowList is null).
+    int scan_rows(const unsigned *rowList, unsigned nRows, unsigned nU, const char *fn);
     // Work list of `count` consecutive items starting at `first`.
     int fill_items(unsigned first, unsigned count, const char *fn);
     // Action values and best-action assembly for all beliefs (or one).
@@ -86,8 +100,10 @@ int tc_build(BackupEngine &eng, const char *fn);
 // Scores every (belief, action, observation) row against the nU unique rows
 // of src (gathered through eng.uniqJ), writes eng.jstar for rows whose argmax
 // is proven, and appends the (belief, action) items that need the exact full
-// scan to eng.items / *nOverflow.
-int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nOverflow, const char *fn);
+// scan to *rowList / *nRows as (a*z+o)*r + i row indices (a device list
+// owned by the tensor-core state, sized for every row).
+int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, const unsigned **rowList,
+             const char *fn);
 void tc_release(TcState *tc);
 unsigned tc_device_error();
 

@@ -1,7 +1,49 @@
-// nova-gb300: tensor-core belief scoring (placeholder until the tcgen05
-// kernel lands; every update takes the exact path).
+// nova-gb300: tensor-core belief scoring for the point-based backup.
+//
+// The score of alpha j for (belief i, action a, observation o) is
+//     score = sum_k B[i,k] * gamma * sum_l O(a,S,o) T(s_k,a,l) Gamma_j(S)
+//           = sum_s A_ao[i,s] * Gamma_j[s],
+//     A_ao[i,s] = gamma * O(a,s,o) * sum_{k,l : S(s_k,a,l) = s} B[i,k] T(s_k,a,l),
+// a dense (r x n) . (n x |Gamma|) product per (a,o) pair. A_ao does not
+// depend on Gamma: it is built once in BF16 ([m*z][rPad][nPad], K-major).
+// Each update packs the unique alphas, shifted by a per-state midpoint c[s]
+// (which changes every score of a row by the same amount), into BF16, and
+// the GEMM scores every row against every unique alpha on the tcgen05
+// tensor cores with FP32 accumulation in TMEM. The epilogue keeps, per row,
+// the 4 best (score, alpha) pairs and the best score it dropped; the scores
+// never reach HBM.
+//
+// Exactness: for every row the kernel's score differs from the reference's
+// FP32 score (pomdp_pbvi_cpu.cpp:50-83) by at most
+//     E = a1 * (U * gmax + g_N * Gmax)
+// (a1 = sum_s |A_ao[i,s]|, gmax = max |Gamma - c|, Gmax = max |Gamma|;
+// U covers the BF16 rounding of both operands, the FP32 build of A and the
+// tensor-core accumulation over nPad terms; g_N = (ns + rz + 3) * 2^-24
+// covers the reference's own rounding). Every alpha within 2E of the best is
+// re-scored in the reference's exact FP32 order and the argmax taken there;
+// if the dropped-score bound says a candidate may be missing, the (belief,
+// action) pair is rescanned exactly over all alphas. The chosen alphas are
+// therefore exactly the reference's.
+//
+// GEMM kernel: persistent, one CTA per SM, 6 warps: warp 0 issues TMA loads
+// (SWIZZLE_128B tiles 128x64 of A and 256x64 of the alphas into a 4-stage
+// ring), warp 1 issues tcgen05.mma (M=128, N=256, K=16, cta_group::1) into
+// two 256-column TMEM accumulators, warps 2-5 drain TMEM with tcgen05.ld and
+// run the top-4 epilogue while the next tile accumulates. Work units are
+// (a*z+o, 128-row tile, alpha group); units that run concurrently share
+// their A tile and stream the same alphas, so both stay in L2. Every
+// mbarrier wait is bounded; on timeout the kernel records an error word,
+// stops issuing, frees its TMEM and returns.
 
 #include "pbvi.h"
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
 
 namespace nova_gb300 {
 
@@ -20,11 +62,829 @@ unsigned read_and_clear_device_error() {
     return h;
 }
 
-unsigned tc_device_error() { return 0; }
+unsigned tc_device_error() { return read_and_clear_device_error(); }
 
-bool tc_supported(const DevModel &) { return false; }
-int tc_build(BackupEngine &, const char *) { return NOVA_ERROR_INVALID_DATA; }
-int tc_score(BackupEngine &, const float *, unsigned, unsigned *, const char *) { return NOVA_ERROR_INVALID_DATA; }
-void tc_release(TcState *) {}
+constexpr int BM = 128;            // rows (beliefs) per tile
+constexpr int BN = 256;            // alphas per tile
+constexpr int BK = 64;             // K (states) per stage: 128 bytes of BF16
+constexpr int STAGES = 4;
+constexpr int TOPK = 8;
+constexpr int MAX_GROUPS = 8;
+constexpr unsigned kNoneU = 0xffffffffu;
+constexpr int A_STAGE_BYTES = BM * BK * 2;   // 16 KB
+constexpr int B_STAGE_BYTES = BN * BK * 2;   // 32 KB
+constexpr int GEMM_THREADS = 192;
+constexpr size_t GEMM_SMEM = (size_t)STAGES * (A_STAGE_BYTES + B_STAGE_BYTES) + 1024 + 256;
+constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
+
+struct TcState {
+    size_t nPad = 0, rPad = 0, capN = 0;
+    unsigned MZ = 0, mTiles = 0;
+    unsigned mode = 0;              // NOVA_SCORING_BF16 or NOVA_SCORING_FP16: element type of A and Gb
+    uint16_t *A = nullptr;          // [MZ][rPad][nPad] BF16 or FP16 bits, each row scaled by a power of 2
+    float *a1 = nullptr;            // [MZ][rPad] bound of sum_s |A| in the row's scaled units
+    float *a1raw = nullptr;         // [MZ][rPad] the same bound unscaled
+    uint16_t *Gb = nullptr;         // [capN][nPad] BF16 or FP16 bits of (alpha - c) * 2^gexp
+    float *shift = nullptr;         // [n]
+    unsigned *scal = nullptr;       // [0] gmax, [1] Gmax, [2] escale, [3..4] counters, [5] max half-range, [6] G scale (float bits)
+    float *candV = nullptr;         // [MZ][r][MAX_GROUPS][TOPK]
+    unsigned *candU = nullptr;
+    float *candX = nullptr;         // [MZ][r][MAX_GROUPS]
+    unsigned *rowFlag = nullptr;    // [MZ*r] rows needing the exact scan
+    unsigned *rowList = nullptr;    // [MZ*r] their indices, compacted
+    unsigned *badModel = nullptr;   // [1] set when a probability is negative or NaN
+    PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    CUtensorMap tmA;
+    cudaEvent_t g0 = nullptr, g1 = nullptr;
+    int numSMs = 0;
+};
+
+void tc_release(TcState *tc) {
+    if (!tc) return;
+    cudaFree(tc->A); cudaFree(tc->a1); cudaFree(tc->a1raw); cudaFree(tc->Gb); cudaFree(tc->shift); cudaFree(tc->scal);
+    cudaFree(tc->candV); cudaFree(tc->candU); cudaFree(tc->candX); cudaFree(tc->rowFlag); cudaFree(tc->rowList);
+    cudaFree(tc->badModel);
+    if (tc->g0) cudaEventDestroy(tc->g0);
+    if (tc->g1) cudaEventDestroy(tc->g1);
+    delete tc;
+}
+
+bool tc_supported(const DevModel &md) {
+    // The dense row of W_a must fit in shared memory while A is built, and
+    // the row index must stay in TMA's 32-bit coordinate range.
+    const size_t nPad = round_up(md.n, BK), rPad = round_up(md.r, BM);
+    return md.n <= 40000 && (size_t)md.m * md.z * rPad < (1ull << 31) && nPad < (1ull << 31) && md.r >= 1;
+}
+
+// ---------------------------------------------------------------------------
+// PTX wrappers (tcgen05 / TMA / mbarrier)
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: returns false (after recording a device error and raising
+// the CTA's abort flag) if the phase does not complete in ~2 s, or if
+// another role of the CTA already aborted.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abortFlag) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (true) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (*abortFlag) return false;
+        if (clock64() - t0 > kWaitCycles) {
+            *abortFlag = 1;
+            atomicExch(&g_device_error, 1u);
+            return false;
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int c0, int c1, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor for a K-major, 128-byte-swizzled tile
+// whose 8-row groups are 1024 bytes apart (the layout TMA writes with
+// CU_TENSOR_MAP_SWIZZLE_128B and a 128-byte inner box).
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1u << 16;              // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024u >> 4) << 32;    // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1u << 46;              // descriptor version (tcgen05)
+    d |= (uint64_t)2u << 61;              // SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor, kind::f16: D FP32; A and B both BF16 (format 1) or
+// both FP16 (format 0), K-major; M=128, N=256.
+__host__ __device__ constexpr uint32_t make_idesc(uint32_t fmt) {
+    return (1u << 4) | (fmt << 7) | (fmt << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_f16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(dtmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int k = 0; k < 32; k++) v[k] = __uint_as_float(r[k]);
+}
+
+// ---------------------------------------------------------------------------
+// The scoring GEMM with the top-8 epilogue
+// ---------------------------------------------------------------------------
+
+struct GemmBarriers {
+    uint64_t full[STAGES];
+    uint64_t empty[STAGES];
+    uint64_t accFull[2];
+    uint64_t accEmpty[2];
+    uint32_t tmemBase;
+    int abortFlag;
+};
+
+__device__ __forceinline__ void decode_unit(unsigned unit, unsigned groups, unsigned mTiles, unsigned nTiles,
+                                            unsigned &ao, unsigned &mt, unsigned &g, unsigned &nt0, unsigned &nt1) {
+    g = unit % groups;
+    const unsigned t = unit / groups;
+    mt = t % mTiles;
+    ao = t / mTiles;
+    nt0 = (unsigned)((unsigned long long)g * nTiles / groups);
+    nt1 = (unsigned)((unsigned long long)(g + 1) * nTiles / groups);
+}
+
+// Sorted top-8 of (score, alpha) in registers; `excl` is the best score
+// that fell off (or never entered) the list.
+struct Top8 {
+    float v[TOPK];
+    unsigned u[TOPK];
+    float excl;
+    __device__ __forceinline__ void reset() {
+#pragma unroll
+        for (int k = 0; k < TOPK; k++) { v[k] = -INFINITY; u[k] = kNoneU; }
+        excl = -INFINITY;
+    }
+    __device__ __forceinline__ void push(float x, unsigned idx) {
+        if (!(x > v[TOPK - 1])) {   // also drops NaN
+            excl = fmaxf(excl, x);
+            return;
+        }
+        excl = fmaxf(excl, v[TOPK - 1]);
+        // insertion from the bottom; equal scores keep the earlier (lower) index first
+#pragma unroll
+        for (int k = TOPK - 1; k > 0; k--) {
+            const bool shift = x > v[k - 1];
+            const bool place = !shift && x > v[k];
+            if (shift) { v[k] = v[k - 1]; u[k] = u[k - 1]; }
+            else if (place) { v[k] = x; u[k] = idx; }
+        }
+        if (x > v[0]) { v[0] = x; u[0] = idx; }
+    }
+};
+
+__global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
+        const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, uint32_t idesc,
+        unsigned MZ, unsigned rPad, unsigned r, unsigned mTiles, unsigned nTiles, unsigned groups, unsigned nU,
+        unsigned kBlocks, float *__restrict__ candV, unsigned *__restrict__ candU, float *__restrict__ candX) {
+    extern __shared__ uint8_t smemRaw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~(uintptr_t)1023);
+    uint8_t *sA = smem;
+    uint8_t *sB = smem + STAGES * A_STAGE_BYTES;
+    GemmBarriers *bar = reinterpret_cast<GemmBarriers *>(smem + STAGES * (A_STAGE_BYTES + B_STAGE_BYTES));
+    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            mbar_init(smem_u32(&bar->full[s]), 1);
+            mbar_init(smem_u32(&bar->empty[s]), 1);
+        }
+        for (int a = 0; a < 2; a++) {
+            mbar_init(smem_u32(&bar->accFull[a]), 1);
+            mbar_init(smem_u32(&bar->accEmpty[a]), 4);
+        }
+        bar->abortFlag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;"
+                     ::"r"(smem_u32(&bar->tmemBase)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = bar->tmemBase;
+    volatile int *abortFlag = &bar->abortFlag;
+    const unsigned totalUnits = MZ * mTiles * groups;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---- TMA producer ----
+            unsigned stage = 0, phase = 0;
+            for (unsigned unit = blockIdx.x; unit < totalUnits && !*abortFlag; unit += gridDim.x) {
+                unsigned ao, mt, g, nt0, nt1;
+                decode_unit(unit, groups, mTiles, nTiles, ao, mt, g, nt0, nt1);
+                const int rowA = (int)(ao * rPad + mt * BM);
+                for (unsigned nt = nt0; nt < nt1 && !*abortFlag; nt++) {
+                    for (unsigned kb = 0; kb < kBlocks; kb++) {
+                        if (!mbar_wait(smem_u32(&bar->empty[stage]), phase ^ 1u, abortFlag)) break;
+                        const uint32_t fb = smem_u32(&bar->full[stage]);
+                        mbar_expect_tx(fb, A_STAGE_BYTES + B_STAGE_BYTES);
+                        tma_load_2d(smem_u32(sA + stage * A_STAGE_BYTES), &tmA, (int)(kb * BK), rowA, fb);
+                        tma_load_2d(smem_u32(sB + stage * B_STAGE_BYTES), &tmB, (int)(kb * BK), (int)(nt * BN), fb);
+                        if (++stage == STAGES) { stage = 0; phase ^= 1u; }
+                    }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // ---- MMA issuer ----
+            unsigned stage = 0, phase = 0, acc = 0, accPhase = 0;
+            for (unsigned unit = blockIdx.x; unit < totalUnits && !*abortFlag; unit += gridDim.x) {
+                unsigned ao, mt, g, nt0, nt1;
+                decode_unit(unit, groups, mTiles, nTiles, ao, mt, g, nt0, nt1);
+                for (unsigned nt = nt0; nt < nt1 && !*abortFlag; nt++) {
+                    if (!mbar_wait(smem_u32(&bar->accEmpty[acc]), accPhase ^ 1u, abortFlag)) break;
+                    tc_fence_after();
+                    const uint32_t dtmem = tmem + acc * BN;
+                    for (unsigned kb = 0; kb < kBlocks; kb++) {
+                        if (!mbar_wait(smem_u32(&bar->full[stage]), phase, abortFlag)) break;
+                        tc_fence_after();
+                        const uint64_t adesc = smem_desc_sw128(smem_u32(sA + stage * A_STAGE_BYTES));
+                        const uint64_t bdesc = smem_desc_sw128(smem_u32(sB + stage * B_STAGE_BYTES));
+#pragma unroll
+                        for (int kk = 0; kk < BK / 16; kk++)
+                            umma_f16(dtmem, adesc + 2u * kk, bdesc + 2u * kk, idesc,
+                                     (kb | (unsigned)kk) != 0u ? 1u : 0u);
+                        umma_commit(smem_u32(&bar->empty[stage]));
+                        if (++stage == STAGES) { stage = 0; phase ^= 1u; }
+                    }
+                    umma_commit(smem_u32(&bar->accFull[acc]));
+                    acc ^= 1u;
+                    if (acc == 0) accPhase ^= 1u;
+                }
+            }
+        }
+    } else {
+        // ---- epilogue: TMEM -> registers -> running top-8 per row ----
+        const unsigned quarter = warp & 3u;   // TMEM lanes this warp may access
+        const unsigned rowInTile = quarter * 32u + lane;
+        unsigned acc = 0, accPhase = 0;
+        Top8 top;
+        for (unsigned unit = blockIdx.x; unit < totalUnits && !*abortFlag; unit += gridDim.x) {
+            unsigned ao, mt, g, nt0, nt1;
+            decode_unit(unit, groups, mTiles, nTiles, ao, mt, g, nt0, nt1);
+            top.reset();
+            bool ok = true;
+            for (unsigned nt = nt0; nt < nt1; nt++) {
+                if (!mbar_wait(smem_u32(&bar->accFull[acc]), accPhase, abortFlag)) { ok = false; break; }
+                tc_fence_after();
+                const uint32_t base = tmem + ((quarter * 32u) << 16) + acc * BN;
+#pragma unroll 1
+                for (unsigned ch = 0; ch < BN / 32; ch++) {
+                    float v[32];
+                    tmem_ld32(base + ch * 32u, v);
+                    const unsigned u0 = nt * BN + ch * 32u;
+#pragma unroll
+                    for (int c = 0; c < 32; c++)
+                        if (u0 + c < nU) top.push(v[c], u0 + c);
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_u32(&bar->accEmpty[acc]));
+                acc ^= 1u;
+                if (acc == 0) accPhase ^= 1u;
+            }
+            if (!ok) break;
+            const unsigned i = mt * BM + rowInTile;
+            if (i < r) {
+                const size_t slot = ((size_t)ao * r + i) * MAX_GROUPS + g;
+                float *cv = candV + slot * TOPK;
+                unsigned *cu = candU + slot * TOPK;
+#pragma unroll
+                for (int k = 0; k < TOPK; k++) { cv[k] = top.v[k]; cu[k] = top.u[k]; }
+                candX[slot] = top.excl;
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Step-invariant operand: A_ao[i, s] in BF16/FP16, each row scaled by a power
+// of two so its largest entry lies in [2^13, 2^14) (FP16's precision is then
+// used fully and nothing overflows); a1 bounds sum_s |A| in the same units.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ uint16_t to_half_bits(float v, bool fp16) {
+    if (fp16) return __half_as_ushort(__float2half_rn(v));
+    return __bfloat16_as_ushort(__float2bfloat16_rn(v));
+}
+
+__global__ void tc_build_a_kernel(DevModel md, const unsigned *__restrict__ succLen,
+                                  const unsigned *__restrict__ suppLen, size_t rPad, size_t nPad, int fp16,
+                                  uint16_t *__restrict__ A, float *__restrict__ a1, float *__restrict__ a1raw,
+                                  float a1Slack, unsigned *__restrict__ badModel) {
+    extern __shared__ float W[];  // [n]
+    const unsigned i = blockIdx.x / md.m, a = blockIdx.x % md.m;
+    for (unsigned s = threadIdx.x; s < md.n; s += blockDim.x) W[s] = 0.0f;
+    __syncthreads();
+    const unsigned Li = suppLen[i];
+    for (unsigned e = threadIdx.x; e < Li * md.ns; e += blockDim.x) {
+        const unsigned k = e / md.ns, l = e % md.ns;
+        const int s = md.Z[(size_t)i * md.rz + k];
+        if (l < succLen[(size_t)s * md.m + a]) {
+            const size_t row = ((size_t)s * md.m + a) * md.ns + l;
+            const float w = md.B[(size_t)i * md.rz + k] * md.T[row];
+            if (!(w >= 0.0f)) atomicOr(badModel, 1u);  // the bound assumes non-negative B, T, O
+            atomicAdd(&W[md.S[row]], w);
+        }
+    }
+    __syncthreads();
+    __shared__ float red[32];
+    __shared__ float rowScale;
+    for (unsigned o = 0; o < md.z; o++) {
+        const size_t ao = (size_t)a * md.z + o;
+        uint16_t *row = A + (ao * rPad + i) * nPad;
+        float mx = 0.0f, sum = 0.0f;
+        for (unsigned s = threadIdx.x; s < md.n; s += blockDim.x) {
+            const float ob = md.O[((size_t)a * md.n + s) * md.z + o];
+            if (!(ob >= 0.0f)) atomicOr(badModel, 1u);
+            const float v = md.gamma * W[s] * ob;
+            mx = fmaxf(mx, v);
+            sum += v;
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+            sum += __shfl_xor_sync(0xffffffffu, sum, off);
+        }
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (unsigned w = 0; w < blockDim.x / 32; w++) mx = fmaxf(mx, red[w]);
+            int e = 0;
+            if (mx > 0.0f) frexpf(mx, &e);          // mx in [2^(e-1), 2^e)
+            rowScale = mx > 0.0f ? ldexpf(1.0f, 14 - e) : 1.0f;
+        }
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sum;
+        __syncthreads();
+        const float scale = rowScale;
+        for (unsigned s = threadIdx.x; s < nPad; s += blockDim.x) {
+            float v = 0.0f;
+            if (s < md.n) v = md.gamma * W[s] * md.O[((size_t)a * md.n + s) * md.z + o];
+            row[s] = to_half_bits(v * scale, fp16 != 0);
+        }
+        if (threadIdx.x == 0) {
+            float t = 0.0f;
+            for (unsigned w = 0; w < blockDim.x / 32; w++) t += red[w];
+            a1[ao * rPad + i] = t * scale * a1Slack;
+            a1raw[ao * rPad + i] = t * a1Slack;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-update packing of the unique alphas
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void atomic_max_nonneg(unsigned *addr, float v) {
+    // Non-negative floats order like their bit patterns; NaN (all exponent
+    // bits set, nonzero mantissa) compares above every finite value, which
+    // disables the margin.
+    atomicMax(addr, __float_as_uint(v));
+}
+
+// Per-state midpoint shift c[s] over the unique alphas, Gmax = max |alpha|
+// (scal[1]) and the largest half-range max (hi - lo) / 2 (scal[5]).
+__global__ void tc_shift_kernel(const float *__restrict__ Gt, size_t gtCols, unsigned n, unsigned nU,
+                                float *__restrict__ shift, unsigned *__restrict__ scal) {
+    const unsigned s = blockIdx.x;
+    const float *row = Gt + (size_t)s * gtCols;
+    float mn = INFINITY, mx = -INFINITY;
+    int nanSeen = 0;
+    for (unsigned u = threadIdx.x; u < nU; u += blockDim.x) {
+        const float v = row[u];
+        mn = fminf(mn, v);
+        mx = fmaxf(mx, v);
+        nanSeen |= (v != v);
+    }
+    __shared__ float smn[32], smx[32];
+    __shared__ int snan;
+    if (threadIdx.x == 0) snan = 0;
+    for (int off = 16; off > 0; off >>= 1) {
+        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, off));
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    }
+    __syncthreads();
+    if (nanSeen) snan = 1;
+    if ((threadIdx.x & 31) == 0) { smn[threadIdx.x >> 5] = mn; smx[threadIdx.x >> 5] = mx; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (unsigned w = 0; w < blockDim.x / 32; w++) { mn = fminf(mn, smn[w]); mx = fmaxf(mx, smx[w]); }
+        shift[s] = 0.5f * mn + 0.5f * mx;
+        const float nanf_ = __uint_as_float(0x7fc00000u);
+        atomic_max_nonneg(&scal[1], snan ? nanf_ : fmaxf(fabsf(mn), fabsf(mx)));
+        atomic_max_nonneg(&scal[5], snan ? nanf_ : 0.5f * (mx - mn));
+    }
+}
+
+// Power-of-two scale for the packed alphas: the largest |alpha - c| lands
+// in [2^13, 2^14) (half-range plus slack for the rounding of c).
+__global__ void tc_gscale_kernel(unsigned *scal) {
+    const float hr = __uint_as_float(scal[5]) * 1.001f + 1e-30f;
+    int e = 0;
+    frexpf(hr, &e);
+    scal[6] = __float_as_uint(hr < 1e30f ? ldexpf(1.0f, 13 - e) : 1.0f);
+}
+
+// Gb[u][s] = half((alpha_u(s) - c[s]) * gscale); rows >= nU, states >= n are 0.
+// Records gmax = max |(alpha - c) * gscale| over the FP32 values.
+__global__ void tc_pack_kernel(const float *__restrict__ G, unsigned n, size_t nPad, const unsigned *__restrict__ uniqJ,
+                               unsigned nU, const float *__restrict__ shift, int fp16, uint16_t *__restrict__ Gb,
+                               unsigned *__restrict__ scal) {
+    const unsigned u = blockIdx.x;
+    const float gscale = __uint_as_float(scal[6]);
+    uint16_t *out = Gb + (size_t)u * nPad;
+    float m = 0.0f;
+    int nanSeen = 0;
+    if (u < nU) {
+        const float *row = G + (size_t)uniqJ[u] * n;
+        for (unsigned s = threadIdx.x; s < nPad; s += blockDim.x) {
+            float v = 0.0f;
+            if (s < n) {
+                v = (row[s] - shift[s]) * gscale;
+                m = fmaxf(m, fabsf(v));
+                nanSeen |= (v != v);
+            }
+            out[s] = to_half_bits(v, fp16 != 0);
+        }
+    } else {
+        for (unsigned s = threadIdx.x; s < nPad; s += blockDim.x) out[s] = 0;
+    }
+    __shared__ float red[32];
+    __shared__ int snan;
+    if (threadIdx.x == 0) snan = 0;
+    for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+    __syncthreads();
+    if (nanSeen) snan = 1;
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (unsigned w = 0; w < blockDim.x / 32; w++) m = fmaxf(m, red[w]);
+        atomic_max_nonneg(&scal[0], snan ? __uint_as_float(0x7fc00000u) : m);
+    }
+}
+
+// escale = U * gmax + gN * Gmax * gscale (all in the packed units); the
+// per-row bound is a1 * escale.
+__global__ void tc_escale_kernel(unsigned *scal, float U, float gN) {
+    const float gmax = __uint_as_float(scal[0]);
+    const float Gmax = __uint_as_float(scal[1]);
+    const float gscale = __uint_as_float(scal[6]);
+    scal[2] = __float_as_uint(U * gmax + gN * Gmax * gscale);
+}
+
+// ---------------------------------------------------------------------------
+// Merge the per-group lists, apply the proven margin, re-score near ties
+// exactly from the projection table. One warp per (a*z+o, belief) row; rows
+// whose candidate set may be incomplete go to the exact row scan.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ float proj_row_score(const float *__restrict__ P, size_t uCols, unsigned u,
+                                                const float *__restrict__ bk, const int *__restrict__ sk, unsigned Li) {
+    float v = 0.0f;
+    for (unsigned k = 0; k < Li; k++) v = fadd(v, fmul(P[(size_t)sk[k] * uCols + u], bk[k]));
+    return v;
+}
+
+__global__ void tc_merge_kernel(DevModel md, const unsigned *__restrict__ suppLen, const float *__restrict__ Proj,
+                                size_t uCols, const unsigned *__restrict__ uniqJ, unsigned groups, size_t rPad,
+                                const float *__restrict__ a1, const float *__restrict__ a1raw,
+                                const unsigned *__restrict__ scal,
+                                const float *__restrict__ candV, const unsigned *__restrict__ candU,
+                                const float *__restrict__ candX, unsigned *__restrict__ ustar,
+                                unsigned *__restrict__ jstar, unsigned *__restrict__ rowFlag,
+                                unsigned *__restrict__ counters, const unsigned *__restrict__ badModel) {
+    const unsigned lane = threadIdx.x & 31;
+    const size_t row = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const size_t rows = (size_t)md.m * md.z * md.r;
+    if (row >= rows) return;
+    const unsigned ao = (unsigned)(row / md.r), i = (unsigned)(row % md.r);
+    const unsigned a = ao / md.z, o = ao % md.z;
+    const size_t base = row * MAX_GROUPS * TOPK;
+    const unsigned nEnt = groups * TOPK;     // <= 64: each lane holds entries lane and lane + 32
+    float v0 = -INFINITY, v1 = -INFINITY;
+    unsigned u0 = kNoneU, u1 = kNoneU;
+    if (lane < nEnt) { u0 = candU[base + lane]; v0 = u0 == kNoneU ? -INFINITY : candV[base + lane]; }
+    if (lane + 32 < nEnt) { u1 = candU[base + lane + 32]; v1 = u1 == kNoneU ? -INFINITY : candV[base + lane + 32]; }
+    float x = lane < groups ? candX[row * MAX_GROUPS + lane] : -INFINITY;
+    float tmax = fmaxf(v0, v1);
+    for (int off = 16; off > 0; off >>= 1) {
+        tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, off));
+        x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, off));
+    }
+    const float bound = a1[(size_t)ao * rPad + i];
+    const float thr = 2.0f * bound * __uint_as_float(scal[2]);
+    // Usable only with a finite margin, non-negative probabilities, and
+    // scores far from the reference's -1e10 sentinel.
+    const float Gmax = __uint_as_float(scal[1]);
+    const bool usable = (thr < 1e30f) && (tmax > -INFINITY) && *badModel == 0u &&
+                        (a1raw[(size_t)ao * rPad + i] * Gmax < 1e9f);
+    const float cut = tmax - thr;
+    if (!usable || x >= cut) {
+        if (lane == 0) rowFlag[row] = 1u;
+        return;
+    }
+    const bool c0 = u0 != kNoneU && v0 >= cut;
+    const bool c1 = u1 != kNoneU && v1 >= cut;
+    const unsigned m0 = __ballot_sync(0xffffffffu, c0), m1 = __ballot_sync(0xffffffffu, c1);
+    const unsigned count = __popc(m0) + __popc(m1);
+    const size_t js = ((size_t)i * md.m + a) * md.z + o;
+    if (count == 1) {
+        const unsigned src = m0 ? __ffs(m0) - 1 : __ffs(m1) - 1;
+        const unsigned uu = m0 ? __shfl_sync(0xffffffffu, u0, src) : __shfl_sync(0xffffffffu, u1, src);
+        if (lane == 0) { ustar[js] = uu; jstar[js] = uniqJ[uu]; }
+        return;
+    }
+    // Several candidates: each lane re-scores its own in the exact order.
+    const float *P = Proj + (size_t)ao * md.n * uCols;
+    const unsigned Li = suppLen[i];
+    const int *sk = md.Z + (size_t)i * md.rz;
+    const float *bk = md.B + (size_t)i * md.rz;
+    float best = -INFINITY;
+    unsigned bu = kNoneU;
+    if (c0) { best = proj_row_score(P, uCols, u0, bk, sk, Li); bu = u0; }
+    if (c1) {
+        const float w = proj_row_score(P, uCols, u1, bk, sk, Li);
+        if (bu == kNoneU || w > best || (w == best && u1 < bu)) { best = w; bu = u1; }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const float b2 = __shfl_xor_sync(0xffffffffu, best, off);
+        const unsigned u2 = __shfl_xor_sync(0xffffffffu, bu, off);
+        if (u2 != kNoneU && (bu == kNoneU || b2 > best || (b2 == best && u2 < bu))) { best = b2; bu = u2; }
+    }
+    if (lane == 0) {
+        if (!(best > -1e10f)) {
+            rowFlag[row] = 1u;  // sentinel case: the exact scan applies the reference's rule
+        } else {
+            ustar[js] = bu;
+            jstar[js] = uniqJ[bu];
+        }
+        atomicAdd(&counters[0], 1u);
+        atomicAdd(&counters[1], count);
+    }
+}
+
+// Flagged rows -> row list (single block, increasing order).
+__global__ void __launch_bounds__(1024) tc_compact_rows_kernel(const unsigned *__restrict__ flag, unsigned count,
+                                                               unsigned *__restrict__ items, unsigned *__restrict__ nOut) {
+    __shared__ unsigned warpSums[32];
+    __shared__ unsigned carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (unsigned base = 0; base < count; base += blockDim.x) {
+        const unsigned t = base + threadIdx.x;
+        const unsigned f = (t < count && flag[t]) ? 1u : 0u;
+        unsigned v = f;
+        for (int off = 1; off < 32; off <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, v, off);
+            if (lane >= (unsigned)off) v += y;
+        }
+        if (lane == 31) warpSums[warp] = v;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned w = lane < (blockDim.x >> 5) ? warpSums[lane] : 0u;
+            for (int off = 1; off < 32; off <<= 1) {
+                const unsigned y = __shfl_up_sync(0xffffffffu, w, off);
+                if (lane >= (unsigned)off) w += y;
+            }
+            warpSums[lane] = w;
+        }
+        __syncthreads();
+        const unsigned pos = carry + (warp > 0 ? warpSums[warp - 1] : 0u) + v - f;
+        if (f) items[pos] = t;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warpSums[(blockDim.x >> 5) - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *nOut = carry;
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+
+static int encode_map(TcState *tc, CUtensorMap *map, const void *base, size_t rows, size_t cols, unsigned boxRows,
+                      const char *fn) {
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(cols * sizeof(uint16_t))};
+    cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)boxRows};
+    cuuint32_t estr[2] = {1, 1};
+    const CUtensorMapDataType dt =
+        tc->mode == NOVA_SCORING_FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    CUresult res = tc->encode(map, dt, 2, const_cast<void *>(base), dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (res != CUDA_SUCCESS) {
+        NOVA_ERR(fn, "Failed to encode a TMA tensor map.");
+        return NOVA_ERROR_KERNEL_EXECUTION;
+    }
+    return NOVA_SUCCESS;
+}
+
+// (Re)builds A in the element type of the engine's scoring mode.
+static int tc_build_operand(BackupEngine &eng, TcState *tc, const char *fn) {
+    const DevModel &md = eng.md;
+    tc->mode = eng.scoring;
+    const size_t aElems = (size_t)tc->MZ * tc->rPad * tc->nPad;
+    cudaMemsetAsync(tc->A, 0, aElems * sizeof(uint16_t), eng.stream);
+    cudaMemsetAsync(tc->a1, 0, (size_t)tc->MZ * tc->rPad * sizeof(float), eng.stream);
+    cudaMemsetAsync(tc->a1raw, 0, (size_t)tc->MZ * tc->rPad * sizeof(float), eng.stream);
+    cudaMemsetAsync(tc->badModel, 0, sizeof(unsigned), eng.stream);
+    // a1 bounds sum_s |A| with A in exact arithmetic: the FP32 sums of
+    // non-negative terms are inflated by their worst-case rounding.
+    const float slack = 1.0f + (float)(md.n + md.rz * md.ns + 8) * 1.2e-7f;
+    tc_build_a_kernel<<<md.r * md.m, 256, md.n * sizeof(float), eng.stream>>>(
+        md, eng.succLen, eng.suppLen, tc->rPad, tc->nPad, tc->mode == NOVA_SCORING_FP16 ? 1 : 0, tc->A, tc->a1,
+        tc->a1raw, slack, tc->badModel);
+    int rc = check_launch(fn, "scoring operand build");
+    if (rc != NOVA_SUCCESS) return rc;
+    return encode_map(tc, &tc->tmA, tc->A, (size_t)tc->MZ * tc->rPad, tc->nPad, BM, fn);
+}
+
+int tc_build(BackupEngine &eng, const char *fn) {
+    if (eng.tc) return NOVA_SUCCESS;
+    const DevModel &md = eng.md;
+    std::unique_ptr<TcState> tc(new TcState());
+    tc->nPad = round_up(md.n, BK);
+    tc->rPad = round_up(md.r, BM);
+    tc->capN = round_up(md.r, BN);
+    tc->MZ = md.m * md.z;
+    tc->mTiles = (unsigned)(tc->rPad / BM);
+    const size_t aElems = (size_t)tc->MZ * tc->rPad * tc->nPad;
+    size_t freeB = 0, totalB = 0;
+    cudaMemGetInfo(&freeB, &totalB);
+    const size_t slots = (size_t)tc->MZ * md.r * MAX_GROUPS;
+    const size_t need = aElems * 2 + tc->capN * tc->nPad * 2 + slots * (TOPK * 8 + 4) + (size_t)tc->MZ * md.r * 4;
+    if (need + (256ull << 20) > freeB) {
+        NOVA_ERR(fn, "Not enough device memory for the tensor-core operands; using exact scoring.");
+        return NOVA_ERROR_DEVICE_MALLOC;
+    }
+    void *fnPtr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fnPtr, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess || q != cudaDriverEntryPointSuccess || fnPtr == nullptr) {
+        cudaGetLastError();
+        NOVA_ERR(fn, "cuTensorMapEncodeTiled is not available.");
+        return NOVA_ERROR_KERNEL_EXECUTION;
+    }
+    tc->encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fnPtr);
+    int rc;
+    if ((rc = dev_alloc(&tc->A, aElems, fn, "the tensor-core scoring operand")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->a1, (size_t)tc->MZ * tc->rPad, fn, "the row bounds")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->a1raw, (size_t)tc->MZ * tc->rPad, fn, "the row bounds")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->Gb, tc->capN * tc->nPad, fn, "the packed alphas")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->shift, md.n, fn, "the alpha shift")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->scal, 8, fn, "the scoring scalars")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->candV, slots * TOPK, fn, "the candidate scores")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->candU, slots * TOPK, fn, "the candidate alphas")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->candX, slots, fn, "the dropped-score bounds")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->rowFlag, (size_t)tc->MZ * md.r, fn, "the exact-scan flags")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->rowList, (size_t)tc->MZ * md.r, fn, "the exact-scan rows")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->badModel, 1, fn, "the model check")) != NOVA_SUCCESS) return rc;
+    if ((rc = tc_build_operand(eng, tc.get(), fn)) != NOVA_SUCCESS) return rc;
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, 0);
+    tc->numSMs = prop.multiProcessorCount;
+    cudaEventCreate(&tc->g0);
+    cudaEventCreate(&tc->g1);
+    if (cudaFuncSetAttribute(tc_score_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        NOVA_ERR(fn, "Failed to configure the scoring kernel's shared memory.");
+        return NOVA_ERROR_KERNEL_EXECUTION;
+    }
+    eng.tc = tc.release();
+    return sync_device(fn);
+}
+
+int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, const unsigned **rowList,
+             const char *fn) {
+    int rc;
+    if (!eng.tc && (rc = tc_build(eng, fn)) != NOVA_SUCCESS) return rc;
+    TcState *tc = eng.tc;
+    if (tc->mode != eng.scoring && (rc = tc_build_operand(eng, tc, fn)) != NOVA_SUCCESS) return rc;
+    const DevModel &md = eng.md;
+    const bool fp16 = tc->mode == NOVA_SCORING_FP16;
+    const size_t nPadRows = round_up(nU, BN);
+    const unsigned nTiles = (unsigned)(nPadRows / BN);
+    // ---- pack the shifted, scaled unique alphas ----
+    cudaMemsetAsync(tc->scal, 0, 8 * sizeof(unsigned), eng.stream);
+    tc_shift_kernel<<<md.n, 256, 0, eng.stream>>>(eng.Gt, eng.gtCols, md.n, nU, tc->shift, tc->scal);
+    if ((rc = check_launch(fn, "alpha shift")) != NOVA_SUCCESS) return rc;
+    tc_gscale_kernel<<<1, 1, 0, eng.stream>>>(tc->scal);
+    if ((rc = check_launch(fn, "alpha scale")) != NOVA_SUCCESS) return rc;
+    tc_pack_kernel<<<(unsigned)nPadRows, 256, 0, eng.stream>>>(src, md.n, tc->nPad, eng.uniqJ, nU, tc->shift,
+                                                              fp16 ? 1 : 0, tc->Gb, tc->scal);
+    if ((rc = check_launch(fn, "alpha packing")) != NOVA_SUCCESS) return rc;
+    // Error factors relative to sum_s |A| |alpha - c| (packed units): the
+    // rounding of both operands to BF16 (2^-9 each) or FP16 (2^-12 each,
+    // plus the absolute error of FP16 subnormals, below 2^-25 per entry),
+    // the FP32 build of A (epsA) and of alpha - c, and the accumulation:
+    // each tcgen05.mma step (K=16) adds at most 2^-22 of the running sum of
+    // magnitudes. The reference's own rounding over ns + rz + 3 operations
+    // is relative to a1 * Gmax.
+    const double u24 = 1.0 / 16777216.0;
+    const double epsA = (double)(md.rz * md.ns + 4) * u24;
+    const double rnd = fp16 ? 1.0 / 2048.0 : 1.0 / 512.0;
+    const double accum = ((double)tc->nPad / 16.0 + 2.0) / 4194304.0;
+    const float U = (float)(((1.0 + epsA) * (1.0 + rnd) * (1.0 + rnd) * (1.0 + 2.0 * u24) - 1.0) +
+                            accum * (1.0 + 2.0 * rnd) + (fp16 ? (double)tc->nPad / 33554432.0 / 8192.0 : 0.0) +
+                            1.0 / 1048576.0);
+    const float gN = (float)((double)(md.ns + md.rz + 3) * u24 * 1.01);
+    tc_escale_kernel<<<1, 1, 0, eng.stream>>>(tc->scal, U, gN);
+    if ((rc = check_launch(fn, "margin")) != NOVA_SUCCESS) return rc;
+    // ---- GEMM ----
+    CUtensorMap tmB;
+    if ((rc = encode_map(tc, &tmB, tc->Gb, nPadRows, tc->nPad, BN, fn)) != NOVA_SUCCESS) return rc;
+    const unsigned groups = std::min<unsigned>(MAX_GROUPS, nTiles);
+    const unsigned totalUnits = tc->MZ * tc->mTiles * groups;
+    const unsigned grid = std::min<unsigned>(totalUnits, (unsigned)tc->numSMs);
+    cudaEventRecord(tc->g0, eng.stream);
+    tc_score_gemm_kernel<<<grid, GEMM_THREADS, GEMM_SMEM, eng.stream>>>(
+        tc->tmA, tmB, make_idesc(fp16 ? 0u : 1u), tc->MZ, (unsigned)tc->rPad, md.r, tc->mTiles, nTiles, groups, nU,
+        (unsigned)(tc->nPad / BK), tc->candV, tc->candU, tc->candX);
+    if ((rc = check_launch(fn, "tensor-core scoring")) != NOVA_SUCCESS) return rc;
+    cudaEventRecord(tc->g1, eng.stream);
+    // ---- merge, margin, exact re-score of near ties ----
+    const size_t rows = (size_t)tc->MZ * md.r;
+    cudaMemsetAsync(tc->rowFlag, 0, rows * sizeof(unsigned), eng.stream);
+    tc_merge_kernel<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, eng.stream>>>(
+        md, eng.suppLen, eng.Proj, eng.projCols, eng.uniqJ, groups, tc->rPad, tc->a1, tc->a1raw, tc->scal, tc->candV,
+        tc->candU,
+        tc->candX, eng.ustar, eng.jstar, tc->rowFlag, tc->scal + 3, tc->badModel);
+    if ((rc = check_launch(fn, "candidate merge")) != NOVA_SUCCESS) return rc;
+    // The list can hold every row: it is sized m*z*r like the flags.
+    tc_compact_rows_kernel<<<1, 1024, 0, eng.stream>>>(tc->rowFlag, (unsigned)rows, tc->rowList, eng.itemCount);
+    if ((rc = check_launch(fn, "exact-scan list")) != NOVA_SUCCESS) return rc;
+    unsigned h[8];
+    unsigned cnt = 0;
+    if (cudaMemcpyAsync(h, tc->scal, sizeof(h), cudaMemcpyDeviceToHost, eng.stream) != cudaSuccess ||
+            cudaMemcpyAsync(&cnt, eng.itemCount, sizeof(unsigned), cudaMemcpyDeviceToHost, eng.stream) !=
+                cudaSuccess ||
+            cudaStreamSynchronize(eng.stream) != cudaSuccess) {
+        cudaGetLastError();
+        NOVA_ERR(fn, "Failed to read the scoring counters.");
+        return NOVA_ERROR_MEMCPY_TO_HOST;
+    }
+    if (tc_device_error() != 0) {
+        NOVA_ERR(fn, "The tensor-core scoring kernel timed out waiting on a barrier.");
+        return NOVA_ERROR_KERNEL_EXECUTION;
+    }
+    *nRows = cnt;
+    *rowList = tc->rowList;
+    eng.stats.rowsMultiCand = h[3];
+    eng.stats.candidates = h[4];
+    cudaEventElapsedTime(&eng.stats.msGemm, tc->g0, tc->g1);
+    return NOVA_SUCCESS;
+}
 
 }  // namespace nova_gb300

@@ -40,8 +40,10 @@ class NovaPBVIStats(ct.Structure):
                 ("rowsOverflow", ct.c_uint),
                 ("candidates", ct.c_uint),
                 ("msDedup", ct.c_float),
+                ("msProject", ct.c_float),
                 ("msScore", ct.c_float),
                 ("msRescore", ct.c_float),
+                ("msActions", ct.c_float),
                 ("msAssemble", ct.c_float),
                 ("msTotal", ct.c_float),
                 ("msGemm", ct.c_float),
@@ -51,6 +53,7 @@ class NovaPBVIStats(ct.Structure):
 
 SCORING_EXACT = 0
 SCORING_BF16 = 1
+SCORING_FP16 = 2
 
 _P = ct.POINTER(pomdp.POMDP)
 _C = ct.POINTER(NovaPOMDPPBVICPU)

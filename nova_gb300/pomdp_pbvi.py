@@ -103,7 +103,7 @@ class POMDPPBVIGPU(npp.NovaPOMDPPBVIGPU):
             raise Exception()
 
     def set_scoring(self, mode):
-        """ npp.SCORING_EXACT or npp.SCORING_BF16 (pomdp_pbvi_set_scoring_gpu). """
+        """ npp.SCORING_EXACT, npp.SCORING_BF16 or npp.SCORING_FP16 (pomdp_pbvi_set_scoring_gpu). """
         result = npp._nova.pomdp_pbvi_set_scoring_gpu(self, int(mode))
         if result != 0:
             raise RuntimeError("pomdp_pbvi_set_scoring_gpu failed with code %d" % result)

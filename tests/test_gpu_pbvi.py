@@ -14,7 +14,7 @@ from nova_gb300 import nova_pomdp_pbvi as npp
 
 pytestmark = pytest.mark.gpu
 
-MODES = [npp.SCORING_EXACT, npp.SCORING_BF16]
+MODES = [npp.SCORING_EXACT, npp.SCORING_BF16, npp.SCORING_FP16]
 
 
 def solve_gpu(model, mode, horizon=None):
@@ -117,3 +117,53 @@ def test_numthreads_must_be_multiple_of_32():
     from nova_gb300 import pomdp_alpha_vectors as pav
     pol = pav.POMDPAlphaVectors()
     assert npp._nova.pomdp_pbvi_execute_gpu(alg.pomdpPtr, alg, pol) == 2  # NOVA_ERROR_INVALID_CUDA_PARAM
+
+
+def _run_mode(model, mode, steps):
+    p = POMDP.from_arrays(model)
+    p.initialize_gpu()
+    alg = POMDPPBVIGPU(p, GammaInitial=model["GammaInitial"])
+    alg.set_scoring(mode)
+    out, stats = [], []
+    for _ in range(steps):
+        alg.update()
+        stats.append(alg.stats())
+        pol = alg.get_policy()
+        out.append((pol.gamma_array(), pol.pi_array()))
+    return out, stats
+
+
+@pytest.mark.parametrize("mode", [npp.SCORING_BF16, npp.SCORING_FP16])
+def test_tensor_core_scoring_is_exact_and_runs(mode):
+    """At a size where the tensor-core path engages (>= 32 distinct alphas),
+    tensor-core scoring with the proven margin gives bit-identical alphas and
+    actions to exact scoring at every step, and the tensor cores decide most
+    rows (few fall back to the exact row scan)."""
+    m = synth.random_pomdp(n=300, m=6, z=12, ns=12, r=700, rz=20, gamma=0.95, horizon=7, seed=5)
+    exact, _ = _run_mode(m, npp.SCORING_EXACT, m["horizon"])
+    tc, stats = _run_mode(m, mode, m["horizon"])
+    for (Ge, pe), (Gt, pt) in zip(exact, tc):
+        np.testing.assert_array_equal(bits(Gt), bits(Ge))
+        np.testing.assert_array_equal(pt, pe)
+    engaged = [s for s in stats if s["scoring"] == mode]
+    assert len(engaged) >= 3, stats
+    rows = m["r"] * m["m"] * m["z"]
+    # BF16's proven margin is about 16x wider than FP16's, so it leaves more
+    # rows to the exact scan (still a minority here).
+    limit = 0.25 if mode == npp.SCORING_BF16 else 0.01
+    for s in engaged:
+        assert s["msGemm"] > 0
+        assert s["rowsOverflow"] <= limit * rows, s
+
+
+@pytest.mark.parametrize("mode", [npp.SCORING_BF16, npp.SCORING_FP16])
+def test_tensor_core_scoring_many_unresolved_rows(mode):
+    """n=512, r=1024: BF16 leaves a large share of rows to the exact scan;
+    every step must still equal exact scoring bit for bit."""
+    m = synth.random_pomdp(n=512, m=8, z=16, ns=16, r=1024, rz=32, gamma=0.95, horizon=5, seed=5)
+    exact, _ = _run_mode(m, npp.SCORING_EXACT, m["horizon"])
+    tc, stats = _run_mode(m, mode, m["horizon"])
+    for (Ge, pe), (Gt, pt) in zip(exact, tc):
+        np.testing.assert_array_equal(bits(Gt), bits(Ge))
+        np.testing.assert_array_equal(pt, pe)
+    assert any(s["scoring"] == mode for s in stats)
