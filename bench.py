@@ -299,18 +299,18 @@ def main():
     value = world * r * args.steps / (ms * 1e-3)
 
     # ---- roofline of the scoring kernel --------------------------------------
-    hbm, bf16, peak_kind = measured_peaks()
+    hbm, tc_peak, peak_kind = measured_peaks()
     n_pad = ((cfg["n"] + 63) // 64) * 64
     gemm = [(s["uniqueAlphas"], s["msGemm"]) for s in stats if s["msGemm"] > 0]
     if gemm:
         flops = [2.0 * r * u * n_pad * cfg["m"] * cfg["z"] for u, _ in gemm]
         achieved = sum(flops) / (sum(t for _, t in gemm) * 1e-3) / 1e12
-        roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
-                    "frac": achieved / bf16, "traffic": None,
+        roofline = {"bound": "tensor", "achieved": achieved, "peak": tc_peak, "unit": "TFLOP/s",
+                    "frac": achieved / tc_peak, "traffic": None,
                     "kernel": "tcgen05 FP16 scoring GEMM (kind::f16, FP32 accumulate in TMEM) with fused top-8 epilogue",
                     "flops_per_launch": flops[-1], "peak_source": peak_kind}
     else:
-        roofline = {"bound": "tensor", "achieved": None, "peak": bf16, "unit": "TFLOP/s", "frac": None,
+        roofline = {"bound": "tensor", "achieved": None, "peak": tc_peak, "unit": "TFLOP/s", "frac": None,
                     "traffic": None, "kernel": "tensor-core scoring did not run (exact scoring only)",
                     "peak_source": peak_kind}
 
