@@ -79,6 +79,26 @@ NOVA_API int mdp_vi_residual_gpu(const MDP *mdp, const MDPVIGPU *vi, double *res
  * device-side error word that bounded waits set instead of hanging. */
 NOVA_API int nova_gb300_device_status(unsigned int *deviceError);
 
+/* Allocation-free V(b) for an alpha-vector policy already in device memory.
+ * This entry point has no counterpart in the reference. It is for callers
+ * that must not call cudaMalloc while they run -- a controller evaluating
+ * its policy inside a real-time loop, where an allocation can stall on
+ * device-wide synchronisation, or a process whose device memory belongs to
+ * another framework's pool. d_Gamma [r][n], d_pi [r] and d_b [n] are device
+ * pointers; *Vb and *a are host results (FP64 value, action of the
+ * maximising alpha, lowest index on ties, as pomdp_pbvi_value_gpu). The call
+ * allocates nothing: its scratch is a fixed device array of
+ * NOVA_VALUE_NOALLOC_MAX_ROWS doubles that every GPU loading the library
+ * keeps until exit; r beyond that limit is rejected with
+ * NOVA_ERROR_INVALID_DATA. Calls share the scratch, so calls that overlap on
+ * the GPU race and must be serialised by the caller. The first call on a
+ * device resolves the scratch's device address for it; make that first call
+ * before any stream capture. Kernels run on the default stream and the call
+ * returns after the result is copied back. */
+#define NOVA_VALUE_NOALLOC_MAX_ROWS 65536u
+NOVA_API int pomdp_alpha_vectors_value_noalloc_gpu(const float *d_Gamma, const unsigned int *d_pi,
+        unsigned int r, unsigned int n, const float *d_b, double *Vb, unsigned int *a);
+
 /* Number of kernels this library has launched since it was loaded. */
 NOVA_API unsigned long long nova_gb300_kernel_launches(void);
 
