@@ -19,6 +19,8 @@
 
 #include "common.h"
 
+#include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include <nova/constants.h>
@@ -106,33 +108,38 @@ __device__ __forceinline__ void residual_commit(double local, ViDeviceState *st,
 }
 
 // One Bellman sweep. G lanes per state, G a power of two in [1, 32], m <= G.
+// The grid is a few waves of resident blocks that stride over 256-thread
+// tiles, so the residual costs two atomics per block, not per tile.
 template <int G, bool VEC>
 __global__ void __launch_bounds__(256) bellman_sweep_kernel(unsigned n, unsigned ns, unsigned m, float gamma,
         const int *__restrict__ S, const float *__restrict__ T, const float *__restrict__ R,
         const float *__restrict__ V, float *__restrict__ Vp, unsigned *__restrict__ pi,
         ViDeviceState *st, double tol, int early_exit) {
     if (early_exit && *(volatile unsigned *)&st->converged) return;  // uniform across the grid
-    const unsigned long long gid = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned s = (unsigned)(gid / G);
-    const unsigned a = (unsigned)(gid % G);
-    const bool active_state = s < n;
-    float q = 0.0f;
-    if (active_state && a < m) q = bellman_q<VEC>(s, a, m, ns, gamma, S, T, R, V);
-
-    // Sequential action scan of mdp_vi_cpu.cpp:55-58 done by the group's lane 0.
+    const unsigned long long tiles = ((unsigned long long)n * G + 255ull) / 256ull;
     const unsigned lane = threadIdx.x & 31;
     const unsigned base = lane & ~(unsigned)(G - 1);
-    float best = __shfl_sync(0xffffffffu, q, base);
-    unsigned besta = 0;
-    for (unsigned k = 1; k < m; k++) {
-        const float qk = __shfl_sync(0xffffffffu, q, base + k);
-        if (qk > best) { best = qk; besta = k; }
-    }
     double local = 0.0;
-    if (active_state && a == 0) {
-        Vp[s] = best;
-        pi[s] = besta;
-        local = fabs((double)best - (double)__ldg(V + s));
+    for (unsigned long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const unsigned long long gid = tile * 256ull + threadIdx.x;
+        const unsigned s = (unsigned)(gid / G);
+        const unsigned a = (unsigned)(gid % G);
+        const bool active_state = s < n;
+        float q = 0.0f;
+        if (active_state && a < m) q = bellman_q<VEC>(s, a, m, ns, gamma, S, T, R, V);
+
+        // Sequential action scan of mdp_vi_cpu.cpp:55-58 done by the group's lane 0.
+        float best = __shfl_sync(0xffffffffu, q, base);
+        unsigned besta = 0;
+        for (unsigned k = 1; k < m; k++) {
+            const float qk = __shfl_sync(0xffffffffu, q, base + k);
+            if (qk > best) { best = qk; besta = k; }
+        }
+        if (active_state && a == 0) {
+            Vp[s] = best;
+            pi[s] = besta;
+            local = fmax(local, fabs((double)best - (double)__ldg(V + s)));
+        }
     }
     residual_commit(local, st, gridDim.x, tol, early_exit != 0);
 }
@@ -160,12 +167,33 @@ __global__ void __launch_bounds__(256) bellman_sweep_wide_kernel(unsigned n, uns
     residual_commit(local, st, gridDim.x, tol, early_exit != 0);
 }
 
+// Resident 256-thread blocks per SM times the SM count of the current device.
+static unsigned resident_blocks() {
+    static std::mutex mu;
+    static unsigned cache[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return 1216u;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (cache[dev] == 0) {
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+            cudaGetLastError();
+            sms = 152;
+        }
+        cache[dev] = (unsigned)sms * 8u;
+    }
+    return cache[dev];
+}
+
 template <int G>
 static void launch_group(unsigned n, unsigned ns, unsigned m, float gamma, const int *S, const float *T,
                          const float *R, const float *V, float *Vp, unsigned *pi, ViDeviceState *st,
                          double tol, int early_exit, bool vec, cudaStream_t stream) {
-    const unsigned long long threads = (unsigned long long)n * G;
-    const unsigned blocks = (unsigned)((threads + 255) / 256);
+    const unsigned long long tiles = ((unsigned long long)n * G + 255ull) / 256ull;
+    const unsigned blocks = (unsigned)std::min<unsigned long long>(tiles, resident_blocks());
     if (vec)
         bellman_sweep_kernel<G, true><<<blocks, 256, 0, stream>>>(n, ns, m, gamma, S, T, R, V, Vp, pi, st, tol, early_exit);
     else
