@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-mdp", action="store_true")
     ap.add_argument("--bf16-steps", type=int, default=2)
+    ap.add_argument("--precision-steps", type=int, default=3)
     return ap.parse_args()
 
 
@@ -205,6 +206,46 @@ def run_reference(args, rank):
     print(json.dumps(out))
 
 
+def run_precision(args):
+    """|V(b0) - V_FP64(b0)| after H backups with the default (FP16 tensor-core)
+    scoring, against the oracle's FP64 restatement of the same backup run from
+    the same GammaInitial. Two workloads: pbvi_n64 over its full horizon, and
+    the n=4096 shapes (m=16, z=32, ns=32, rz=64) with r=256 beliefs, where the
+    FP64 CPU backup takes about a second per step. V(b0) of the GPU policy is
+    its FP64 device reduction (pomdp_pbvi_value_gpu)."""
+    import torch
+    from nova_gb300 import synth
+    from nova_gb300.pomdp import POMDP
+    from nova_gb300.pomdp_pbvi import POMDPPBVIGPU
+    from oracle import oracle as orc
+    out = {}
+    for name, horizon in (("pbvi_n64", None), ("pbvi_n4096_r256", args.precision_steps)):
+        cfg = dict(synth.POMDP_CONFIGS[name])
+        model = synth.random_pomdp(**cfg, seed=args.seed)
+        H = cfg["horizon"] if horizon is None else horizon
+        p = POMDP.from_arrays(model)
+        p.initialize_gpu()
+        alg = POMDPPBVIGPU(p, GammaInitial=model["GammaInitial"])
+        for _ in range(H):
+            alg.update()
+        b0 = synth.dense_belief(model, 0)
+        Vg, _ = alg.value(b0)
+        del alg
+        p.uninitialize_gpu()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        G = model["GammaInitial"].astype(np.float64)
+        for _ in range(H):
+            G, _ = orc.pbvi_update_f64(model, G)
+        V64 = float(np.max(G @ b0.astype(np.float64)))
+        out[name] = {"horizon": H, "r": cfg["r"], "V_b0_fp64": V64, "V_b0": Vg, "dV_b0": abs(Vg - V64),
+                     "oracle_seconds": time.perf_counter() - t0}
+    out["max_dV_b0"] = max(v["dV_b0"] for v in out.values())
+    out["note"] = ("the tensor-core path's alphas are bit-identical to the plain FP32 path's, so this is the "
+                   "FP32 algorithm's own error against FP64")
+    return out
+
+
 def run_mdp(args, dist_rank):
     """Bellman sweep n=2^20, m=8, ns=16 (memory-bound): GB/s of algorithmic bytes.
     Sweeps are timed through mdp_vi_execute_gpu (sweeps queued back to back):
@@ -236,7 +277,13 @@ def run_mdp(args, dist_rank):
             raise RuntimeError("mdp_vi_execute_gpu failed: %d" % rc)
         return e0.elapsed_time(e1)
 
+    from nova_gb300 import mdp_vi as mvi
+    mvi.set_tiling(nmvi.TILING_NEVER)
     solve(20)
+    gather_ms = (solve(201) - solve(1)) / 200.0
+    mvi.set_tiling(nmvi.TILING_AUTO)
+    solve(20)
+    kernel = {1: "tiled (shared-memory V tiles)", 2: "per-row gather"}.get(mvi.tiling_status(), "unknown")
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
         t1 = solve(1)
         t201 = solve(201)
@@ -249,6 +296,7 @@ def run_mdp(args, dist_rank):
     pol, nsweeps, resid = MDPValueIterationGPU(m, Vinitial=np.zeros(md["n"], np.float32)).solve_until_converged(
         tol=1e-6, maxSweeps=cfg["horizon"])
     return {"workload": "vi_n1m (n=2^20,m=8,ns=16,gamma=0.99)", "ms_per_sweep": ms, "GB_per_s": gbs,
+            "sweep_kernel": kernel, "gather_ms_per_sweep": gather_ms,
             "algorithmic_bytes_per_sweep": alg_bytes, "frac_of_hbm": gbs / hbm, "clocks": clocks.summary(),
             "converged_sweeps": nsweeps, "final_residual_fp64": resid, "converged": bool(resid < 1e-6),
             "note": "FP32 values near 78 have a 7.6e-6 ulp; the FP64 residual of the FP32 iteration stalls above 1e-6"}
@@ -408,6 +456,7 @@ def main():
                          "(r=%d) in %.1f s on %d threads" % (pairs, cfg["r"], wall, cores)}
 
     mdp = None if args.no_mdp else run_mdp(args, rank)
+    precision = run_precision(args) if (rank == 0 and args.precision_steps > 0) else None
 
     last = stats[-1]
     out = {
@@ -431,6 +480,7 @@ def main():
         "unique_alphas": [s["uniqueAlphas"] for s in stats],
         "rows_rescored": last["rowsMultiCand"], "pairs_full_exact": last["rowsOverflow"],
         "mdp_vi": mdp,
+        "precision_vs_fp64": precision,
     }
     if rank == 0:
         print(json.dumps(out))

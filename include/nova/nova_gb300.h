@@ -74,6 +74,30 @@ NOVA_API int mdp_vi_execute_until_converged_gpu(const MDP *mdp, MDPVIGPU *vi,
  * mdp_vi_update_gpu on this solver. */
 NOVA_API int mdp_vi_residual_gpu(const MDP *mdp, const MDPVIGPU *vi, double *residual);
 
+/* Sweep kernel selection. Replaces nothing in the reference (its sweep,
+ * mdp_vi_gpu.cu:37-87, has one form). When every (s, a) row lists its valid
+ * successors in ascending state order, the sweep can stage V in shared-memory
+ * tiles and add each row's products tile by tile, which is the reference's
+ * own order (mdp_vi_cpu.cpp:45-52), so results stay bit-identical; other
+ * models use the per-row gather sweep. A solver builds its tile plan (8 bytes
+ * per successor entry) at its first sweep after initialize, from the model's
+ * S and T as they are then.
+ *  mode: NOVA_VI_TILING_AUTO (default: tiled for models with at least 2^22
+ *        successor entries), NOVA_VI_TILING_ALWAYS (whenever the model
+ *        qualifies), NOVA_VI_TILING_NEVER.
+ *  tileStates: states per shared-memory tile of V, a multiple of 4 in
+ *        [64, 16384], or 0 for the default 12288.
+ * The setting is process-wide and applies to plans built after the call. */
+#define NOVA_VI_TILING_AUTO   0u
+#define NOVA_VI_TILING_ALWAYS 1u
+#define NOVA_VI_TILING_NEVER  2u
+NOVA_API int mdp_vi_set_tiling_gpu(unsigned int mode, unsigned int tileStates);
+
+/* Sweep kernel of an initialized solver struct (an MDPVIGPU or MDPVICPU):
+ * 0 = no sweep yet, 1 = tiled, 2 = per-row gather. With vi == NULL, the
+ * status of the plan built last in this process. */
+NOVA_API int mdp_vi_tiling_status_gpu(const void *vi, unsigned int *status);
+
 /* Library self-description: 1 if the library was built for sm_103a and a
  * device is present, 0 otherwise; *deviceError receives (and clears) the
  * device-side error word that bounded waits set instead of hanging. */

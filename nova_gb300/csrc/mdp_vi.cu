@@ -17,7 +17,7 @@
 //   * The sweep's Bellman residual max_s |V'(s) - V(s)| is reduced in FP64 in
 //     the same pass (one atomic per block).
 
-#include "common.h"
+#include "vi.h"
 
 #include <algorithm>
 #include <mutex>
@@ -36,16 +36,6 @@ using nova::MDPVIGPU;
 using nova::MDPValueFunction;
 
 namespace nova_gb300 {
-
-// Convergence bookkeeping shared by the sweep kernels of one solver.
-struct ViDeviceState {
-    unsigned long long resid_bits;   // max |V' - V| of the current sweep, as FP64 bits
-    unsigned int blocks_done;        // blocks finished in the current sweep
-    unsigned int sweeps_done;        // sweeps that ran (early-exit mode)
-    unsigned int converged;          // 1 once a sweep's residual fell below tol
-    unsigned int pad;
-    double last_resid;               // residual of the last finished sweep
-};
 
 template <bool VEC>
 __device__ __forceinline__ float bellman_q(unsigned s, unsigned a, unsigned m, unsigned ns, float gamma,
@@ -77,34 +67,6 @@ __device__ __forceinline__ float bellman_q(unsigned s, unsigned a, unsigned m, u
         }
     }
     return q;
-}
-
-__device__ __forceinline__ void residual_commit(double local, ViDeviceState *st, unsigned nblocks, double tol,
-                                                bool early_exit) {
-    // Block max, then one FP64 atomic max (non-negative doubles order like
-    // their bit patterns), then the last block closes the sweep.
-    __shared__ double red[32];
-    for (int off = 16; off > 0; off >>= 1) local = fmax(local, __shfl_xor_sync(0xffffffffu, local, off));
-    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) red[warp] = local;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double m = 0.0;
-        for (unsigned w = 0; w < (blockDim.x + 31) / 32; w++) m = fmax(m, red[w]);
-        atomicMax(&st->resid_bits, (unsigned long long)__double_as_longlong(m));
-        __threadfence();
-        const unsigned done = atomicAdd(&st->blocks_done, 1u);
-        if (done == nblocks - 1) {
-            __threadfence();
-            const double r = __longlong_as_double((long long)atomicAdd(&st->resid_bits, 0ull));
-            st->last_resid = r;
-            st->resid_bits = 0ull;
-            st->blocks_done = 0u;
-            st->sweeps_done += 1u;
-            if (early_exit && r < tol) st->converged = 1u;
-            __threadfence();
-        }
-    }
 }
 
 // One Bellman sweep. G lanes per state, G a power of two in [1, 32], m <= G.
@@ -203,7 +165,15 @@ static void launch_group(unsigned n, unsigned ns, unsigned m, float gamma, const
 // Launch one sweep V -> Vp. Returns NOVA_SUCCESS or a launch error.
 static int launch_sweep(const MDP *mdp, const int *S, const float *T, const float *R, const float *V, float *Vp,
                         unsigned *pi, ViDeviceState *st, double tol, int early_exit, cudaStream_t stream,
-                        const char *fn) {
+                        ViTilePlan *plan, const char *fn) {
+    if (plan != nullptr) {
+        // The plan is built at the solver's first sweep from the model as it
+        // is then; the tiled sweep needs V 16-byte aligned for cp.async.
+        int rc = vi_plan_build(plan, mdp, S, T, stream, fn);
+        if (rc != NOVA_SUCCESS) return rc;
+        if (plan->status == ViTilePlan::kTiled && ((uintptr_t)V % 16u) == 0u)
+            return vi_tiled_sweep(plan, mdp, R, V, Vp, pi, st, tol, early_exit, stream, fn);
+    }
     const unsigned n = mdp->n, ns = mdp->ns, m = mdp->m;
     const float gamma = mdp->gamma;
     const bool vec = (ns % 4u) == 0u && ((uintptr_t)S % 16u) == 0u && ((uintptr_t)T % 16u) == 0u;
@@ -238,6 +208,7 @@ struct ViGpuWorkspace : Workspace {
     float *d_V = nullptr, *d_VPrime = nullptr;
     unsigned *d_pi = nullptr;
     ViDeviceState *st = nullptr;
+    ViTilePlan plan;
     ~ViGpuWorkspace() override {
         cudaFree(d_V); cudaFree(d_VPrime); cudaFree(d_pi); cudaFree(st);
     }
@@ -252,6 +223,7 @@ struct ViCpuWorkspace : Workspace {
     ViDeviceState *st = nullptr;
     float *hostV = nullptr, *hostVPrime = nullptr;   // the arrays this library gave the struct
     unsigned *hostPi = nullptr;
+    ViTilePlan plan;
     ~ViCpuWorkspace() override {
         cudaFree(S); cudaFree(T); cudaFree(R); cudaFree(V); cudaFree(VPrime); cudaFree(pi); cudaFree(st);
     }
@@ -358,10 +330,14 @@ extern "C" int mdp_vi_initialize_gpu(const MDP *mdp, MDPVIGPU *vi) {
 
 static int vi_gpu_sweep(const MDP *mdp, MDPVIGPU *vi, double tol, int early_exit, bool sync, const char *fn) {
     ViDeviceState *st = nullptr;
+    ViTilePlan *plan = nullptr;
     {
         std::lock_guard<std::mutex> lock(registry_mutex());
         auto *ws = find_workspace<ViGpuWorkspace>(vi);
-        if (ws != nullptr) st = ws->st;
+        if (ws != nullptr) {
+            st = ws->st;
+            plan = &ws->plan;
+        }
     }
     if (st == nullptr) {
         NOVA_ERR(fn, "The solver is not initialized.");
@@ -370,7 +346,7 @@ static int vi_gpu_sweep(const MDP *mdp, MDPVIGPU *vi, double tol, int early_exit
     const bool even = (vi->currentHorizon % 2u) == 0u;
     const float *src = even ? vi->d_V : vi->d_VPrime;
     float *dst = even ? vi->d_VPrime : vi->d_V;
-    int rc = launch_sweep(mdp, mdp->d_S, mdp->d_T, mdp->d_R, src, dst, vi->d_pi, st, tol, early_exit, 0, fn);
+    int rc = launch_sweep(mdp, mdp->d_S, mdp->d_T, mdp->d_R, src, dst, vi->d_pi, st, tol, early_exit, 0, plan, fn);
     if (rc != NOVA_SUCCESS) return rc;
     if (sync) {
         rc = sync_device(fn);
@@ -492,9 +468,12 @@ extern "C" int mdp_vi_execute_until_converged_gpu(const MDP *mdp, MDPVIGPU *vi, 
     rc = mdp_vi_initialize_gpu(mdp, vi);
     if (rc != NOVA_SUCCESS) return rc;
     ViDeviceState *st = nullptr;
+    ViTilePlan *plan = nullptr;
     {
         std::lock_guard<std::mutex> lock(registry_mutex());
-        st = find_workspace<ViGpuWorkspace>(vi)->st;
+        auto *ws = find_workspace<ViGpuWorkspace>(vi);
+        st = ws->st;
+        plan = &ws->plan;
     }
     // Sweeps are queued in batches; a sweep launched after convergence
     // returns at once, so the device state ends at the first converged sweep.
@@ -508,7 +487,7 @@ extern "C" int mdp_vi_execute_until_converged_gpu(const MDP *mdp, MDPVIGPU *vi, 
             const bool even = (launched % 2u) == 0u;
             const float *src = even ? vi->d_V : vi->d_VPrime;
             float *dst = even ? vi->d_VPrime : vi->d_V;
-            rc = launch_sweep(mdp, mdp->d_S, mdp->d_T, mdp->d_R, src, dst, vi->d_pi, st, tol, 1, 0, fn);
+            rc = launch_sweep(mdp, mdp->d_S, mdp->d_T, mdp->d_R, src, dst, vi->d_pi, st, tol, 1, 0, plan, fn);
             if (rc != NOVA_SUCCESS) { mdp_vi_uninitialize_gpu(mdp, vi); return rc; }
             launched++;
         }
@@ -617,7 +596,7 @@ extern "C" int mdp_vi_update_cpu(const MDP *mdp, MDPVICPU *vi) {
     // Host arrays are the source of truth between calls (callers may edit them).
     int rc = h2d(ws->V, hsrc, n * sizeof(float), fn, "the value function");
     if (rc != NOVA_SUCCESS) return rc;
-    rc = launch_sweep(mdp, ws->S, ws->T, ws->R, ws->V, ws->VPrime, ws->pi, ws->st, 0.0, 0, 0, fn);
+    rc = launch_sweep(mdp, ws->S, ws->T, ws->R, ws->V, ws->VPrime, ws->pi, ws->st, 0.0, 0, 0, &ws->plan, fn);
     if (rc != NOVA_SUCCESS) return rc;
     rc = d2h(hdst, ws->VPrime, n * sizeof(float), fn, "the value function (prime)");
     if (rc != NOVA_SUCCESS) return rc;
@@ -664,7 +643,7 @@ extern "C" int mdp_vi_execute_cpu(const MDP *mdp, MDPVICPU *vi, MDPValueFunction
     while (rc == NOVA_SUCCESS && vi->currentHorizon < mdp->horizon) {
         const bool even = (vi->currentHorizon % 2u) == 0u;
         rc = launch_sweep(mdp, ws->S, ws->T, ws->R, even ? ws->V : ws->VPrime, even ? ws->VPrime : ws->V, ws->pi,
-                          ws->st, 0.0, 0, 0, fn);
+                          ws->st, 0.0, 0, 0, &ws->plan, fn);
         if (rc == NOVA_SUCCESS) vi->currentHorizon++;
     }
     if (rc == NOVA_SUCCESS) rc = sync_device(fn);
@@ -678,4 +657,26 @@ extern "C" int mdp_vi_execute_cpu(const MDP *mdp, MDPVICPU *vi, MDPValueFunction
         return rc;
     }
     return mdp_vi_uninitialize_cpu(mdp, vi);
+}
+
+extern "C" int mdp_vi_tiling_status_gpu(const void *vi, unsigned int *status) {
+    if (status == nullptr) {
+        NOVA_ERR("mdp_vi_tiling_status_gpu", "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    if (vi == nullptr) {
+        *status = vi_last_plan_status();
+        return NOVA_SUCCESS;
+    }
+    std::lock_guard<std::mutex> lock(registry_mutex());
+    if (auto *g = find_workspace<ViGpuWorkspace>(vi)) {
+        *status = g->plan.status;
+        return NOVA_SUCCESS;
+    }
+    if (auto *c = find_workspace<ViCpuWorkspace>(vi)) {
+        *status = c->plan.status;
+        return NOVA_SUCCESS;
+    }
+    NOVA_ERR("mdp_vi_tiling_status_gpu", "The solver is not initialized.");
+    return NOVA_ERROR_INVALID_DATA;
 }

@@ -96,3 +96,23 @@ class MDPValueIterationGPU(nmvi.NovaMDPValueIterationGPU):
         if result != 0:
             raise RuntimeError("mdp_vi_execute_until_converged_gpu failed with code %d" % result)
         return policy, sweeps.value, resid.value
+
+
+def set_tiling(mode, tileStates=0):
+    """ Select the Bellman sweep kernel for solvers that build their plan after
+    this call (mdp_vi_set_tiling_gpu): nova_mdp_vi.TILING_AUTO, _ALWAYS or
+    _NEVER, and the states per shared-memory tile (0 = default). """
+    result = nmvi._nova.mdp_vi_set_tiling_gpu(int(mode), int(tileStates))
+    if result != 0:
+        raise ValueError("mdp_vi_set_tiling_gpu rejected mode=%r tileStates=%r" % (mode, tileStates))
+
+
+def tiling_status(solver=None):
+    """ 0 = no sweep yet, 1 = tiled sweep, 2 = per-row gather sweep, for an
+    initialized solver object, or for the plan built last when solver is None. """
+    st = ct.c_uint(0)
+    ptr = None if solver is None else ct.addressof(solver)
+    result = nmvi._nova.mdp_vi_tiling_status_gpu(ptr, ct.byref(st))
+    if result != 0:
+        raise RuntimeError("mdp_vi_tiling_status_gpu failed with code %d" % result)
+    return st.value

@@ -43,3 +43,9 @@ _G = ct.POINTER(NovaMDPValueIterationGPU)
 _nova.mdp_vi_execute_until_converged_gpu.argtypes = (_M, _G, _F, ct.c_double, ct.c_uint, ct.POINTER(ct.c_uint),
                                                      ct.POINTER(ct.c_double))
 _nova.mdp_vi_residual_gpu.argtypes = (_M, _G, ct.POINTER(ct.c_double))
+_nova.mdp_vi_set_tiling_gpu.argtypes = (ct.c_uint, ct.c_uint)
+_nova.mdp_vi_tiling_status_gpu.argtypes = (ct.c_void_p, ct.POINTER(ct.c_uint))
+
+TILING_AUTO = 0
+TILING_ALWAYS = 1
+TILING_NEVER = 2

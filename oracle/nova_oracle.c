@@ -14,9 +14,12 @@
  * (build with -ffp-contract=off): the reference is built by g++ for x86-64
  * without FMA, and these functions reproduce its operation order exactly.
  */
+#define _POSIX_C_SOURCE 200809L
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
+#include <pthread.h>
+#include <unistd.h>
 
 #define ORACLE_FLT_MIN (-1e+10f)   /* nova's FLT_MIN, include/nova/constants.h:34 */
 
@@ -226,26 +229,46 @@ void oracle_pbvi_update_factored(unsigned n, unsigned ns, unsigned m, unsigned z
 }
 
 /* FP64 restatement of the same backup (factored form, all arithmetic in
- * double, same argmax rules): the reference solution for V(b0) error. */
-void oracle_pbvi_update_f64(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz, double gamma,
-                            const int *S, const double *T, const double *O, const double *R, const int *Z,
-                            const double *B, const double *Gamma, double *GammaPrime, unsigned *pi) {
+ * double, same argmax rules): the reference solution for V(b0) error.
+ * Actions are independent until the final action argmax, so they are spread
+ * over host threads (each with its own projection buffer). */
+typedef struct {
+    unsigned n, ns, m, z, r, rz;
+    double gamma;
+    const int *S;
+    const double *T, *O;
+    const int *Z;
+    const double *B, *Gamma;
+    double *alphaAll;
+    unsigned a0, astep;
+} F64Job;
+
+static void *f64_action_worker(void *arg) {
+    const F64Job *J = (const F64Job *)arg;
+    const unsigned n = J->n, ns = J->ns, m = J->m, z = J->z, r = J->r, rz = J->rz;
     double *Proj = (double *)malloc(sizeof(double) * (size_t)r * n);
-    double *alphaAll = (double *)malloc(sizeof(double) * (size_t)r * m * n);
-    for (unsigned i = 0; i < r; i++)
-        for (unsigned a = 0; a < m; a++)
-            for (unsigned s = 0; s < n; s++) alphaAll[((size_t)i * m + a) * n + s] = R[s * m + a];
-    for (unsigned a = 0; a < m; a++) {
+    double *C = (double *)malloc(sizeof(double) * (size_t)n * ns);
+    for (unsigned a = J->a0; a < m; a += J->astep) {
         for (unsigned o = 0; o < z; o++) {
+            /* C = O(a, s', o) * T(s, a, l), the first product of O*T*Gamma. */
+            for (unsigned s = 0; s < n; s++)
+                for (unsigned l = 0; l < ns; l++) {
+                    int sp = J->S[(size_t)s * m * ns + a * ns + l];
+                    C[(size_t)s * ns + l] = sp < 0 ? 0.0
+                        : J->O[(size_t)a * n * z + (size_t)sp * z + o] * J->T[(size_t)s * m * ns + a * ns + l];
+                }
             for (unsigned j = 0; j < r; j++) {
+                const double *g = J->Gamma + (size_t)j * n;
                 for (unsigned s = 0; s < n; s++) {
+                    const int *Srow = J->S + (size_t)s * m * ns + a * ns;
+                    const double *Crow = C + (size_t)s * ns;
                     double v = 0.0;
                     for (unsigned l = 0; l < ns; l++) {
-                        int sp = S[s * m * ns + a * ns + l];
+                        int sp = Srow[l];
                         if (sp < 0) break;
-                        v += O[a * n * z + sp * z + o] * T[s * m * ns + a * ns + l] * Gamma[(size_t)j * n + sp];
+                        v += Crow[l] * g[sp];
                     }
-                    Proj[(size_t)j * n + s] = v * gamma;
+                    Proj[(size_t)j * n + s] = v * J->gamma;
                 }
             }
             for (unsigned i = 0; i < r; i++) {
@@ -254,26 +277,57 @@ void oracle_pbvi_update_f64(unsigned n, unsigned ns, unsigned m, unsigned z, uns
                 for (unsigned j = 0; j < r; j++) {
                     double value = 0.0;
                     for (unsigned k = 0; k < rz; k++) {
-                        int s = Z[i * rz + k];
+                        int s = J->Z[(size_t)i * rz + k];
                         if (s < 0) break;
-                        value += Proj[(size_t)j * n + s] * B[i * rz + k];
+                        value += Proj[(size_t)j * n + s] * J->B[(size_t)i * rz + k];
                     }
                     if (value > bestValue) { bestj = j; bestValue = value; }
                 }
-                double *alpha = alphaAll + ((size_t)i * m + a) * n;
+                double *alpha = J->alphaAll + ((size_t)i * m + a) * n;
                 for (unsigned s = 0; s < n; s++) alpha[s] += Proj[(size_t)bestj * n + s];
             }
         }
     }
+    free(C);
+    free(Proj);
+    return NULL;
+}
+
+void oracle_pbvi_update_f64(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz, double gamma,
+                            const int *S, const double *T, const double *O, const double *R, const int *Z,
+                            const double *B, const double *Gamma, double *GammaPrime, unsigned *pi) {
+    double *alphaAll = (double *)malloc(sizeof(double) * (size_t)r * m * n);
+    for (unsigned i = 0; i < r; i++)
+        for (unsigned a = 0; a < m; a++)
+            for (unsigned s = 0; s < n; s++) alphaAll[((size_t)i * m + a) * n + s] = R[(size_t)s * m + a];
+    long cores = sysconf(_SC_NPROCESSORS_ONLN);
+    unsigned nt = (unsigned)(cores < 1 ? 1 : cores);
+    if (nt > m) nt = m;
+    if (nt > 64) nt = 64;
+    F64Job jobs[64];
+    pthread_t tid[64];
+    for (unsigned t = 0; t < nt; t++) {
+        F64Job J = {n, ns, m, z, r, rz, gamma, S, T, O, Z, B, Gamma, alphaAll, t, nt};
+        jobs[t] = J;
+    }
+    unsigned started = 0;
+    for (unsigned t = 1; t < nt; t++) {
+        if (pthread_create(&tid[t], NULL, f64_action_worker, &jobs[t]) != 0) break;
+        started = t;
+    }
+    f64_action_worker(&jobs[0]);
+    for (unsigned t = 1; t <= started; t++) pthread_join(tid[t], NULL);
+    /* Actions of threads that failed to start run here. */
+    for (unsigned t = started + 1; t < nt; t++) f64_action_worker(&jobs[t]);
     for (unsigned i = 0; i < r; i++) {
         double bestValue = -1e10;
         for (unsigned a = 0; a < m; a++) {
             const double *alpha = alphaAll + ((size_t)i * m + a) * n;
             double value = 0.0;
             for (unsigned k = 0; k < rz; k++) {
-                int s = Z[i * rz + k];
+                int s = Z[(size_t)i * rz + k];
                 if (s < 0) break;
-                value += alpha[s] * B[i * rz + k];
+                value += alpha[s] * B[(size_t)i * rz + k];
             }
             if (value > bestValue) {
                 memcpy(&GammaPrime[(size_t)i * n], alpha, n * sizeof(double));
@@ -282,7 +336,6 @@ void oracle_pbvi_update_f64(unsigned n, unsigned ns, unsigned m, unsigned z, uns
             }
         }
     }
-    free(Proj);
     free(alphaAll);
 }
 

@@ -105,3 +105,117 @@ def test_action_counts_and_until_converged(m_actions):
     np.testing.assert_array_equal(pol.pi_array(), pi)
     Vprev, _ = orc.mdp_vi_solve(md, horizon=sweeps - 1, VInitial=np.zeros(md["n"], np.float32))
     assert resid == np.max(np.abs(V.astype(np.float64) - Vprev.astype(np.float64)))
+
+
+# ---------------------------------------------------------------------------
+# Column-tiled sweep (shared-memory V tiles; rows with ascending successors)
+# ---------------------------------------------------------------------------
+
+@pytest.fixture
+def tiling():
+    from nova_gb300 import mdp_vi
+    yield mdp_vi
+    mdp_vi.set_tiling(nmvi.TILING_AUTO, 0)
+
+
+def ragged_sorted_mdp(n, m, ns, seed, gamma=0.95, horizon=10):
+    """Random MDP whose rows keep ascending successors but stop early (-1),
+    including rows with no successor at all."""
+    md = synth.random_mdp(n=n, m=m, ns=ns, gamma=gamma, horizon=horizon, seed=seed)
+    rng = np.random.default_rng(seed + 100)
+    lens = rng.integers(0, ns + 1, size=(n, m))
+    cut = np.arange(ns)[None, None, :] >= lens[:, :, None]
+    md["S"] = np.where(cut, -1, md["S"]).astype(np.int32)
+    md["T"] = np.where(cut, 0.0, md["T"]).astype(np.float32)
+    return md
+
+
+@pytest.mark.parametrize("n,m_actions,ns,tile", [(3000, 5, 12, 256), (1000, 1, 7, 64), (999, 33, 5, 100), (700, 3, 20, 0),
+                                                 (4097, 8, 16, 0)])
+def test_tiled_sweeps_match_oracle(tiling, n, m_actions, ns, tile):
+    tiling.set_tiling(nmvi.TILING_ALWAYS, tile)
+    md = ragged_sorted_mdp(n, m_actions, ns, seed=n + m_actions)
+    m = MDP.from_arrays(md)
+    m.initialize_gpu()
+    alg = MDPValueIterationGPU(m, Vinitial=np.zeros(md["n"], np.float32))
+    V = np.zeros(md["n"], np.float32)
+    for h in range(6):
+        assert nmvi._nova.mdp_vi_update_gpu(alg.mdpPtr, alg) == 0
+        assert tiling.tiling_status(alg) == 1
+        Vn, pi = orc.mdp_vi_sweep(md, V)
+        resid = ct.c_double(0)
+        assert nmvi._nova.mdp_vi_residual_gpu(alg.mdpPtr, alg, ct.byref(resid)) == 0
+        assert resid.value == np.max(np.abs(Vn.astype(np.float64) - V.astype(np.float64)))
+        V = Vn
+    from nova_gb300 import mdp_value_function as mvf
+    pol = mvf.MDPValueFunction()
+    assert nmvi._nova.mdp_vi_get_policy_gpu(alg.mdpPtr, alg, pol) == 0
+    np.testing.assert_array_equal(bits(pol.V_array()), bits(V))
+    np.testing.assert_array_equal(pol.pi_array(), pi)
+
+
+def test_tiled_execute_until_converged_and_cpu_api(tiling):
+    tiling.set_tiling(nmvi.TILING_ALWAYS, 512)
+    md = ragged_sorted_mdp(2500, 4, 6, seed=9, gamma=0.9, horizon=40)
+    m = MDP.from_arrays(md)
+    m.initialize_gpu()
+    V, pi = orc.mdp_vi_solve(md, horizon=40, VInitial=np.zeros(md["n"], np.float32))
+    pol = MDPValueIterationGPU(m, Vinitial=np.zeros(md["n"], np.float32)).solve()
+    assert tiling.tiling_status() == 1
+    np.testing.assert_array_equal(bits(pol.V_array()), bits(V))
+    np.testing.assert_array_equal(pol.pi_array(), pi)
+    pol = MDPValueIterationCPU(m, Vinitial=np.zeros(md["n"], np.float32)).solve()
+    assert tiling.tiling_status() == 1
+    np.testing.assert_array_equal(bits(pol.V_array()), bits(V))
+    np.testing.assert_array_equal(pol.pi_array(), pi)
+    pol, sweeps, resid = MDPValueIterationGPU(m, Vinitial=np.zeros(md["n"], np.float32)).solve_until_converged(
+        tol=1e-4, maxSweeps=300)
+    assert resid < 1e-4 and 0 < sweeps < 300
+    V, pi = orc.mdp_vi_solve(md, horizon=sweeps, VInitial=np.zeros(md["n"], np.float32))
+    np.testing.assert_array_equal(bits(pol.V_array()), bits(V))
+    np.testing.assert_array_equal(pol.pi_array(), pi)
+
+
+def test_unsorted_rows_keep_gather_sweep(tiling):
+    tiling.set_tiling(nmvi.TILING_ALWAYS, 256)
+    md = synth.random_mdp(n=1500, m=3, ns=8, gamma=0.95, horizon=12, seed=21)
+    rng = np.random.default_rng(5)
+    perm = rng.permuted(np.broadcast_to(np.arange(8), md["S"].shape), axis=2)
+    md["S"] = np.take_along_axis(md["S"], perm, axis=2).astype(np.int32)
+    md["T"] = np.take_along_axis(md["T"], perm, axis=2).astype(np.float32)
+    m = MDP.from_arrays(md)
+    m.initialize_gpu()
+    alg = MDPValueIterationGPU(m, Vinitial=np.zeros(md["n"], np.float32))
+    assert nmvi._nova.mdp_vi_update_gpu(alg.mdpPtr, alg) == 0
+    assert tiling.tiling_status(alg) == 2
+    pol = MDPValueIterationGPU(m, Vinitial=np.zeros(md["n"], np.float32)).solve()
+    V, pi = orc.mdp_vi_solve(md, horizon=12, VInitial=np.zeros(md["n"], np.float32))
+    np.testing.assert_array_equal(bits(pol.V_array()), bits(V))
+    np.testing.assert_array_equal(pol.pi_array(), pi)
+
+
+def test_tiled_equals_gather_at_full_size(tiling):
+    """n = 2^20, m = 8, ns = 16: the tiled sweep (chosen automatically) and the
+    per-row sweep give the same bits after 12 sweeps, and the first sweep
+    equals the oracle's."""
+    cfg = synth.MDP_CONFIGS["vi_n1m"]
+    md = synth.random_mdp(n=cfg["n"], m=cfg["m"], ns=cfg["ns"], gamma=cfg["gamma"], horizon=12, seed=0)
+    m = MDP.from_arrays(md)
+    m.initialize_gpu()
+    out = {}
+    for mode in (nmvi.TILING_AUTO, nmvi.TILING_NEVER):
+        tiling.set_tiling(mode, 0)
+        pol = MDPValueIterationGPU(m, Vinitial=np.zeros(md["n"], np.float32)).solve()
+        out[mode] = (pol.V_array().copy(), pol.pi_array().copy(), tiling.tiling_status())
+    assert out[nmvi.TILING_AUTO][2] == 1 and out[nmvi.TILING_NEVER][2] == 2
+    np.testing.assert_array_equal(bits(out[nmvi.TILING_AUTO][0]), bits(out[nmvi.TILING_NEVER][0]))
+    np.testing.assert_array_equal(out[nmvi.TILING_AUTO][1], out[nmvi.TILING_NEVER][1])
+    tiling.set_tiling(nmvi.TILING_AUTO, 0)
+    alg = MDPValueIterationGPU(m, Vinitial=np.zeros(md["n"], np.float32))
+    assert nmvi._nova.mdp_vi_update_gpu(alg.mdpPtr, alg) == 0
+    from nova_gb300 import mdp_value_function as mvf
+    pol = mvf.MDPValueFunction()
+    assert nmvi._nova.mdp_vi_get_policy_gpu(alg.mdpPtr, alg, pol) == 0
+    V1, pi1 = orc.mdp_vi_sweep(md, np.zeros(md["n"], np.float32))
+    np.testing.assert_array_equal(bits(pol.V_array()), bits(V1))
+    np.testing.assert_array_equal(pol.pi_array(), pi1)
