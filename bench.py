@@ -208,41 +208,36 @@ def run_reference(args, rank):
 
 def run_precision(args):
     """|V(b0) - V_FP64(b0)| after H backups with the default (FP16 tensor-core)
-    scoring, against the oracle's FP64 restatement of the same backup run from
-    the same GammaInitial. Two workloads: pbvi_n64 over its full horizon, and
-    the n=4096 shapes (m=16, z=32, ns=32, rz=64) with r=256 beliefs, where the
-    FP64 CPU backup takes about a second per step. V(b0) of the GPU policy is
-    its FP64 device reduction (pomdp_pbvi_value_gpu)."""
-    import torch
+    scoring. Two FP64 references from the oracle, on the same GammaInitial:
+    `dV_b0` re-evaluates the GPU run's own selections (recorded actions,
+    per-observation alphas and final argmax) in FP64, which isolates the
+    arithmetic error; `dV_b0_free_fp64_run` is an independent FP64 PBVI run,
+    whose own argmax choices can part from the FP32 ones at near-ties. Two
+    workloads: pbvi_n64 over its full horizon, and the n=4096 shapes (m=16,
+    z=32, ns=32, rz=64) with r=256 beliefs."""
     from nova_gb300 import synth
-    from nova_gb300.pomdp import POMDP
-    from nova_gb300.pomdp_pbvi import POMDPPBVIGPU
+    from nova_gb300.pomdp_adjoint import pbvi_record_and_adjoint
     from oracle import oracle as orc
     out = {}
     for name, horizon in (("pbvi_n64", None), ("pbvi_n4096_r256", args.precision_steps)):
         cfg = dict(synth.POMDP_CONFIGS[name])
         model = synth.random_pomdp(**cfg, seed=args.seed)
         H = cfg["horizon"] if horizon is None else horizon
-        p = POMDP.from_arrays(model)
-        p.initialize_gpu()
-        alg = POMDPPBVIGPU(p, GammaInitial=model["GammaInitial"])
-        for _ in range(H):
-            alg.update()
         b0 = synth.dense_belief(model, 0)
-        Vg, _ = alg.value(b0)
-        del alg
-        p.uninitialize_gpu()
-        torch.cuda.synchronize()
+        Vg, istar, _, _, _, _, acts, sels = pbvi_record_and_adjoint(model, b0, H, 10)
         t0 = time.perf_counter()
+        Vfix, _ = orc.pbvi_fixed_forward_f64(model, model["GammaInitial"], acts, sels, b0, istar=istar)
         G = model["GammaInitial"].astype(np.float64)
         for _ in range(H):
             G, _ = orc.pbvi_update_f64(model, G)
-        V64 = float(np.max(G @ b0.astype(np.float64)))
-        out[name] = {"horizon": H, "r": cfg["r"], "V_b0_fp64": V64, "V_b0": Vg, "dV_b0": abs(Vg - V64),
+        Vfree = float(np.max(G @ b0.astype(np.float64)))
+        out[name] = {"horizon": H, "r": cfg["r"], "V_b0": Vg, "V_b0_fp64_same_selections": Vfix,
+                     "dV_b0": abs(Vg - Vfix), "V_b0_free_fp64_run": Vfree, "dV_b0_free_fp64_run": abs(Vg - Vfree),
                      "oracle_seconds": time.perf_counter() - t0}
     out["max_dV_b0"] = max(v["dV_b0"] for v in out.values())
-    out["note"] = ("the tensor-core path's alphas are bit-identical to the plain FP32 path's, so this is the "
-                   "FP32 algorithm's own error against FP64")
+    out["note"] = ("tensor-core alphas are bit-identical to the plain FP32 path's; dV_b0 is their FP32 rounding "
+                   "against FP64 on the same selections, dV_b0_free_fp64_run the gap to an FP64 solve that made "
+                   "different argmax choices at near-ties")
     return out
 
 

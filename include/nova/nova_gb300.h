@@ -61,6 +61,36 @@ NOVA_API int pomdp_pbvi_get_stats_gpu(const POMDPPBVIGPU *pbvi, NovaPBVIStats *s
 NOVA_API int pomdp_pbvi_value_gpu(const POMDP *pomdp, const POMDPPBVIGPU *pbvi,
         const float *b, double *Vb, unsigned int *a);
 
+/* One pomdp_pbvi_update_gpu that also records its selections into caller
+ * device arrays: d_action[i] = the action whose alpha became GammaPrime[i]
+ * (pi[i]) and d_select[i*z + o] = the alpha index j* taken for (i, that
+ * action, o), i.e. the argmax results of pomdp_pbvi_cpu.cpp:37-103 (lowest
+ * index among equal rows). No reference counterpart. */
+NOVA_API int pomdp_pbvi_update_record_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi,
+        unsigned int *d_action, unsigned int *d_select);
+
+/* horizon recorded updates from the solver's current state. Before update t
+ * with t % checkpointEvery == 0 the current Gamma is copied to
+ * d_checkpoints[t / checkpointEvery] ([ceil(horizon/checkpointEvery)][r][n]);
+ * the selections of update t go to d_actions[t] ([horizon][r]) and
+ * d_selects[t] ([horizon][r][z]). No reference counterpart. */
+NOVA_API int pomdp_pbvi_execute_recorded_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi,
+        unsigned int horizon, unsigned int checkpointEvery, float *d_checkpoints,
+        unsigned int *d_actions, unsigned int *d_selects);
+
+/* Reverse mode of horizon recorded backups (selections held fixed):
+ * V(b) = max_i b . Gamma_H[i] (FP64, lowest index on ties) and its gradient
+ * with respect to the model's R (d_dR [n][m]), T (d_dT [n][m][ns]) and O
+ * (d_dO [m][n][z]), all FP64 device arrays, plus optionally Gamma_0
+ * (d_dGamma0 [r][n]). Alphas between checkpoints are recomputed in FP32 in
+ * the reference's operation order, bit-identical to the forward pass. The
+ * model's device arrays must be those the recorded forward ran on. No
+ * reference counterpart (the reference has no differentiation). */
+NOVA_API int pomdp_pbvi_adjoint_gpu(const POMDP *pomdp, unsigned int horizon,
+        unsigned int checkpointEvery, const float *d_checkpoints, const unsigned int *d_actions,
+        const unsigned int *d_selects, const float *d_b, double *d_dR, double *d_dT, double *d_dO,
+        double *d_dGamma0, double *Vb, unsigned int *bestAlpha);
+
 /* Value iteration until the Bellman residual max_s |V'(s) - V(s)|, computed
  * in FP64 on the device after every sweep, drops below tol, or maxSweeps
  * sweeps ran. The reference's VI has no convergence test (mdp_vi_gpu.cu:163-221

@@ -978,6 +978,41 @@ int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsi
     return NOVA_SUCCESS;
 }
 
+// Selections of the last backup: for belief i, the action a = pi[i] whose
+// alpha became GammaPrime[i] and, per observation o, the alpha index j* that
+// alpha took for (i, a, o). The projection-table path keeps its choices as
+// unique-alpha indices (mapped back through uniqJ, the lowest original index
+// of each distinct row, which is the reference's choice among equal rows).
+__global__ void record_selection_kernel(unsigned r, unsigned m, unsigned z, const unsigned *__restrict__ pi,
+                                        int fromUnique, const unsigned *__restrict__ ustar,
+                                        const unsigned *__restrict__ uniqJ, const unsigned *__restrict__ jstar,
+                                        unsigned *__restrict__ actOut, unsigned *__restrict__ selOut) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (size_t)r * z) return;
+    const unsigned i = (unsigned)(idx / z), o = (unsigned)(idx % z);
+    unsigned a = pi[i];
+    if (a >= m) a = 0;
+    const size_t k = ((size_t)i * m + a) * z + o;
+    unsigned j;
+    if (fromUnique) {
+        const unsigned u = ustar[k];
+        j = u == kNone ? 0u : uniqJ[u];
+    } else {
+        j = jstar[k];
+        if (j == kNone) j = 0;
+    }
+    selOut[idx] = j;
+    if (o == 0) actOut[i] = a;
+}
+
+int BackupEngine::record(const unsigned *pi, unsigned *actOut, unsigned *selOut, const char *fn) {
+    record_selection_kernel<<<ceil_div((size_t)md.r * md.z, 256), 256, 0, stream>>>(
+        md.r, md.m, md.z, pi, useProjNow ? 1 : 0, ustar, uniqJ, jstar, actOut, selOut);
+    int rc = check_launch(fn, "selection record");
+    if (rc != NOVA_SUCCESS) return rc;
+    return sync_device(fn);
+}
+
 // ---------------------------------------------------------------------------
 // Solver workspaces
 // ---------------------------------------------------------------------------
@@ -1174,6 +1209,19 @@ extern "C" int pomdp_pbvi_update_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi) {
     pbvi->currentHorizon++;
     ws->eng.stats.horizon = pbvi->currentHorizon;
     return NOVA_SUCCESS;
+}
+
+extern "C" int pomdp_pbvi_update_record_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi, unsigned int *d_action,
+                                            unsigned int *d_select) {
+    static const char *fn = "pomdp_pbvi_update_record_gpu";
+    if (d_action == nullptr || d_select == nullptr) {
+        NOVA_ERR(fn, "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    int rc = pomdp_pbvi_update_gpu(pomdp, pbvi);
+    if (rc != NOVA_SUCCESS) return rc;
+    PbviGpuWorkspace *ws = pbvi_gpu_ws(pbvi);
+    return ws->eng.record(pbvi->d_pi, d_action, d_select, fn);
 }
 
 extern "C" int pomdp_pbvi_get_policy_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi, POMDPAlphaVectors *policy) {

@@ -88,6 +88,9 @@ struct BackupEngine {
     int scan_rows(const unsigned *rowList, unsigned nRows, unsigned nU, const char *fn);
     // Work list of `count` consecutive items starting at `first`.
     int fill_items(unsigned first, unsigned count, const char *fn);
+    // Write the last backup's selections (action per belief, alpha per
+    // (belief, observation) under that action) to device arrays.
+    int record(const unsigned *pi, unsigned *actOut, unsigned *selOut, const char *fn);
     // Action values and best-action assembly for all beliefs (or one).
     int assemble(const float *src, float *dst, unsigned *pi, int onlyBelief, float *dstRowOverride,
                  unsigned *actionOut, const char *fn);

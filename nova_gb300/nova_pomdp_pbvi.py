@@ -72,3 +72,9 @@ _nova.pomdp_pbvi_set_scoring_gpu.argtypes = (_G, ct.c_uint)
 _nova.pomdp_pbvi_get_stats_gpu.argtypes = (_G, ct.POINTER(NovaPBVIStats))
 _nova.pomdp_pbvi_value_gpu.argtypes = (_P, _G, ct.POINTER(ct.c_float), ct.POINTER(ct.c_double),
                                        ct.POINTER(ct.c_uint))
+_nova.pomdp_pbvi_update_record_gpu.argtypes = (_P, _G, ct.c_void_p, ct.c_void_p)
+_nova.pomdp_pbvi_execute_recorded_gpu.argtypes = (_P, _G, ct.c_uint, ct.c_uint, ct.c_void_p, ct.c_void_p,
+                                                  ct.c_void_p)
+_nova.pomdp_pbvi_adjoint_gpu.argtypes = (_P, ct.c_uint, ct.c_uint, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                         ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                         ct.POINTER(ct.c_double), ct.POINTER(ct.c_uint))

@@ -591,3 +591,194 @@ float oracle_pbvi_belief_action(unsigned n, unsigned ns, unsigned m, unsigned z,
     }
     return value;
 }
+
+/* ------------------------------------------------------------------------ */
+/* PBVI with recorded selections, FP64 (reference for the GPU adjoint)       */
+/* ------------------------------------------------------------------------ */
+
+/* With the selections of each backup held fixed -- act[t][i] (the action
+ * whose alpha became Gamma_{t+1}[i]) and sel[t][i][o] (the alpha chosen for
+ * observation o) -- a backup of pomdp_pbvi_cpu.cpp:37-162 is
+ *   Gamma_{t+1}[i](s) = R(s,a) + sum_o gamma sum_l O(a,S,o) T(s,a,l) Gamma_t[j_o](S),
+ * and V(b) = max_i b . Gamma_H[i] (pomdp_alpha_vectors.cpp:52-79, lowest index
+ * on ties). Everything here is FP64 and multi-threaded over beliefs. */
+typedef struct {
+    unsigned n, ns, m, z, r;
+    double gamma;
+    const int *S;
+    const double *T, *O, *R;
+    const unsigned *act, *sel; /* this step's [r] and [r][z] */
+    const double *Gin;
+    double *Gout;
+    unsigned i0, i1;
+    /* reverse only */
+    const double *lam;
+    double *lamPrev, *dR, *dT, *dO;
+} FixedJob;
+
+static void *fixed_forward_worker(void *arg) {
+    const FixedJob *J = (const FixedJob *)arg;
+    for (unsigned i = J->i0; i < J->i1; i++) {
+        const unsigned a = J->act[i];
+        double *out = J->Gout + (size_t)i * J->n;
+        for (unsigned s = 0; s < J->n; s++) {
+            double v = J->R[(size_t)s * J->m + a];
+            for (unsigned o = 0; o < J->z; o++) {
+                const double *g = J->Gin + (size_t)J->sel[(size_t)i * J->z + o] * J->n;
+                double p = 0.0;
+                for (unsigned l = 0; l < J->ns; l++) {
+                    const size_t row = ((size_t)s * J->m + a) * J->ns + l;
+                    const int sp = J->S[row];
+                    if (sp < 0) break;
+                    p += J->O[((size_t)a * J->n + sp) * J->z + o] * J->T[row] * g[sp];
+                }
+                v += J->gamma * p;
+            }
+            out[s] = v;
+        }
+    }
+    return NULL;
+}
+
+static void *fixed_reverse_worker(void *arg) {
+    const FixedJob *J = (const FixedJob *)arg;
+    for (unsigned i = J->i0; i < J->i1; i++) {
+        const unsigned a = J->act[i];
+        for (unsigned s = 0; s < J->n; s++) {
+            const double lam = J->lam[(size_t)i * J->n + s];
+            if (lam == 0.0) continue;
+            J->dR[(size_t)s * J->m + a] += lam;
+            for (unsigned l = 0; l < J->ns; l++) {
+                const size_t row = ((size_t)s * J->m + a) * J->ns + l;
+                const int sp = J->S[row];
+                if (sp < 0) break;
+                const double tv = J->T[row];
+                for (unsigned o = 0; o < J->z; o++) {
+                    const unsigned j = J->sel[(size_t)i * J->z + o];
+                    const double g = J->Gin[(size_t)j * J->n + sp];
+                    const size_t oi = ((size_t)a * J->n + sp) * J->z + o;
+                    const double ov = J->O[oi];
+                    J->dT[row] += J->gamma * lam * ov * g;
+                    J->dO[oi] += J->gamma * lam * tv * g;
+                    J->lamPrev[(size_t)j * J->n + sp] += J->gamma * lam * tv * ov;
+                }
+            }
+        }
+    }
+    return NULL;
+}
+
+static unsigned oracle_threads(unsigned cap) {
+    long cores = sysconf(_SC_NPROCESSORS_ONLN);
+    unsigned nt = (unsigned)(cores < 1 ? 1 : cores);
+    if (nt > cap) nt = cap;
+    if (nt > 64) nt = 64;
+    return nt < 1 ? 1 : nt;
+}
+
+static void run_jobs(FixedJob *jobs, unsigned nt, void *(*fn)(void *)) {
+    pthread_t tid[64];
+    int started[64] = {0};
+    for (unsigned t = 1; t < nt; t++) started[t] = pthread_create(&tid[t], NULL, fn, &jobs[t]) == 0;
+    fn(&jobs[0]);
+    for (unsigned t = 1; t < nt; t++) {
+        if (started[t]) pthread_join(tid[t], NULL);
+        else fn(&jobs[t]);
+    }
+}
+
+/* Forward pass; GammaAll ([H+1][r][n]) receives every Gamma_t. Returns V(b)
+ * and the maximising row in *istar; when *istar holds a row index on entry,
+ * that row is used instead (the final argmax recorded too). */
+double oracle_pbvi_fixed_forward_f64(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, double gamma,
+                                     const int *S, const double *T, const double *O, const double *R,
+                                     const double *Gamma0, unsigned H, const unsigned *act, const unsigned *sel,
+                                     const double *b, unsigned *istar, double *GammaAll) {
+    const size_t rn = (size_t)r * n;
+    memcpy(GammaAll, Gamma0, rn * sizeof(double));
+    const unsigned nt = oracle_threads(r);
+    FixedJob jobs[64];
+    for (unsigned t = 0; t < H; t++) {
+        for (unsigned k = 0; k < nt; k++) {
+            FixedJob J;
+            memset(&J, 0, sizeof(J));
+            J.n = n; J.ns = ns; J.m = m; J.z = z; J.r = r; J.gamma = gamma;
+            J.S = S; J.T = T; J.O = O; J.R = R;
+            J.act = act + (size_t)t * r; J.sel = sel + (size_t)t * r * z;
+            J.Gin = GammaAll + (size_t)t * rn; J.Gout = GammaAll + (size_t)(t + 1) * rn;
+            J.i0 = (unsigned)((size_t)r * k / nt); J.i1 = (unsigned)((size_t)r * (k + 1) / nt);
+            jobs[k] = J;
+        }
+        run_jobs(jobs, nt, fixed_forward_worker);
+    }
+    const double *GH = GammaAll + (size_t)H * rn;
+    if (*istar < r) {
+        double v = 0.0;
+        for (unsigned s = 0; s < n; s++) v += GH[(size_t)*istar * n + s] * b[s];
+        return v;
+    }
+    double best = -1e10;
+    unsigned bi = 0xffffffffu;
+    for (unsigned i = 0; i < r; i++) {
+        double v = 0.0;
+        for (unsigned s = 0; s < n; s++) v += GH[(size_t)i * n + s] * b[s];
+        if (v > best) { best = v; bi = i; }
+    }
+    *istar = bi;
+    return best;
+}
+
+/* Reverse pass (direct form, every (i, s, l, o) term): gradients of V(b) with
+ * respect to R [n][m], T [n][m][ns], O [m][n][z] and Gamma0 [r][n]. A row
+ * index in istarFixed fixes the final argmax (0xffffffff: take the FP64 one). */
+double oracle_pbvi_fixed_reverse_f64(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, double gamma,
+                                     const int *S, const double *T, const double *O, const double *R,
+                                     const double *Gamma0, unsigned H, const unsigned *act, const unsigned *sel,
+                                     const double *b, unsigned istarFixed, double *dR, double *dT, double *dO,
+                                     double *dGamma0) {
+    const size_t rn = (size_t)r * n;
+    double *GammaAll = (double *)malloc(sizeof(double) * (size_t)(H + 1) * rn);
+    unsigned istar = istarFixed;
+    const double V = oracle_pbvi_fixed_forward_f64(n, ns, m, z, r, gamma, S, T, O, R, Gamma0, H, act, sel, b,
+                                                   &istar, GammaAll);
+    const size_t nR = (size_t)n * m, nT = (size_t)n * m * ns, nO = (size_t)m * n * z;
+    memset(dR, 0, nR * sizeof(double));
+    memset(dT, 0, nT * sizeof(double));
+    memset(dO, 0, nO * sizeof(double));
+    double *lam = (double *)calloc(rn, sizeof(double));
+    if (istar != 0xffffffffu) memcpy(lam + (size_t)istar * n, b, n * sizeof(double));
+    const unsigned nt = oracle_threads(r);
+    /* Per-thread accumulators, summed after every step. */
+    double *acc = (double *)malloc(sizeof(double) * (size_t)nt * (rn + nR + nT + nO));
+    FixedJob jobs[64];
+    for (unsigned t = H; t >= 1; t--) {
+        memset(acc, 0, sizeof(double) * (size_t)nt * (rn + nR + nT + nO));
+        for (unsigned k = 0; k < nt; k++) {
+            double *base = acc + (size_t)k * (rn + nR + nT + nO);
+            FixedJob J;
+            memset(&J, 0, sizeof(J));
+            J.n = n; J.ns = ns; J.m = m; J.z = z; J.r = r; J.gamma = gamma;
+            J.S = S; J.T = T; J.O = O; J.R = R;
+            J.act = act + (size_t)(t - 1) * r; J.sel = sel + (size_t)(t - 1) * r * z;
+            J.Gin = GammaAll + (size_t)(t - 1) * rn;
+            J.i0 = (unsigned)((size_t)r * k / nt); J.i1 = (unsigned)((size_t)r * (k + 1) / nt);
+            J.lam = lam;
+            J.lamPrev = base; J.dR = base + rn; J.dT = base + rn + nR; J.dO = base + rn + nR + nT;
+            jobs[k] = J;
+        }
+        run_jobs(jobs, nt, fixed_reverse_worker);
+        memset(lam, 0, rn * sizeof(double));
+        for (unsigned k = 0; k < nt; k++) {
+            const double *base = acc + (size_t)k * (rn + nR + nT + nO);
+            for (size_t e = 0; e < rn; e++) lam[e] += base[e];
+            for (size_t e = 0; e < nR; e++) dR[e] += base[rn + e];
+            for (size_t e = 0; e < nT; e++) dT[e] += base[rn + nR + e];
+            for (size_t e = 0; e < nO; e++) dO[e] += base[rn + nR + nT + e];
+        }
+    }
+    if (dGamma0) memcpy(dGamma0, lam, rn * sizeof(double));
+    free(acc);
+    free(lam);
+    free(GammaAll);
+    return V;
+}

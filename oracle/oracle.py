@@ -69,6 +69,11 @@ def lib():
         L.oracle_pbvi_belief_action.argtypes = [ct.c_uint] * 6 + [ct.c_float, _I, _F, _F, _F, _I, _F, _F, ct.c_uint,
                                                                   ct.c_uint, _F]
         L.oracle_pbvi_belief_action.restype = ct.c_float
+        fixed = [ct.c_uint] * 5 + [ct.c_double, _I, _D, _D, _D, _D, ct.c_uint, _U, _U, _D]
+        L.oracle_pbvi_fixed_forward_f64.argtypes = fixed + [_U, _D]
+        L.oracle_pbvi_fixed_forward_f64.restype = ct.c_double
+        L.oracle_pbvi_fixed_reverse_f64.argtypes = fixed + [ct.c_uint, _D, _D, _D, _D]
+        L.oracle_pbvi_fixed_reverse_f64.restype = ct.c_double
     return _oracle
 
 
@@ -373,3 +378,70 @@ def ref_alpha_value(Gamma, pi, b):
     if rc != 0:
         raise RuntimeError("reference value_and_action failed: %d" % rc)
     return V.value, a.value
+
+
+# ---------------------------------------------------------------------------
+# PBVI with recorded selections (FP64): reference for the GPU adjoint
+# ---------------------------------------------------------------------------
+
+def pbvi_record(model, horizon, GammaInitial=None):
+    """nova's PBVI (FP32, the factored restatement) for `horizon` backups,
+    recording the selections: actions [H][r] (pi after each backup) and
+    selects [H][r][z] (the alpha chosen per observation under that action).
+    Returns (Gamma_H float32 [r,n], actions, selects)."""
+    n, ns, m, z, r, rz = _dims(model)
+    G = np.ascontiguousarray(model["GammaInitial"] if GammaInitial is None else GammaInitial, dtype=np.float32)
+    acts = np.zeros((horizon, r), np.uint32)
+    sels = np.zeros((horizon, r, z), np.uint32)
+    for t in range(horizon):
+        Gp = np.empty_like(G)
+        pi = np.zeros(r, np.uint32)
+        js = np.zeros((r, m, z), np.uint32)
+        pbvi_update(model, G, Gp, pi, jstar=js)
+        acts[t] = pi
+        sels[t] = js[np.arange(r), pi]
+        G = Gp
+    return G, acts, sels
+
+
+def _fixed_args(model, Gamma0, actions, selects, b, T=None, O=None, R=None):
+    n, ns, m, z, r, rz = _dims(model)
+    S = np.ascontiguousarray(model["S"], dtype=np.int32)
+    T = np.ascontiguousarray(model["T"] if T is None else T, dtype=np.float64)
+    O = np.ascontiguousarray(model["O"] if O is None else O, dtype=np.float64)
+    R = np.ascontiguousarray(model["R"] if R is None else R, dtype=np.float64)
+    G0 = np.ascontiguousarray(Gamma0, dtype=np.float64)
+    A = np.ascontiguousarray(actions, dtype=np.uint32)
+    Se = np.ascontiguousarray(selects, dtype=np.uint32)
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    keep = (S, T, O, R, G0, A, Se, bb)
+    args = [n, ns, m, z, r, float(model["gamma"]), _p(S, _I), _p(T, _D), _p(O, _D), _p(R, _D), _p(G0, _D),
+            A.shape[0], _p(A, _U), _p(Se, _U), _p(bb, _D)]
+    return args, keep
+
+
+def pbvi_fixed_forward_f64(model, Gamma0, actions, selects, b, T=None, O=None, R=None, istar=None):
+    """V(b) = max_i b . Gamma_H[i] in FP64 with the recorded selections
+    (optionally with T, O, R replaced, and the final argmax fixed to row
+    `istar`); returns (V, i*)."""
+    n, ns, m, z, r, rz = _dims(model)
+    args, keep = _fixed_args(model, Gamma0, actions, selects, b, T, O, R)
+    H = args[11]
+    GammaAll = np.empty((H + 1) * r * n, np.float64)
+    istar = ct.c_uint(0xFFFFFFFF if istar is None else int(istar))
+    V = lib().oracle_pbvi_fixed_forward_f64(*args, ct.byref(istar), _p(GammaAll, _D))
+    _ = keep
+    return V, istar.value
+
+
+def pbvi_fixed_reverse_f64(model, Gamma0, actions, selects, b, istar=None):
+    """FP64 reverse mode (direct form) of the recorded backups (final argmax
+    fixed to row `istar` when given); returns
+    (V, dR [n,m], dT [n,m,ns], dO [m,n,z], dGamma0 [r,n])."""
+    n, ns, m, z, r, rz = _dims(model)
+    args, keep = _fixed_args(model, Gamma0, actions, selects, b)
+    dR = np.zeros((n, m)); dT = np.zeros((n, m, ns)); dO = np.zeros((m, n, z)); dG = np.zeros((r, n))
+    V = lib().oracle_pbvi_fixed_reverse_f64(*args, 0xFFFFFFFF if istar is None else int(istar), _p(dR, _D),
+                                            _p(dT, _D), _p(dO, _D), _p(dG, _D))
+    _ = keep
+    return V, dR, dT, dO, dG
