@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--no-mdp", action="store_true")
     ap.add_argument("--bf16-steps", type=int, default=2)
     ap.add_argument("--precision-steps", type=int, default=3)
+    ap.add_argument("--batch-horizon", type=int, default=20)
+    ap.add_argument("--batch-threads", type=int, default=16)
     return ap.parse_args()
 
 
@@ -241,6 +243,127 @@ def run_precision(args):
     return out
 
 
+def run_gradient(args):
+    """Gradient of V(b0) after H=50 PBVI backups w.r.t. R, T, O (n=1024, m=8,
+    z=16, ns=16, r=2048, rz=32, b0 uniform, checkpoints every 10 steps):
+    GPU time of the recorded forward and of the reverse pass, and the
+    gradient's error against the oracle's FP64 reverse mode and against FP64
+    central differences (h=1e-6) on 64 random coordinates."""
+    import torch
+    from nova_gb300 import synth
+    from nova_gb300.pomdp_adjoint import PBVIGradSpec, pbvi_value, pbvi_record_and_adjoint
+    from oracle import oracle as orc
+    cfg = dict(synth.POMDP_CONFIGS["grad_n1024"])
+    model = synth.random_pomdp(**cfg, seed=args.seed)
+    H = cfg["horizon"]
+    b0 = np.full(model["n"], 1.0 / model["n"], np.float32)
+    spec = PBVIGradSpec(model=model, b0=b0, horizon=H, checkpoint_every=10)
+    times = []
+    for it in range(args.warmup + args.steps):
+        R = torch.tensor(model["R"], device="cuda", requires_grad=True)
+        T = torch.tensor(model["T"], device="cuda", requires_grad=True)
+        O = torch.tensor(model["O"], device="cuda", requires_grad=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        V = pbvi_value(R, T, O, spec)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        V.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        if it >= args.warmup:
+            times.append((t1 - t0, t2 - t1))
+    fwd = float(np.median([a for a, _ in times]))
+    bwd = float(np.median([b for _, b in times]))
+    Vg, istar, dR, dT, dO, dG, acts, sels = pbvi_record_and_adjoint(model, b0, H, 10)
+    t0 = time.perf_counter()
+    V64, dR64, dT64, dO64, _ = orc.pbvi_fixed_reverse_f64(model, model["GammaInitial"], acts, sels, b0, istar=istar)
+    t_rev = time.perf_counter() - t0
+
+    def rel(a, b):
+        return float(np.max(np.abs(a - b)) / max(1e-30, np.max(np.abs(b))))
+    rng = np.random.default_rng(args.seed + 1)
+    grads = {"R": dR, "T": dT, "O": dO}
+    worst, h = 0.0, 1e-6
+    t0 = time.perf_counter()
+    for k in range(64):
+        name = ("R", "T", "O")[k % 3]
+        idx = tuple(int(rng.integers(0, d)) for d in model[name].shape)
+        A = model[name].astype(np.float64).copy()
+        A[idx] += h
+        Vp, _ = orc.pbvi_fixed_forward_f64(model, model["GammaInitial"], acts, sels, b0, istar=istar, **{name: A})
+        A[idx] -= 2 * h
+        Vm, _ = orc.pbvi_fixed_forward_f64(model, model["GammaInitial"], acts, sels, b0, istar=istar, **{name: A})
+        fd = (Vp - Vm) / (2 * h)
+        worst = max(worst, abs(grads[name][idx] - fd) / max(abs(fd), 1e-3))
+    t_fd = time.perf_counter() - t0
+    return {"metric": "gradients of V(b0) per second (H=50 PBVI backups, forward + reverse)",
+            "value": 1.0 / (fwd + bwd), "unit": "gradients/s", "steps": args.steps, "warmup": args.warmup,
+            "forward_s": fwd, "reverse_s": bwd, "higher_is_better": True,
+            "config": {"workload": "grad_n1024 (n=1024,m=8,z=16,ns=16,r=2048,rz=32,gamma=0.95,H=50,b0 uniform,"
+                                   "checkpoint every 10,seed=%d)" % args.seed},
+            "V_b0": Vg, "V_b0_fp64_same_selections": V64, "dV_b0": abs(Vg - V64),
+            "rel_err_vs_fp64_reverse": {"R": rel(dR, dR64), "T": rel(dT, dT64), "O": rel(dO, dO64)},
+            "fd_max_rel_err_64_coords": worst, "fd_step": h,
+            "oracle_reverse_seconds": t_rev, "fd_seconds": t_fd, "host_cores": host_cores()}
+
+
+def run_batch(args):
+    """256 independent random POMDPs (n, r log-uniform in [32, 2048] and
+    [128, 4096], m in 2..16, z in 2..32, ns = min(16, n), rz = min(32, n),
+    gamma 0.95) for --batch-horizon backups each: belief-backups/s summed over
+    the batch for the batched solve (host-thread pool, per-thread streams) with
+    FP16 and BF16 tensor-core scoring, against solving them one after another
+    with plain FP32 scoring; every batched policy is checked bit for bit
+    against the sequential plain one."""
+    import torch
+    from nova_gb300 import synth
+    from nova_gb300 import nova_pomdp_pbvi as npp
+    from nova_gb300.pomdp import POMDP
+    from nova_gb300.pomdp_pbvi import solve_batched
+    H = args.batch_horizon
+    t0 = time.perf_counter()
+    models = synth.batch_pomdps(256, seed=args.seed, horizon=H)
+    gen_s = time.perf_counter() - t0
+    pomdps = []
+    for md in models:
+        p = POMDP.from_arrays(md)
+        p.initialize_gpu()
+        pomdps.append(p)
+    total = float(sum(md["r"] for md in models) * H)
+
+    def timed(mode, threads, horizon=H):
+        for p in pomdps:
+            p.horizon = horizon
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        pols = solve_batched(pomdps, scoring=mode, hostThreads=threads)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t, pols
+
+    timed(npp.SCORING_FP16, args.batch_threads, horizon=1)  # warm-up: builds and first launches
+    t_fp16, pol_fp16 = timed(npp.SCORING_FP16, args.batch_threads)
+    g16 = [(p.gamma_array(), p.pi_array()) for p in pol_fp16]
+    del pol_fp16
+    t_bf16, pol_bf16 = timed(npp.SCORING_BF16, args.batch_threads)
+    g_bf = [(p.gamma_array(), p.pi_array()) for p in pol_bf16]
+    del pol_bf16
+    t_plain, pol_plain = timed(npp.SCORING_EXACT, 1)
+    identical = 0
+    for (G16, p16), (Gb, pb), pol in zip(g16, g_bf, pol_plain):
+        G, pi = pol.gamma_array(), pol.pi_array()
+        identical += int(np.array_equal(G16.view(np.uint32), G.view(np.uint32)) and np.array_equal(p16, pi) and
+                         np.array_equal(Gb.view(np.uint32), G.view(np.uint32)) and np.array_equal(pb, pi))
+    return {"metric": "belief-backups/s summed over a batch of 256 random POMDPs", "unit": "belief-backups/s",
+            "value": total / t_fp16, "horizon": H, "host_threads": args.batch_threads,
+            "fp16_batched_s": t_fp16, "bf16_batched": {"value": total / t_bf16, "seconds": t_bf16},
+            "plain_fp32_one_by_one": {"value": total / t_plain, "seconds": t_plain},
+            "policies_bit_identical": "%d of 256" % identical,
+            "belief_backups": total, "generation_s": gen_s,
+            "config": {"workload": "batch256 (n~logU[32,2048], r~logU[128,4096], m~U{2..16}, z~U{2..32}, "
+                                   "ns=min(16,n), rz=min(32,n), gamma=0.95, H=%d, seed=%d)" % (H, args.seed)}}
+
+
 def run_mdp(args, dist_rank):
     """Bellman sweep n=2^20, m=8, ns=16 (memory-bound): GB/s of algorithmic bytes.
     Sweeps are timed through mdp_vi_execute_gpu (sweeps queued back to back):
@@ -304,6 +427,18 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.config == "batch256":
+        import torch
+        torch.cuda.set_device(local_rank)
+        if rank == 0:
+            print(json.dumps({"batch": run_batch(args)}))
+        return
+    if args.config == "grad_n1024":
+        import torch
+        torch.cuda.set_device(local_rank)
+        if rank == 0:
+            print(json.dumps({"gradient": run_gradient(args)}))
         return
     if args.config == "vi_n1m":
         import torch

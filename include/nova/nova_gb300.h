@@ -14,6 +14,7 @@
 #include <nova/mdp/policies/mdp_value_function.h>
 #include <nova/pomdp/pomdp.h>
 #include <nova/pomdp/algorithms/pomdp_pbvi_gpu.h>
+#include <nova/pomdp/policies/pomdp_alpha_vectors.h>
 
 NOVA_NS_BEGIN
 
@@ -90,6 +91,19 @@ NOVA_API int pomdp_pbvi_adjoint_gpu(const POMDP *pomdp, unsigned int horizon,
         unsigned int checkpointEvery, const float *d_checkpoints, const unsigned int *d_actions,
         const unsigned int *d_selects, const float *d_b, double *d_dR, double *d_dT, double *d_dO,
         double *d_dGamma0, double *Vb, unsigned int *bestAlpha);
+
+/* Solve count independent POMDPs, each as pomdp_pbvi_execute_gpu would
+ * (initialize, `horizon` updates with the given NOVA_SCORING_* mode,
+ * get_policy into policies[k], uninitialize), with identical results. A pool
+ * of hostThreads host threads (0: min(count, 16)) takes the POMDPs largest
+ * first; every thread drives its own per-thread default stream, so small
+ * solves overlap on the device. Every POMDP must already have its device
+ * copy (pomdp_initialize_gpu) and every solver struct must be distinct.
+ * Returns the first failing solve's code (the others still run). No
+ * reference counterpart. */
+NOVA_API int pomdp_pbvi_execute_batched_gpu(const POMDP *const *pomdps, POMDPPBVIGPU *const *solvers,
+        POMDPAlphaVectors *const *policies, unsigned int count, unsigned int scoring,
+        unsigned int hostThreads);
 
 /* Value iteration until the Bellman residual max_s |V'(s) - V(s)|, computed
  * in FP64 on the device after every sweep, drops below tol, or maxSweeps

@@ -18,10 +18,10 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "lib", "libnova.so")
 
-SOURCES = ["runtime.cpp", "mdp_vi.cu", "mdp_vi_tiled.cu", "pbvi.cu", "pbvi_tc.cu", "pbvi_adjoint.cu", "perseus.cu", "value_noalloc.cu"]
+SOURCES = ["runtime.cpp", "mdp_vi.cu", "mdp_vi_tiled.cu", "pbvi.cu", "pbvi_tc.cu", "pbvi_adjoint.cu", "pbvi_batched.cu", "perseus.cu", "value_noalloc.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "--default-stream", "per-thread", "-Xcompiler", "-fPIC,-ffp-contract=off",
           "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 
 
@@ -55,10 +55,22 @@ def _header_mtimes():
     return out
 
 
-def _compile(src, verbose):
+def _flags_stamp():
+    """Objects are rebuilt when the compiler flags change, not only when sources do."""
+    stamp = os.path.join(BUILD, "flags.txt")
+    flags = " ".join(ARCH + COMMON)
+    old = open(stamp).read() if os.path.exists(stamp) else None
+    if old != flags:
+        with open(stamp, "w") as f:
+            f.write(flags)
+    return os.path.getmtime(stamp)
+
+
+def _compile(src, verbose, stamp_mtime=0.0):
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
     srcp = os.path.join(CSRC, src)
-    if os.path.exists(obj) and os.path.getmtime(obj) >= max([os.path.getmtime(srcp)] + _header_mtimes()):
+    if os.path.exists(obj) and os.path.getmtime(obj) >= max([os.path.getmtime(srcp), stamp_mtime] +
+                                                            _header_mtimes()):
         return obj
     cmd = [_nvcc(), "-c", srcp, "-o", obj] + ARCH + COMMON
     if src.endswith(".cpp"):
@@ -77,8 +89,9 @@ def build(verbose=False):
     """Compile every CUDA/C++ source for sm_103a and link lib/libnova.so."""
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    stamp_mtime = _flags_stamp()
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
+        objs = list(ex.map(lambda s: _compile(s, verbose, stamp_mtime), SOURCES))
     if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
         return LIB
     tmp = LIB + ".tmp"
@@ -86,7 +99,7 @@ def build(verbose=False):
     vscript = os.path.join(BUILD, "exports.map")
     with open(vscript, "w") as f:
         f.write("{\n  global:\n" + "".join("    %s;\n" % n for n in exported_symbols()) + "  local: *;\n};\n")
-    cmd = [_nvcc(), "-shared", "-o", tmp] + objs + ARCH + ["-Xcompiler", "-fPIC", "-cudart", "static",
+    cmd = [_nvcc(), "-shared", "-o", tmp] + objs + ARCH + ["-Xcompiler", "-fPIC,-pthread", "-cudart", "static",
                                                           "-Xlinker", "--version-script=" + vscript]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:

@@ -92,6 +92,7 @@ struct TcState {
     float *candX = nullptr;         // [MZ][r][MAX_GROUPS]
     unsigned *rowFlag = nullptr;    // [MZ*r] rows needing the exact scan
     unsigned *rowList = nullptr;    // [MZ*r] their indices, compacted
+    unsigned *chunkCount = nullptr; // [ceil(MZ*r / 4096)] flagged rows per chunk, then chunk offsets
     unsigned *badModel = nullptr;   // [1] set when a probability is negative or NaN
     PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     CUtensorMap tmA;
@@ -103,6 +104,7 @@ void tc_release(TcState *tc) {
     if (!tc) return;
     cudaFree(tc->A); cudaFree(tc->a1); cudaFree(tc->a1raw); cudaFree(tc->Gb); cudaFree(tc->shift); cudaFree(tc->scal);
     cudaFree(tc->candV); cudaFree(tc->candU); cudaFree(tc->candX); cudaFree(tc->rowFlag); cudaFree(tc->rowList);
+    cudaFree(tc->chunkCount);
     cudaFree(tc->badModel);
     if (tc->g0) cudaEventDestroy(tc->g0);
     if (tc->g1) cudaEventDestroy(tc->g1);
@@ -594,18 +596,18 @@ __device__ __forceinline__ float proj_row_score(const float *__restrict__ P, siz
     return v;
 }
 
-__global__ void tc_merge_kernel(DevModel md, const unsigned *__restrict__ suppLen, const float *__restrict__ Proj,
-                                size_t uCols, const unsigned *__restrict__ uniqJ, unsigned groups, size_t rPad,
-                                const float *__restrict__ a1, const float *__restrict__ a1raw,
-                                const unsigned *__restrict__ scal,
-                                const float *__restrict__ candV, const unsigned *__restrict__ candU,
-                                const float *__restrict__ candX, unsigned *__restrict__ ustar,
-                                unsigned *__restrict__ jstar, unsigned *__restrict__ rowFlag,
-                                unsigned *__restrict__ counters, const unsigned *__restrict__ badModel) {
-    const unsigned lane = threadIdx.x & 31;
-    const size_t row = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const size_t rows = (size_t)md.m * md.z * md.r;
-    if (row >= rows) return;
+// One warp per row; returns (in every lane) the number of candidates it
+// re-scored exactly, 0 when the row was settled without re-scoring or sent to
+// the exact scan.
+__device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevModel md,
+                                              const unsigned *__restrict__ suppLen, const float *__restrict__ Proj,
+                                              size_t uCols, const unsigned *__restrict__ uniqJ, unsigned groups,
+                                              size_t rPad, const float *__restrict__ a1,
+                                              const float *__restrict__ a1raw, const unsigned *__restrict__ scal,
+                                              const float *__restrict__ candV, const unsigned *__restrict__ candU,
+                                              const float *__restrict__ candX, unsigned *__restrict__ ustar,
+                                              unsigned *__restrict__ jstar, unsigned *__restrict__ rowFlag,
+                                              const unsigned *__restrict__ badModel) {
     const unsigned ao = (unsigned)(row / md.r), i = (unsigned)(row % md.r);
     const unsigned a = ao / md.z, o = ao % md.z;
     const size_t base = row * MAX_GROUPS * TOPK;
@@ -630,7 +632,7 @@ __global__ void tc_merge_kernel(DevModel md, const unsigned *__restrict__ suppLe
     const float cut = tmax - thr;
     if (!usable || x >= cut) {
         if (lane == 0) rowFlag[row] = 1u;
-        return;
+        return 0u;
     }
     const bool c0 = u0 != kNoneU && v0 >= cut;
     const bool c1 = u1 != kNoneU && v1 >= cut;
@@ -641,7 +643,7 @@ __global__ void tc_merge_kernel(DevModel md, const unsigned *__restrict__ suppLe
         const unsigned src = m0 ? __ffs(m0) - 1 : __ffs(m1) - 1;
         const unsigned uu = m0 ? __shfl_sync(0xffffffffu, u0, src) : __shfl_sync(0xffffffffu, u1, src);
         if (lane == 0) { ustar[js] = uu; jstar[js] = uniqJ[uu]; }
-        return;
+        return 0u;
     }
     // Several candidates: each lane re-scores its own in the exact order.
     const float *P = Proj + (size_t)ao * md.n * uCols;
@@ -667,45 +669,120 @@ __global__ void tc_merge_kernel(DevModel md, const unsigned *__restrict__ suppLe
             ustar[js] = bu;
             jstar[js] = uniqJ[bu];
         }
-        atomicAdd(&counters[0], 1u);
-        atomicAdd(&counters[1], count);
+    }
+    return count;
+}
+
+// Rows re-scored and candidates re-scored are counted per block in shared
+// memory, then added to the global counters once per block.
+__global__ void __launch_bounds__(1024) tc_merge_kernel(DevModel md, const unsigned *__restrict__ suppLen, const float *__restrict__ Proj,
+                                size_t uCols, const unsigned *__restrict__ uniqJ, unsigned groups, size_t rPad,
+                                const float *__restrict__ a1, const float *__restrict__ a1raw,
+                                const unsigned *__restrict__ scal,
+                                const float *__restrict__ candV, const unsigned *__restrict__ candU,
+                                const float *__restrict__ candX, unsigned *__restrict__ ustar,
+                                unsigned *__restrict__ jstar, unsigned *__restrict__ rowFlag,
+                                unsigned *__restrict__ counters, const unsigned *__restrict__ badModel) {
+    __shared__ unsigned blockCount[2];
+    if (threadIdx.x == 0) { blockCount[0] = 0u; blockCount[1] = 0u; }
+    __syncthreads();
+    const unsigned lane = threadIdx.x & 31;
+    const size_t row = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const size_t rows = (size_t)md.m * md.z * md.r;
+    unsigned rescored = 0;
+    if (row < rows)
+        rescored = merge_row(row, lane, md, suppLen, Proj, uCols, uniqJ, groups, rPad, a1, a1raw, scal, candV, candU,
+                             candX, ustar, jstar, rowFlag, badModel);
+    if (lane == 0 && rescored) {
+        atomicAdd(&blockCount[0], 1u);
+        atomicAdd(&blockCount[1], rescored);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && blockCount[0]) {
+        atomicAdd(&counters[0], blockCount[0]);
+        atomicAdd(&counters[1], blockCount[1]);
     }
 }
 
-// Flagged rows -> row list (single block, increasing order).
-__global__ void __launch_bounds__(1024) tc_compact_rows_kernel(const unsigned *__restrict__ flag, unsigned count,
-                                                               unsigned *__restrict__ items, unsigned *__restrict__ nOut) {
-    __shared__ unsigned warpSums[32];
-    __shared__ unsigned carry;
-    if (threadIdx.x == 0) carry = 0;
+// List of flagged rows in increasing order, in three launches: flagged rows
+// per chunk of 4096, a one-block scan of the chunk counts, then each chunk
+// writes its rows at its offset.
+constexpr unsigned kCompactChunk = 4096;  // rows per block (4 per thread)
+
+__global__ void __launch_bounds__(1024) tc_compact_count_kernel(const unsigned *__restrict__ flag, unsigned count,
+                                                                unsigned *__restrict__ chunkCount) {
+    const unsigned base = blockIdx.x * kCompactChunk;
+    unsigned c = 0;
+    for (unsigned k = threadIdx.x; k < kCompactChunk; k += blockDim.x)
+        if (base + k < count && flag[base + k]) c++;
+    for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
+    __shared__ unsigned ws[32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
     __syncthreads();
-    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (unsigned base = 0; base < count; base += blockDim.x) {
-        const unsigned t = base + threadIdx.x;
-        const unsigned f = (t < count && flag[t]) ? 1u : 0u;
-        unsigned v = f;
-        for (int off = 1; off < 32; off <<= 1) {
-            const unsigned y = __shfl_up_sync(0xffffffffu, v, off);
-            if (lane >= (unsigned)off) v += y;
-        }
-        if (lane == 31) warpSums[warp] = v;
+    if (threadIdx.x == 0) {
+        unsigned t = 0;
+        for (unsigned w = 0; w < blockDim.x / 32; w++) t += ws[w];
+        chunkCount[blockIdx.x] = t;
+    }
+}
+
+// Exclusive scan of chunkCount[0..nChunks) in place; the total goes to *nOut.
+__global__ void __launch_bounds__(1024) tc_compact_scan_kernel(unsigned *__restrict__ chunkCount, unsigned nChunks,
+                                                               unsigned *__restrict__ nOut) {
+    __shared__ unsigned sums[1024];
+    const unsigned per = (nChunks + blockDim.x - 1) / blockDim.x;
+    const unsigned b = threadIdx.x * per, e = min(nChunks, b + per);
+    unsigned s = 0;
+    for (unsigned i = b; i < e; i++) s += chunkCount[i];
+    sums[threadIdx.x] = s;
+    __syncthreads();
+    for (unsigned off = 1; off < blockDim.x; off <<= 1) {
+        const unsigned v = threadIdx.x >= off ? sums[threadIdx.x - off] : 0u;
         __syncthreads();
-        if (warp == 0) {
-            unsigned w = lane < (blockDim.x >> 5) ? warpSums[lane] : 0u;
-            for (int off = 1; off < 32; off <<= 1) {
-                const unsigned y = __shfl_up_sync(0xffffffffu, w, off);
-                if (lane >= (unsigned)off) w += y;
-            }
-            warpSums[lane] = w;
-        }
-        __syncthreads();
-        const unsigned pos = carry + (warp > 0 ? warpSums[warp - 1] : 0u) + v - f;
-        if (f) items[pos] = t;
-        __syncthreads();
-        if (threadIdx.x == 0) carry += warpSums[(blockDim.x >> 5) - 1];
+        sums[threadIdx.x] += v;
         __syncthreads();
     }
-    if (threadIdx.x == 0) *nOut = carry;
+    unsigned run = threadIdx.x ? sums[threadIdx.x - 1] : 0u;
+    for (unsigned i = b; i < e; i++) {
+        const unsigned c = chunkCount[i];
+        chunkCount[i] = run;
+        run += c;
+    }
+    if (threadIdx.x == blockDim.x - 1) *nOut = sums[blockDim.x - 1];
+}
+
+__global__ void __launch_bounds__(1024) tc_compact_write_kernel(const unsigned *__restrict__ flag, unsigned count,
+                                                                const unsigned *__restrict__ chunkStart,
+                                                                unsigned *__restrict__ items) {
+    const unsigned base = blockIdx.x * kCompactChunk + 4u * threadIdx.x;
+    unsigned f[4], local = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        f[k] = (base + k < count && flag[base + k]) ? 1u : 0u;
+        local += f[k];
+    }
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned incl = local;
+    for (int off = 1; off < 32; off <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= (unsigned)off) incl += y;
+    }
+    __shared__ unsigned wsum[32];
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned x = lane < blockDim.x / 32 ? wsum[lane] : 0u;
+        for (int off = 1; off < 32; off <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= (unsigned)off) x += y;
+        }
+        wsum[lane] = x;
+    }
+    __syncthreads();
+    unsigned pos = chunkStart[blockIdx.x] + (warp ? wsum[warp - 1] : 0u) + incl - local;
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        if (f[k]) items[pos++] = base + k;
 }
 
 // ---------------------------------------------------------------------------
@@ -789,6 +866,9 @@ int tc_build(BackupEngine &eng, const char *fn) {
     if ((rc = dev_alloc(&tc->candX, slots, fn, "the dropped-score bounds")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->rowFlag, (size_t)tc->MZ * md.r, fn, "the exact-scan flags")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->rowList, (size_t)tc->MZ * md.r, fn, "the exact-scan rows")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->chunkCount, ceil_div((size_t)tc->MZ * md.r, kCompactChunk), fn,
+                        "the exact-scan chunk counts")) != NOVA_SUCCESS)
+        return rc;
     if ((rc = dev_alloc(&tc->badModel, 1, fn, "the model check")) != NOVA_SUCCESS) return rc;
     if ((rc = tc_build_operand(eng, tc.get(), fn)) != NOVA_SUCCESS) return rc;
     cudaDeviceProp prop;
@@ -857,14 +937,22 @@ int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, 
     // ---- merge, margin, exact re-score of near ties ----
     const size_t rows = (size_t)tc->MZ * md.r;
     cudaMemsetAsync(tc->rowFlag, 0, rows * sizeof(unsigned), eng.stream);
-    tc_merge_kernel<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, eng.stream>>>(
+    tc_merge_kernel<<<(unsigned)ceil_div(rows * 32, 1024), 1024, 0, eng.stream>>>(
         md, eng.suppLen, eng.Proj, eng.projCols, eng.uniqJ, groups, tc->rPad, tc->a1, tc->a1raw, tc->scal, tc->candV,
         tc->candU,
         tc->candX, eng.ustar, eng.jstar, tc->rowFlag, tc->scal + 3, tc->badModel);
     if ((rc = check_launch(fn, "candidate merge")) != NOVA_SUCCESS) return rc;
     // The list can hold every row: it is sized m*z*r like the flags.
-    tc_compact_rows_kernel<<<1, 1024, 0, eng.stream>>>(tc->rowFlag, (unsigned)rows, tc->rowList, eng.itemCount);
-    if ((rc = check_launch(fn, "exact-scan list")) != NOVA_SUCCESS) return rc;
+    {
+        const unsigned nChunks = ceil_div(rows, kCompactChunk);
+        tc_compact_count_kernel<<<nChunks, 1024, 0, eng.stream>>>(tc->rowFlag, (unsigned)rows, tc->chunkCount);
+        if ((rc = check_launch(fn, "exact-scan list (count)")) != NOVA_SUCCESS) return rc;
+        tc_compact_scan_kernel<<<1, 1024, 0, eng.stream>>>(tc->chunkCount, nChunks, eng.itemCount);
+        if ((rc = check_launch(fn, "exact-scan list (scan)")) != NOVA_SUCCESS) return rc;
+        tc_compact_write_kernel<<<nChunks, 1024, 0, eng.stream>>>(tc->rowFlag, (unsigned)rows, tc->chunkCount,
+                                                                  tc->rowList);
+        if ((rc = check_launch(fn, "exact-scan list (write)")) != NOVA_SUCCESS) return rc;
+    }
     unsigned h[8];
     unsigned cnt = 0;
     if (cudaMemcpyAsync(h, tc->scal, sizeof(h), cudaMemcpyDeviceToHost, eng.stream) != cudaSuccess ||

@@ -78,3 +78,7 @@ _nova.pomdp_pbvi_execute_recorded_gpu.argtypes = (_P, _G, ct.c_uint, ct.c_uint, 
 _nova.pomdp_pbvi_adjoint_gpu.argtypes = (_P, ct.c_uint, ct.c_uint, ct.c_void_p, ct.c_void_p, ct.c_void_p,
                                          ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,
                                          ct.POINTER(ct.c_double), ct.POINTER(ct.c_uint))
+from . import nova_pomdp_alpha_vectors as _npav  # noqa: E402
+_nova.pomdp_pbvi_execute_batched_gpu.argtypes = (ct.POINTER(_P), ct.POINTER(_G),
+                                                 ct.POINTER(ct.POINTER(_npav.NovaPOMDPAlphaVectors)), ct.c_uint,
+                                                 ct.c_uint, ct.c_uint)

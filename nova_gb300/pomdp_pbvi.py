@@ -150,3 +150,31 @@ class POMDPPBVIGPU(npp.NovaPOMDPPBVIGPU):
 
     def __str__(self):
         return "currentHorizon: %i\n\nnumThreads: %i\n\n" % (self.currentHorizon, self.numThreads)
+
+
+def solve_batched(pomdps, scoring=npp.SCORING_FP16, hostThreads=0, GammaInitials=None):
+    """ Solve independent POMDPs (each already copied to the device with
+    initialize_gpu) with pomdp_pbvi_execute_batched_gpu; returns one
+    POMDPAlphaVectors per POMDP, as each POMDPPBVIGPU(p).solve() would. """
+    from . import pomdp_alpha_vectors as pav
+    count = len(pomdps)
+    solvers, bufs = [], []
+    for k, p in enumerate(pomdps):
+        s = npp.NovaPOMDPPBVIGPU()
+        buf = _initial_gamma(p, None if GammaInitials is None else GammaInitials[k])
+        bufs.append(buf)
+        s.GammaInitial = ct.cast(buf, ct.POINTER(ct.c_float))
+        s.numThreads = 1024
+        s.currentHorizon = 0
+        solvers.append(s)
+    policies = [pav.POMDPAlphaVectors() for _ in range(count)]
+    P = (ct.POINTER(pomdp.POMDP) * count)(*[ct.pointer(p) for p in pomdps])
+    G = (ct.POINTER(npp.NovaPOMDPPBVIGPU) * count)(*[ct.pointer(s) for s in solvers])
+    A = (ct.POINTER(npp._npav.NovaPOMDPAlphaVectors) * count)(*[ct.cast(ct.pointer(a),
+                                                                         ct.POINTER(npp._npav.NovaPOMDPAlphaVectors))
+                                                                 for a in policies])
+    result = npp._nova.pomdp_pbvi_execute_batched_gpu(P, G, A, count, int(scoring), int(hostThreads))
+    _ = bufs
+    if result != 0:
+        raise RuntimeError("pomdp_pbvi_execute_batched_gpu failed with code %d" % result)
+    return policies

@@ -23,6 +23,7 @@ POMDP_CONFIGS = {
     "pbvi_n512": dict(n=512, m=8, z=16, ns=16, r=1024, rz=32, gamma=0.95, horizon=50),
     "pbvi_n4096_small": dict(n=4096, m=2, z=4, ns=32, r=4096, rz=64, gamma=0.95, horizon=10),
     "pbvi_n4096_r256": dict(n=4096, m=16, z=32, ns=32, r=256, rz=64, gamma=0.95, horizon=4),
+    "pbvi_n4096_prof": dict(n=4096, m=2, z=32, ns=32, r=2048, rz=64, gamma=0.95, horizon=10),
     "grad_n1024": dict(n=1024, m=8, z=16, ns=16, r=2048, rz=32, gamma=0.95, horizon=50),
 }
 MDP_CONFIGS = {
@@ -85,3 +86,25 @@ def dense_belief(model, i):
             break
         b[s] = p
     return b
+
+
+def batch_shapes(count=256, seed=0, n_range=(32, 2048), r_range=(128, 4096), m_range=(2, 16), z_range=(2, 32),
+                 horizon=100):
+    """Shapes of a batch of independent POMDPs: n and r log-uniform, m and z
+    uniform integers, ns = min(16, n), rz = min(32, n), gamma = 0.95."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for k in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1])))))
+        r = int(round(np.exp(rng.uniform(np.log(r_range[0]), np.log(r_range[1])))))
+        m = int(rng.integers(m_range[0], m_range[1] + 1))
+        z = int(rng.integers(z_range[0], z_range[1] + 1))
+        out.append(dict(n=n, m=m, z=z, ns=min(16, n), r=r, rz=min(32, n), gamma=0.95, horizon=horizon,
+                        seed=seed * 100003 + k + 1))
+    return out
+
+
+def batch_pomdps(count=256, seed=0, **kw):
+    """The seeded batch of random POMDPs of batch_shapes (config of the
+    batched-solve benchmark: 256 POMDPs, horizon 100)."""
+    return [random_pomdp(**s) for s in batch_shapes(count, seed, **kw)]
