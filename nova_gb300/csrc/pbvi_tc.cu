@@ -589,10 +589,21 @@ __global__ void tc_escale_kernel(unsigned *scal, float U, float gN) {
 // whose candidate set may be incomplete go to the exact row scan.
 // ---------------------------------------------------------------------------
 
+// score(u) = sum_k fl(Proj[s_k][u] * b_k) in support order
+// (pomdp_pbvi_cpu.cpp:50-83). Eight table entries are fetched before their
+// eight ordered additions, so the gathers overlap.
 __device__ __forceinline__ float proj_row_score(const float *__restrict__ P, size_t uCols, unsigned u,
                                                 const float *__restrict__ bk, const int *__restrict__ sk, unsigned Li) {
     float v = 0.0f;
-    for (unsigned k = 0; k < Li; k++) v = fadd(v, fmul(P[(size_t)sk[k] * uCols + u], bk[k]));
+    unsigned k = 0;
+    for (; k + 8 <= Li; k += 8) {
+        float pv[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) pv[q] = P[(size_t)sk[k + q] * uCols + u];
+#pragma unroll
+        for (int q = 0; q < 8; q++) v = fadd(v, fmul(pv[q], bk[k + q]));
+    }
+    for (; k < Li; k++) v = fadd(v, fmul(P[(size_t)sk[k] * uCols + u], bk[k]));
     return v;
 }
 
@@ -675,7 +686,7 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
 
 // Rows re-scored and candidates re-scored are counted per block in shared
 // memory, then added to the global counters once per block.
-__global__ void __launch_bounds__(1024) tc_merge_kernel(DevModel md, const unsigned *__restrict__ suppLen, const float *__restrict__ Proj,
+__global__ void __launch_bounds__(256) tc_merge_kernel(DevModel md, const unsigned *__restrict__ suppLen, const float *__restrict__ Proj,
                                 size_t uCols, const unsigned *__restrict__ uniqJ, unsigned groups, size_t rPad,
                                 const float *__restrict__ a1, const float *__restrict__ a1raw,
                                 const unsigned *__restrict__ scal,
@@ -937,7 +948,7 @@ int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, 
     // ---- merge, margin, exact re-score of near ties ----
     const size_t rows = (size_t)tc->MZ * md.r;
     cudaMemsetAsync(tc->rowFlag, 0, rows * sizeof(unsigned), eng.stream);
-    tc_merge_kernel<<<(unsigned)ceil_div(rows * 32, 1024), 1024, 0, eng.stream>>>(
+    tc_merge_kernel<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, eng.stream>>>(
         md, eng.suppLen, eng.Proj, eng.projCols, eng.uniqJ, groups, tc->rPad, tc->a1, tc->a1raw, tc->scal, tc->candV,
         tc->candU,
         tc->candX, eng.ustar, eng.jstar, tc->rowFlag, tc->scal + 3, tc->badModel);
