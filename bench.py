@@ -501,8 +501,18 @@ def main():
     if gemm:
         flops = [2.0 * r * u * n_pad * cfg["m"] * cfg["z"] for u, _ in gemm]
         achieved = sum(flops) / (sum(t for _, t in gemm) * 1e-3) / 1e12
+        # DRAM traffic per launch: the ncu capture of the n=4096 small case
+        # (profiles/tc_score_gemm_n4096_small.md: 540.1 MB read + 20.2 MB
+        # written over 2048 work units) scaled by this launch's work units
+        # (m*z pairs x 128-row tiles x alpha groups); traffic grows with the
+        # units, since each unit streams one A tile and writes one candidate set.
+        u_last = gemm[-1][0]
+        units = cfg["m"] * cfg["z"] * ((r + 127) // 128) * min(8, (u_last + 255) // 256)
+        traffic = (540.1e6 + 20.2e6) / 2048.0 * units
         roofline = {"bound": "tensor", "achieved": achieved, "peak": tc_peak, "unit": "TFLOP/s",
-                    "frac": achieved / tc_peak, "traffic": None,
+                    "frac": achieved / tc_peak, "traffic": traffic,
+                    "traffic_note": "bytes per launch, scaled from an ncu capture of a 2048-unit launch to %d units"
+                                    % units,
                     "kernel": "tcgen05 FP16 scoring GEMM (kind::f16, FP32 accumulate in TMEM) with fused top-8 epilogue",
                     "flops_per_launch": flops[-1], "peak_source": peak_kind}
     else:
