@@ -105,6 +105,12 @@ NOVA_API int pomdp_pbvi_execute_batched_gpu(const POMDP *const *pomdps, POMDPPBV
         POMDPAlphaVectors *const *policies, unsigned int count, unsigned int scoring,
         unsigned int hostThreads);
 
+/* Random belief expansion seeds libc rand() with time(nullptr), as the
+ * reference does (pomdp_expand_cpu.cpp:91, pomdp_expand_gpu.cu:139). With
+ * fixed != 0, later expansions call srand(seed) instead, so runs repeat;
+ * fixed == 0 restores the clock. No reference counterpart. */
+NOVA_API int nova_gb300_expand_seed(unsigned int fixed, unsigned int seed);
+
 /* Value iteration until the Bellman residual max_s |V'(s) - V(s)|, computed
  * in FP64 on the device after every sweep, drops below tol, or maxSweeps
  * sweeps ran. The reference's VI has no convergence test (mdp_vi_gpu.cu:163-221

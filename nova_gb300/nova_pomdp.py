@@ -51,3 +51,14 @@ for _name in ("pomdp_initialize_gpu", "pomdp_uninitialize_gpu",
               "pomdp_initialize_nonzero_beliefs_gpu", "pomdp_uninitialize_nonzero_beliefs_gpu",
               "pomdp_initialize_belief_points_gpu", "pomdp_uninitialize_belief_points_gpu"):
     getattr(_nova, _name).argtypes = (_P,)
+
+# Belief-set expansion and sigma approximation (pomdp_expand_cpu.h,
+# pomdp_expand_gpu.h, pomdp_sigma_cpu.h), computed on the GPU.
+from . import nova_pomdp_alpha_vectors as _npav  # noqa: E402
+_nova.pomdp_expand_random_cpu.argtypes = (_P, ct.c_uint)
+_nova.pomdp_expand_distinct_beliefs_cpu.argtypes = (_P,)
+_nova.pomdp_expand_pema_cpu.argtypes = (_P, ct.POINTER(_npav.NovaPOMDPAlphaVectors))
+_nova.pomdp_sigma_cpu.argtypes = (_P, ct.c_uint, ct.POINTER(ct.c_float))
+_nova.pomdp_expand_random_gpu.argtypes = (_P, ct.c_uint, ct.c_uint, ct.POINTER(ct.c_uint),
+                                          ct.POINTER(ct.POINTER(ct.c_float)))
+_nova.nova_gb300_expand_seed.argtypes = (ct.c_uint, ct.c_uint)

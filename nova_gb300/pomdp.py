@@ -3,7 +3,8 @@
 Same class, fields and methods as the reference wrapper. Arrays are owned by
 the C library (pomdp_initialize_cpu allocates them); `set_arrays` fills them
 from numpy in one copy per array instead of the reference's element loop.
-File loading and belief-set expansion are not part of this library.
+File loading is not part of this library; belief-set expansion and the sigma
+approximation run on the GPU.
 """
 import ctypes as ct
 
@@ -116,12 +117,46 @@ class POMDP(npm.NovaPOMDP):
         raise NotImplementedError("nova-gb300 does not parse POMDP files; fill the arrays with set_arrays()")
 
     def expand(self, method='random', numBeliefsToAdd=1000, pemaPolicy=None, pemaAlgorithm=None):
-        """ Not provided: belief-set expansion is outside this library. """
-        raise NotImplementedError("nova-gb300 does not expand belief sets; pass Z/B with set_arrays()")
+        """ Expand the belief points (pomdp.py:202-229 of the reference): 'random' trajectories
+            (pomdp_expand_random_cpu), 'distinct_beliefs' (pomdp_expand_distinct_beliefs_cpu) or
+            'pema' (pomdp_expand_pema_cpu, with pemaPolicy or pemaAlgorithm.solve()). """
+        if method not in ["random", "distinct_beliefs", "pema"]:
+            print("Failed to expand. Method '%s' is not defined." % (method))
+            raise Exception()
+        if method == "random":
+            result = npm._nova.pomdp_expand_random_cpu(self, numBeliefsToAdd)
+        elif method == "distinct_beliefs":
+            result = npm._nova.pomdp_expand_distinct_beliefs_cpu(self)
+        else:
+            if pemaPolicy is None:
+                pemaPolicy = pemaAlgorithm.solve()
+            result = npm._nova.pomdp_expand_pema_cpu(self, ct.cast(ct.pointer(pemaPolicy),
+                                                                   ct.POINTER(npm._npav.NovaPOMDPAlphaVectors)))
+        if result != 0:
+            raise RuntimeError("belief expansion '%s' failed with code %d" % (method, result))
 
     def sigma_approximate(self, numDesiredNonZeroValues=1):
-        """ Not provided: sigma-approximation is outside this library. """
-        raise NotImplementedError("nova-gb300 does not provide the sigma approximation")
+        """ Sigma approximation of the beliefs (pomdp_sigma_cpu); returns sigma = min_b sigma_b. """
+        sigma = ct.c_float(0.0)
+        result = npm._nova.pomdp_sigma_cpu(self, numDesiredNonZeroValues, ct.byref(sigma))
+        if result != 0:
+            print("Failed to perform sigma-approximation.")
+            raise Exception()
+        return sigma.value
+
+    def arrays(self):
+        """ The model and belief arrays as numpy copies (dict of synth.py's layout). """
+        def get(ptr, count, dtype):
+            return np.ctypeslib.as_array(ptr, shape=(count,)).astype(dtype).copy() if count else \
+                np.zeros(0, dtype)
+        n, ns, m, z, r, rz = self.n, self.ns, self.m, self.z, self.r, self.rz
+        return dict(n=n, ns=ns, m=m, z=z, r=r, rz=rz, gamma=float(self.gamma), horizon=int(self.horizon),
+                    S=get(self.S, n * m * ns, np.int32).reshape(n, m, ns),
+                    T=get(self.T, n * m * ns, np.float32).reshape(n, m, ns),
+                    O=get(self.O, m * n * z, np.float32).reshape(m, n, z),
+                    R=get(self.R, n * m, np.float32).reshape(n, m),
+                    Z=get(self.Z, r * rz, np.int32).reshape(r, rz),
+                    B=get(self.B, r * rz, np.float32).reshape(r, rz))
 
     def belief_update(self, b, a, o):
         """ Belief update b' = normalise(O(a,.,o) * T(.,a,.)^T b) (pomdp_belief_update_cpu). """

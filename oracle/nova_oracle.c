@@ -782,3 +782,258 @@ double oracle_pbvi_fixed_reverse_f64(unsigned n, unsigned ns, unsigned m, unsign
     free(GammaAll);
     return V;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Belief expansion (pomdp_expand_cpu.cpp, pomdp_expand_gpu.cu)              */
+/* ------------------------------------------------------------------------ */
+
+#define ORACLE_FLT_MAX (1e+10f)    /* nova's FLT_MAX, include/nova/constants.h:33 */
+
+/* pomdp_expand_construct_belief_cpu, pomdp_expand_cpu.cpp:39-53 */
+static void construct_belief(unsigned n, unsigned rz, const int *Z, const float *B, unsigned i, float *b) {
+    for (unsigned s = 0; s < n; s++) b[s] = 0.0f;
+    for (unsigned j = 0; j < rz; j++) {
+        int s = Z[(size_t)i * rz + j];
+        if (s < 0) break;
+        b[s] = B[(size_t)i * rz + j];
+    }
+}
+
+/* pomdp_belief_update_cpu, pomdp_model_cpu.cpp:89-137. Returns 0, or 1 when
+ * the normaliser is below FLT_ERR_TOL (bp then holds the unnormalised values). */
+int oracle_belief_update(unsigned n, unsigned ns, unsigned m, unsigned z, const int *S, const float *T,
+                         const float *O, const float *b, unsigned a, unsigned o, float *bp) {
+    for (unsigned sp = 0; sp < n; sp++) bp[sp] = 0.0f;
+    for (unsigned s = 0; s < n; s++) {
+        for (unsigned i = 0; i < ns; i++) {
+            int sp = S[(size_t)s * m * ns + a * ns + i];
+            if (sp < 0) break;
+            float t = T[(size_t)s * m * ns + a * ns + i] * b[s];
+            bp[sp] = bp[sp] + t;
+        }
+    }
+    float norm = 0.0f;
+    for (unsigned sp = 0; sp < n; sp++) {
+        bp[sp] = bp[sp] * O[(size_t)a * n * z + (size_t)sp * z + o];
+        norm = norm + bp[sp];
+    }
+    if (fabs((double)fabsf(norm)) < 1e-9) return 1;
+    for (unsigned sp = 0; sp < n; sp++) bp[sp] = bp[sp] / norm;
+    return 0;
+}
+
+/* pomdp_expand_probability_observation_cpu, pomdp_expand_cpu.cpp:56-78 */
+static float prob_obs(unsigned n, unsigned ns, unsigned m, unsigned z, const int *S, const float *T,
+                      const float *O, const float *b, unsigned a, unsigned o) {
+    float pr = 0.0f;
+    for (unsigned s = 0; s < n; s++) {
+        float val = 0.0f;
+        for (unsigned i = 0; i < ns; i++) {
+            int sp = S[(size_t)s * m * ns + a * ns + i];
+            if (sp < 0) break;
+            float t = T[(size_t)s * m * ns + a * ns + i] * O[(size_t)a * n * z + (size_t)sp * z + o];
+            val = val + t;
+        }
+        float q = val * b[s];
+        pr = pr + q;
+    }
+    return pr;
+}
+
+static unsigned draw(float scale) {
+    return (unsigned)((float)rand() / (float)RAND_MAX * scale);
+}
+
+/* pomdp_expand_random_cpu, pomdp_expand_cpu.cpp:81-150, after srand(seed)
+ * (the reference seeds with time(nullptr)). Bnew [num][n]. */
+void oracle_expand_random(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz, unsigned horizon,
+                          const int *S, const float *T, const float *O, const int *Z, const float *B, unsigned num,
+                          unsigned seed, float *Bnew) {
+    srand(seed);
+    float *b = (float *)malloc(sizeof(float) * n);
+    float *bp = (float *)malloc(sizeof(float) * n);
+    for (size_t k = 0; k < (size_t)num * n; k++) Bnew[k] = 0.0f;
+    unsigned i = 0;
+    while (i < num) {
+        unsigned b0 = draw((float)r);
+        construct_belief(n, rz, Z, B, b0, b);
+        unsigned h = draw((float)(horizon + 1));
+        for (unsigned t = 0; t < h; t++) {
+            unsigned a = draw((float)m);
+            float cur = 0.0f;
+            float target = (float)rand() / (float)RAND_MAX;
+            unsigned o = 0;
+            for (unsigned op = 0; op < z; op++) {
+                float pr = prob_obs(n, ns, m, z, S, T, O, b, a, op);
+                cur = cur + pr;
+                if (cur >= target && pr > 0.0f) { o = op; break; }
+            }
+            oracle_belief_update(n, ns, m, z, S, T, O, b, a, o, bp);
+            memcpy(b, bp, sizeof(float) * n);
+            memcpy(Bnew + (size_t)i * n, b, sizeof(float) * n);
+            i++;
+            if (i >= num) break;
+        }
+    }
+    free(b);
+    free(bp);
+}
+
+/* pomdp_expand_random_gpu, pomdp_expand_gpu.cu:127-215, after srand(seed):
+ * starts every trajectory at belief 0, which is also Bnew[0]; returns the
+ * maximum non-zero count over the expanded beliefs (rows 1..). */
+unsigned oracle_expand_random_from_b0(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned rz, unsigned horizon,
+                                      const int *S, const float *T, const float *O, const int *Z, const float *B,
+                                      unsigned num, unsigned seed, float *Bnew) {
+    srand(seed);
+    unsigned maxNZ = 0;
+    float *b0 = (float *)malloc(sizeof(float) * n);
+    float *b = (float *)malloc(sizeof(float) * n);
+    float *bp = (float *)malloc(sizeof(float) * n);
+    construct_belief(n, rz, Z, B, 0, b0);
+    memcpy(Bnew, b0, sizeof(float) * n);
+    unsigned i = 1;
+    while (i < num) {
+        unsigned h = draw((float)(horizon + 1));
+        memcpy(b, b0, sizeof(float) * n);
+        for (unsigned t = 0; t < h; t++) {
+            unsigned a = draw((float)m);
+            float cur = 0.0f;
+            float target = (float)rand() / (float)RAND_MAX;
+            unsigned o = 0;
+            for (unsigned op = 0; op < z; op++) {
+                float pr = prob_obs(n, ns, m, z, S, T, O, b, a, op);
+                cur = cur + pr;
+                if (cur >= target) { o = op; break; }
+            }
+            oracle_belief_update(n, ns, m, z, S, T, O, b, a, o, bp);
+            memcpy(b, bp, sizeof(float) * n);
+            unsigned nz = 0;
+            for (unsigned s = 0; s < n; s++) nz += b[s] > 0.0f ? 1u : 0u;
+            if (nz > maxNZ) maxNZ = nz;
+            memcpy(Bnew + (size_t)i * n, b, sizeof(float) * n);
+            i++;
+            if (i >= num) break;
+        }
+    }
+    free(b0);
+    free(b);
+    free(bp);
+    return maxNZ;
+}
+
+/* pomdp_expand_distinct_beliefs_cpu, pomdp_expand_cpu.cpp:153-241. Bnew
+ * [r][n]; a belief with no valid (a, o) gets a zero row (the reference
+ * copies an uninitialised buffer). */
+void oracle_expand_distinct(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz, const int *S,
+                            const float *T, const float *O, const int *Z, const float *B, float *Bnew) {
+    float *b = (float *)malloc(sizeof(float) * n);
+    float *bp = (float *)malloc(sizeof(float) * n);
+    float *btmp = (float *)malloc(sizeof(float) * n);
+    for (unsigned i = 0; i < r; i++) {
+        construct_belief(n, rz, Z, B, i, b);
+        float *star = Bnew + (size_t)i * n;
+        for (unsigned s = 0; s < n; s++) star[s] = 0.0f;
+        float starValue = ORACLE_FLT_MIN;
+        for (unsigned a = 0; a < m; a++) {
+            for (unsigned o = 0; o < z; o++) {
+                float pr = prob_obs(n, ns, m, z, S, T, O, b, a, o);
+                if (pr == 0.0f) continue;
+                if (oracle_belief_update(n, ns, m, z, S, T, O, b, a, o, bp) != 0) continue;
+                float jStar = ORACLE_FLT_MAX;
+                for (unsigned j = 0; j < r; j++) {
+                    construct_belief(n, rz, Z, B, j, btmp);
+                    float d = 0.0f;
+                    for (unsigned s = 0; s < n; s++) d = d + fabsf(btmp[s] - bp[s]);
+                    if (d < jStar) jStar = d;
+                }
+                if (jStar > starValue) {
+                    memcpy(star, bp, sizeof(float) * n);
+                    starValue = jStar;
+                }
+            }
+        }
+    }
+    free(b);
+    free(bp);
+    free(btmp);
+}
+
+/* pomdp_expand_pema_cpu, pomdp_expand_cpu.cpp:244-383 (policy Gamma [pr][n]).
+ * Bnew [n] (one belief). */
+void oracle_expand_pema(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz, float gamma,
+                        const int *S, const float *T, const float *O, const float *R, const int *Z, const float *B,
+                        unsigned pr, const float *Gamma, float *Bnew) {
+    for (unsigned s = 0; s < n; s++) Bnew[s] = 0.0f;
+    float bStar = ORACLE_FLT_MIN;
+    float Rmax = ORACLE_FLT_MIN, Rmin = ORACLE_FLT_MAX;
+    for (unsigned s = 0; s < n; s++)
+        for (unsigned a = 0; a < m; a++) {
+            float v = R[(size_t)s * m + a];
+            if (Rmax < v) Rmax = v;
+            if (Rmin > v) Rmin = v;
+        }
+    float *b = (float *)malloc(sizeof(float) * n);
+    float *bp = (float *)malloc(sizeof(float) * n);
+    float *bc = (float *)malloc(sizeof(float) * n);
+    float *bt = (float *)malloc(sizeof(float) * n);
+    unsigned *oStar = (unsigned *)malloc(sizeof(unsigned) * m);
+    float *oStarValue = (float *)malloc(sizeof(float) * m);
+    const float hi = Rmax / (1.0f - gamma), lo = Rmin / (1.0f - gamma);
+    for (unsigned i = 0; i < r; i++) {
+        unsigned aStar = 0;
+        float aStarValue = ORACLE_FLT_MIN;
+        construct_belief(n, rz, Z, B, i, b);
+        for (unsigned a = 0; a < m; a++) { oStar[a] = 0; oStarValue[a] = ORACLE_FLT_MIN; }
+        for (unsigned a = 0; a < m; a++) {
+            float aValue = 0.0f;
+            for (unsigned o = 0; o < z; o++) {
+                float p = 0.0f;
+                for (unsigned j = 0; j < rz; j++) {
+                    int s = Z[(size_t)i * rz + j];
+                    if (s < 0) break;
+                    for (unsigned k = 0; k < ns; k++) {
+                        int sp = S[(size_t)s * m * ns + a * ns + k];
+                        if (sp < 0) break;
+                        float t1 = T[(size_t)s * m * ns + a * ns + k] * O[(size_t)a * n * z + (size_t)sp * z + o];
+                        float t2 = t1 * B[(size_t)i * rz + j];
+                        p = p + t2;
+                    }
+                }
+                if (oracle_belief_update(n, ns, m, z, S, T, O, b, a, o, bp) != 0) continue;
+                float best = ORACLE_FLT_MAX;
+                for (unsigned j = 0; j < r; j++) {
+                    construct_belief(n, rz, Z, B, j, bt);
+                    float d = 0.0f;
+                    for (unsigned s = 0; s < n; s++) d = d + fabsf(bp[s] - bt[s]);
+                    if (d < best) { memcpy(bc, bt, sizeof(float) * n); best = d; }
+                }
+                unsigned alphaStar = 0;
+                for (unsigned j = 0; j < pr; j++)
+                    for (unsigned s = 0; s < n; s++) {
+                        float Vb = Gamma[(size_t)j * n + s] * bc[s];
+                        if (Vb < ORACLE_FLT_MIN) alphaStar = j;
+                    }
+                float eps = 0.0f;
+                for (unsigned s = 0; s < n; s++) {
+                    float d = bp[s] - bc[s];
+                    float c = (bp[s] >= b[s] ? hi : lo) - Gamma[(size_t)alphaStar * n + s];
+                    float t = c * d;
+                    eps = eps + t;
+                }
+                float v = p * eps;
+                if (v > oStarValue[a]) { oStar[a] = o; oStarValue[a] = v; }
+                aValue = aValue + v;
+            }
+            if (aValue > aStarValue) { aStar = a; aStarValue = aValue; }
+        }
+        if (aStarValue > bStar) {
+            if (oracle_belief_update(n, ns, m, z, S, T, O, b, aStar, oStar[aStar], bp) == 0)
+                memcpy(Bnew, bp, sizeof(float) * n);
+            else
+                memcpy(Bnew, b, sizeof(float) * n);
+            bStar = aStarValue;
+        }
+    }
+    free(b); free(bp); free(bc); free(bt); free(oStar); free(oStarValue);
+}

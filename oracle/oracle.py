@@ -445,3 +445,221 @@ def pbvi_fixed_reverse_f64(model, Gamma0, actions, selects, b, istar=None):
                                             _p(dT, _D), _p(dO, _D), _p(dG, _D))
     _ = keep
     return V, dR, dT, dO, dG
+
+
+# ---------------------------------------------------------------------------
+# Belief expansion and sigma approximation
+# ---------------------------------------------------------------------------
+
+def _exp_lib():
+    L = lib()
+    if not getattr(L, "_exp_bound", False):
+        L.oracle_belief_update.argtypes = [ct.c_uint] * 4 + [_I, _F, _F, _F, ct.c_uint, ct.c_uint, _F]
+        L.oracle_belief_update.restype = ct.c_int
+        L.oracle_expand_random.argtypes = [ct.c_uint] * 7 + [_I, _F, _F, _I, _F, ct.c_uint, ct.c_uint, _F]
+        L.oracle_expand_random_from_b0.argtypes = [ct.c_uint] * 6 + [_I, _F, _F, _I, _F, ct.c_uint, ct.c_uint, _F]
+        L.oracle_expand_random_from_b0.restype = ct.c_uint
+        L.oracle_expand_distinct.argtypes = [ct.c_uint] * 6 + [_I, _F, _F, _I, _F, _F]
+        L.oracle_expand_pema.argtypes = [ct.c_uint] * 6 + [ct.c_float, _I, _F, _F, _F, _I, _F, ct.c_uint, _F, _F]
+        L._exp_bound = True
+    return L
+
+
+def belief_update(model, b, a, o):
+    """nova's belief update (FP32); returns (b', valid)."""
+    L = _exp_lib()
+    S, T, O, R, Z, B = _arrays(model)
+    n, ns, m, z, r, rz = _dims(model)
+    bb = np.ascontiguousarray(b, dtype=np.float32)
+    bp = np.empty(n, np.float32)
+    rc = L.oracle_belief_update(n, ns, m, z, _p(S, _I), _p(T, _F), _p(O, _F), _p(bb, _F), a, o, _p(bp, _F))
+    return bp, rc == 0
+
+
+def expand_random(model, num, seed):
+    """pomdp_expand_random_cpu after srand(seed); returns Bnew [num, n]."""
+    L = _exp_lib()
+    S, T, O, R, Z, B = _arrays(model)
+    n, ns, m, z, r, rz = _dims(model)
+    out = np.empty((num, n), np.float32)
+    L.oracle_expand_random(n, ns, m, z, r, rz, model["horizon"], _p(S, _I), _p(T, _F), _p(O, _F), _p(Z, _I),
+                           _p(B, _F), num, seed, _p(out, _F))
+    return out
+
+
+def expand_random_from_b0(model, num, seed):
+    """pomdp_expand_random_gpu after srand(seed); returns (Bnew [num, n], maxNonZeroValues)."""
+    L = _exp_lib()
+    S, T, O, R, Z, B = _arrays(model)
+    n, ns, m, z, r, rz = _dims(model)
+    out = np.empty((num, n), np.float32)
+    nz = L.oracle_expand_random_from_b0(n, ns, m, z, rz, model["horizon"], _p(S, _I), _p(T, _F), _p(O, _F),
+                                        _p(Z, _I), _p(B, _F), num, seed, _p(out, _F))
+    return out, nz
+
+
+def expand_distinct(model):
+    """pomdp_expand_distinct_beliefs_cpu's new beliefs Bnew [r, n]."""
+    L = _exp_lib()
+    S, T, O, R, Z, B = _arrays(model)
+    n, ns, m, z, r, rz = _dims(model)
+    out = np.empty((r, n), np.float32)
+    L.oracle_expand_distinct(n, ns, m, z, r, rz, _p(S, _I), _p(T, _F), _p(O, _F), _p(Z, _I), _p(B, _F),
+                             _p(out, _F))
+    return out
+
+
+def expand_pema(model, Gamma):
+    """pomdp_expand_pema_cpu's new belief [n] for the policy's Gamma [pr, n]."""
+    L = _exp_lib()
+    S, T, O, R, Z, B = _arrays(model)
+    n, ns, m, z, r, rz = _dims(model)
+    G = np.ascontiguousarray(Gamma, dtype=np.float32)
+    out = np.empty(n, np.float32)
+    L.oracle_expand_pema(n, ns, m, z, r, rz, model["gamma"], _p(S, _I), _p(T, _F), _p(O, _F), _p(R, _F),
+                         _p(Z, _I), _p(B, _F), G.shape[0], _p(G, _F), _p(out, _F))
+    return out
+
+
+def merge_raw_beliefs(Z, B, Bnew):
+    """pomdp_add_new_raw_beliefs_cpu (pomdp_model_cpu.cpp:157-227) on arrays:
+    appends the positive entries of each row of Bnew; returns (Z, B)."""
+    r, rz = Z.shape
+    nz = [(row > 0.0).sum() for row in Bnew]
+    rz2 = max([rz] + [int(v) for v in nz])
+    Zf = np.full((r + len(Bnew), rz2), -1, np.int32)
+    Bf = np.zeros((r + len(Bnew), rz2), np.float32)
+    Zf[:r, :rz] = Z
+    Bf[:r, :rz] = B
+    for i, row in enumerate(Bnew):
+        idx = np.nonzero(row > 0.0)[0]
+        Zf[r + i, :len(idx)] = idx
+        Bf[r + i, :len(idx)] = row[idx]
+    return Zf, Bf
+
+
+def _ref_bind_expand(L):
+    if not getattr(L, "_exp_bound", False):
+        P = ct.POINTER(_RefPOMDP)
+        L.pomdp_initialize_cpu.argtypes = [P] + [ct.c_uint] * 6 + [ct.c_float, ct.c_uint]
+        L.pomdp_uninitialize_cpu.argtypes = [P]
+        L.pomdp_expand_random_cpu.argtypes = [P, ct.c_uint]
+        L.pomdp_expand_distinct_beliefs_cpu.argtypes = [P]
+        L.pomdp_expand_pema_cpu.argtypes = [P, ct.POINTER(_RefAlpha)]
+        L.pomdp_sigma_cpu.argtypes = [P, ct.c_uint, ct.POINTER(ct.c_float)]
+        L.pomdp_expand_random_gpu.argtypes = [P, ct.c_uint, ct.c_uint, ct.POINTER(ct.c_uint), ct.POINTER(_F)]
+        L._exp_bound = True
+
+
+def _ref_pomdp_owned(model):
+    """A reference POMDP whose arrays the reference allocated (its expansion
+    frees and reallocates Z and B)."""
+    L = ref_lib()
+    _ref_bind_expand(L)
+    n, ns, m, z, r, rz = _dims(model)
+    p = _RefPOMDP()
+    if L.pomdp_initialize_cpu(ct.byref(p), n, ns, m, z, r, rz, model["gamma"], model["horizon"]) != 0:
+        raise RuntimeError("reference pomdp_initialize_cpu failed")
+    for name, arr, t in zip(("S", "T", "O", "R", "Z", "B"), _arrays(model), (_I, _F, _F, _F, _I, _F)):
+        ct.memmove(getattr(p, name), arr.ctypes.data, arr.nbytes)
+    return L, p
+
+
+def _ref_beliefs(p):
+    Z = np.ctypeslib.as_array(p.Z, shape=(p.r * p.rz,)).reshape(p.r, p.rz).copy()
+    B = np.ctypeslib.as_array(p.B, shape=(p.r * p.rz,)).reshape(p.r, p.rz).copy()
+    return Z, B
+
+
+def ref_expand_distinct(model):
+    L, p = _ref_pomdp_owned(model)
+    if L.pomdp_expand_distinct_beliefs_cpu(ct.byref(p)) != 0:
+        raise RuntimeError("reference distinct expansion failed")
+    out = _ref_beliefs(p)
+    L.pomdp_uninitialize_cpu(ct.byref(p))
+    return out
+
+
+def ref_expand_pema(model, Gamma, pi):
+    L, p = _ref_pomdp_owned(model)
+    G = np.ascontiguousarray(Gamma, dtype=np.float32)
+    P = np.ascontiguousarray(pi, dtype=np.uint32)
+    pol = _RefAlpha()
+    pol.n, pol.m, pol.r = model["n"], model["m"], G.shape[0]
+    pol.Gamma, pol.pi = _p(G, _F), _p(P, _U)
+    if L.pomdp_expand_pema_cpu(ct.byref(p), ct.byref(pol)) != 0:
+        raise RuntimeError("reference PEMA expansion failed")
+    out = _ref_beliefs(p)
+    L.pomdp_uninitialize_cpu(ct.byref(p))
+    return out
+
+
+def ref_sigma(model, k):
+    L, p = _ref_pomdp_owned(model)
+    sigma = ct.c_float(0.0)
+    if L.pomdp_sigma_cpu(ct.byref(p), k, ct.byref(sigma)) != 0:
+        raise RuntimeError("reference sigma approximation failed")
+    out = _ref_beliefs(p)
+    L.pomdp_uninitialize_cpu(ct.byref(p))
+    return out + (sigma.value,)
+
+
+def ref_expand_random(model, num, tries=20):
+    """The reference's random expansion seeds with time(nullptr): a call that
+    starts and ends within one clock second used that second as its seed.
+    Returns (Z, B, seed)."""
+    import time
+    for _ in range(tries):
+        L, p = _ref_pomdp_owned(model)
+        t0 = int(time.time())
+        rc = L.pomdp_expand_random_cpu(ct.byref(p), num)
+        t1 = int(time.time())
+        if rc != 0:
+            raise RuntimeError("reference random expansion failed")
+        out = _ref_beliefs(p)
+        L.pomdp_uninitialize_cpu(ct.byref(p))
+        if t0 == t1:
+            return out + (t0,)
+    raise RuntimeError("could not pin the reference's clock seed")
+
+
+def ref_expand_random_from_b0(model, num, tries=20):
+    """pomdp_expand_random_gpu of the reference (host code); returns (Bnew, maxNonZeroValues, seed)."""
+    import time
+    for _ in range(tries):
+        L, p = _ref_pomdp_owned(model)
+        nz = ct.c_uint(0)
+        Bn = _F()
+        t0 = int(time.time())
+        rc = L.pomdp_expand_random_gpu(ct.byref(p), 32, num, ct.byref(nz), ct.byref(Bn))
+        t1 = int(time.time())
+        if rc != 0:
+            raise RuntimeError("reference random expansion (b0 form) failed")
+        out = np.ctypeslib.as_array(Bn, shape=(num * model["n"],)).reshape(num, model["n"]).copy()
+        L.pomdp_uninitialize_cpu(ct.byref(p))
+        if t0 == t1:
+            return out, nz.value, t0
+    raise RuntimeError("could not pin the reference's clock seed")
+
+
+def sigma_approximate(model, k):
+    """pomdp_sigma_cpu (pomdp_sigma_cpu.cpp:49-118) on arrays: each belief
+    keeps its k largest values (equal values in support order), divided by
+    their FP32 sum; returns (Z, B, sigma)."""
+    Z, B = model["Z"], model["B"]
+    r, rz = Z.shape
+    Zn = np.full((r, k), -1, np.int32)
+    Bn = np.zeros((r, k), np.float32)
+    sigma = np.float32(1.0)
+    for i in range(r):
+        order = sorted(range(rz), key=lambda q: -float(B[i, q]))  # stable: ties keep support order
+        sb = np.float32(0.0)
+        for q in order[:k]:
+            sb = np.float32(sb + B[i, q])
+        if sb < sigma:
+            sigma = sb
+        for t, q in enumerate(order[:k]):
+            if B[i, q] > 0.0:
+                Bn[i, t] = np.float32(B[i, q] / sb)
+                Zn[i, t] = Z[i, q]
+    return Zn, Bn, float(sigma)

@@ -128,6 +128,27 @@ def main():
     G, pi = orc.ref_perseus_solve(mp, seed=42)
     save("perseus_small", mp, Gamma=G, pi=pi, srand=np.int64(42))
 
+    # Belief expansion and sigma approximation (the random forms seed from
+    # the clock; the seed of a call that stayed within one second is stored).
+    me = synth.random_pomdp(n=24, m=3, z=4, ns=5, r=30, rz=6, gamma=0.9, horizon=8, seed=3)
+    Z, B = orc.ref_expand_distinct(me)
+    save("expand_distinct", me, Z=Z, B=B)
+    mr = ragged(synth.random_pomdp(n=20, m=2, z=3, ns=4, r=25, rz=5, gamma=0.9, horizon=6, seed=41), seed=42)
+    # No empty belief here: for one the reference copies an uninitialised buffer.
+    base = synth.random_pomdp(n=20, m=2, z=3, ns=4, r=25, rz=5, gamma=0.9, horizon=6, seed=41)
+    mr["Z"][12], mr["B"][12] = base["Z"][12], base["B"][12]
+    Z, B = orc.ref_expand_distinct(mr)
+    save("expand_distinct_ragged", mr, Z=Z, B=B)
+    Z, B, seed = orc.ref_expand_random(me, 40)
+    save("expand_random", me, Z=Z, B=B, num=np.int64(40), srand=np.int64(seed))
+    Bn, nz, seed = orc.ref_expand_random_from_b0(me, 25)
+    save("expand_random_b0", me, Bnew=Bn, maxNonZero=np.int64(nz), num=np.int64(25), srand=np.int64(seed))
+    G, pi = orc.ref_pbvi_solve(me, horizon=5)
+    Z, B = orc.ref_expand_pema(me, G, pi)
+    save("expand_pema", me, Z=Z, B=B, policyGamma=G, policyPi=pi)
+    Z, B, sigma = orc.ref_sigma(me, 3)
+    save("sigma_k3", me, Z=Z, B=B, sigma=np.float32(sigma), k=np.int64(3))
+
     md = synth.random_mdp(n=1000, m=4, ns=8, gamma=0.95, horizon=50, seed=31)
     rmd = ragged(dict(md, Z=np.zeros((2, 2), np.int32), B=np.zeros((2, 2), np.float32)), seed=32)
     md.update(S=rmd["S"], T=rmd["T"])

@@ -99,7 +99,9 @@ def test_reference_python_names_are_bound():
               "pomdp_add_new_raw_beliefs_cpu", "pomdp_initialize_gpu", "pomdp_uninitialize_gpu",
               "mdp_initialize_cpu", "mdp_uninitialize_cpu", "mdp_initialize_gpu", "mdp_uninitialize_gpu",
               "pomdp_alpha_vectors_initialize", "pomdp_alpha_vectors_value_and_action",
-              "pomdp_alpha_vectors_uninitialize", "mdp_value_function_initialize", "mdp_value_function_uninitialize"]
+              "pomdp_alpha_vectors_uninitialize", "mdp_value_function_initialize", "mdp_value_function_uninitialize",
+              "pomdp_expand_random_cpu", "pomdp_expand_distinct_beliefs_cpu", "pomdp_expand_pema_cpu",
+              "pomdp_sigma_cpu", "pomdp_expand_random_gpu"]
     for what in ("successors", "state_transitions", "observation_transitions", "rewards", "nonzero_beliefs",
                  "belief_points"):
         names += ["pomdp_initialize_%s_gpu" % what, "pomdp_uninitialize_%s_gpu" % what]

@@ -151,3 +151,61 @@ def test_fixed_selection_reverse_matches_finite_differences():
             Vm, _ = orc.pbvi_fixed_forward_f64(model, model["GammaInitial"], acts, sels, b0, **{name: A})
             fd = (Vp - Vm) / (2 * h)
             assert abs(fd - grad[idx]) <= 1e-6 * max(1.0, abs(fd)), (name, idx, fd, grad[idx])
+
+
+def _model_of(g):
+    return {k: g[k] for k in ("n", "ns", "m", "z", "r", "rz", "gamma", "horizon", "S", "T", "O", "R", "Z", "B")}
+
+
+@pytest.mark.parametrize("name", ["expand_distinct", "expand_distinct_ragged"])
+def test_expand_distinct_matches_reference(name):
+    g = load_golden(name)
+    m = _model_of(g)
+    Z, B = orc.merge_raw_beliefs(m["Z"], m["B"], orc.expand_distinct(m))
+    np.testing.assert_array_equal(Z, g["out_Z"])
+    np.testing.assert_array_equal(bits(B), bits(g["out_B"]))
+
+
+def test_expand_random_matches_reference():
+    g = load_golden("expand_random")
+    m = _model_of(g)
+    Bn = orc.expand_random(m, int(g["out_num"]), int(g["out_srand"]))
+    Z, B = orc.merge_raw_beliefs(m["Z"], m["B"], Bn)
+    np.testing.assert_array_equal(Z, g["out_Z"])
+    np.testing.assert_array_equal(bits(B), bits(g["out_B"]))
+    g = load_golden("expand_random_b0")
+    Bn, nz = orc.expand_random_from_b0(_model_of(g), int(g["out_num"]), int(g["out_srand"]))
+    np.testing.assert_array_equal(bits(Bn), bits(g["out_Bnew"]))
+    assert nz == int(g["out_maxNonZero"])
+
+
+def test_expand_pema_and_sigma_match_reference():
+    g = load_golden("expand_pema")
+    m = _model_of(g)
+    Z, B = orc.merge_raw_beliefs(m["Z"], m["B"], orc.expand_pema(m, g["out_policyGamma"])[None, :])
+    np.testing.assert_array_equal(Z, g["out_Z"])
+    np.testing.assert_array_equal(bits(B), bits(g["out_B"]))
+    g = load_golden("sigma_k3")
+    Z, B, sigma = orc.sigma_approximate(_model_of(g), int(g["out_k"]))
+    np.testing.assert_array_equal(Z, g["out_Z"])
+    np.testing.assert_array_equal(bits(B), bits(g["out_B"]))
+    assert np.float32(sigma) == g["out_sigma"]
+
+
+def test_belief_update_matches_reference_when_present():
+    if not orc.ref_available():
+        pytest.skip("reference library not built")
+    m = synth.random_pomdp(n=30, m=3, z=4, ns=5, r=8, rz=6, gamma=0.9, horizon=4, seed=8)
+    b = synth.dense_belief(m, 2)
+    L, p = orc._ref_pomdp_owned(m)
+    import ctypes as ct
+    L.pomdp_belief_update_cpu.argtypes = [ct.POINTER(orc._RefPOMDP), ct.POINTER(ct.c_float), ct.c_uint, ct.c_uint,
+                                          ct.POINTER(ct.POINTER(ct.c_float))]
+    for a, o in ((0, 0), (2, 3), (1, 1)):
+        bp = ct.POINTER(ct.c_float)()
+        rc = L.pomdp_belief_update_cpu(ct.byref(p), b.ctypes.data_as(ct.POINTER(ct.c_float)), a, o, ct.byref(bp))
+        ref = np.ctypeslib.as_array(bp, shape=(m["n"],)).copy()
+        ours, ok = orc.belief_update(m, b, a, o)
+        assert ok == (rc == 0)
+        np.testing.assert_array_equal(bits(ours), bits(ref))
+    L.pomdp_uninitialize_cpu(ct.byref(p))
