@@ -364,6 +364,70 @@ def run_batch(args):
                                    "ns=min(16,n), rz=min(32,n), gamma=0.95, H=%d, seed=%d)" % (H, args.seed)}}
 
 
+def run_expand(args):
+    """Belief-set expansion on n=512, m=8, z=16, ns=16, r=1024, rz=32:
+    pomdp_expand_distinct_beliefs_cpu (1024 new beliefs; about m*z*r*n =
+    6.7e7 L1 terms per belief) and pomdp_expand_random_cpu (2048 beliefs from
+    seeded random trajectories), timed on the GPU through the C API with host
+    arrays; beside them nova's CPU algorithm (the oracle port) on a bounded
+    sample of beliefs on one host thread; the GPU rows are checked bit for bit
+    against the sampled oracle rows."""
+    import torch
+    from nova_gb300 import synth
+    from nova_gb300 import nova_pomdp as npm
+    from nova_gb300.pomdp import POMDP
+    from oracle import oracle as orc
+    cfg = dict(synth.POMDP_CONFIGS["expand_n512"])
+    model = synth.random_pomdp(**cfg, seed=args.seed)
+    n, r = cfg["n"], cfg["r"]
+
+    def distinct_once():
+        p = POMDP.from_arrays(model)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p.expand(method="distinct_beliefs")
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, p.arrays()
+
+    distinct_once()
+    times, out = [], None
+    for _ in range(max(1, args.steps)):
+        t, out = distinct_once()
+        times.append(t)
+    t_gpu = float(np.median(times))
+    sample = 16
+    t0 = time.perf_counter()
+    rows = orc.expand_distinct_rows(model, 0, sample)
+    t_cpu = time.perf_counter() - t0
+    ok = 0
+    for i in range(sample):
+        dense = np.zeros(n, np.float32)
+        for zz, bb in zip(out["Z"][r + i], out["B"][r + i]):
+            if zz >= 0:
+                dense[zz] = bb
+        ok += int(np.array_equal(dense.view(np.uint32), np.where(rows[i] > 0, rows[i], 0).astype(np.float32)
+                                 .view(np.uint32)))
+    npm._nova.nova_gb300_expand_seed(1, 77)
+    p = POMDP.from_arrays(model)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    p.expand(method="random", numBeliefsToAdd=2048)
+    torch.cuda.synchronize()
+    t_rand = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    orc.expand_random(model, 512, 77)
+    t_rand_cpu = time.perf_counter() - t0
+    npm._nova.nova_gb300_expand_seed(0, 0)
+    return {"workload": "expand_n512 (n=512,m=8,z=16,ns=16,r=1024,rz=32,seed=%d)" % args.seed,
+            "distinct": {"beliefs_per_s": r / t_gpu, "seconds": t_gpu,
+                         "cpu_baseline": {"beliefs_per_s": sample / t_cpu, "cores": 1, "kind": "port",
+                                          "sample": "%d beliefs of the distinct expansion" % sample},
+                         "rows_bit_identical_to_oracle": "%d of %d sampled" % (ok, sample)},
+            "random": {"beliefs_per_s": 2048 / t_rand, "seconds": t_rand,
+                       "cpu_baseline": {"beliefs_per_s": 512 / t_rand_cpu, "cores": 1, "kind": "port",
+                                        "sample": "512 beliefs of a seeded random expansion"}}}
+
+
 def run_mdp(args, dist_rank):
     """Bellman sweep n=2^20, m=8, ns=16 (memory-bound): GB/s of algorithmic bytes.
     Sweeps are timed through mdp_vi_execute_gpu (sweeps queued back to back):
@@ -427,6 +491,12 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.config == "expand_n512":
+        import torch
+        torch.cuda.set_device(local_rank)
+        if rank == 0:
+            print(json.dumps({"expand": run_expand(args)}))
         return
     if args.config == "batch256":
         import torch

@@ -925,12 +925,13 @@ unsigned oracle_expand_random_from_b0(unsigned n, unsigned ns, unsigned m, unsig
 /* pomdp_expand_distinct_beliefs_cpu, pomdp_expand_cpu.cpp:153-241. Bnew
  * [r][n]; a belief with no valid (a, o) gets a zero row (the reference
  * copies an uninitialised buffer). */
-void oracle_expand_distinct(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz, const int *S,
-                            const float *T, const float *O, const int *Z, const float *B, float *Bnew) {
+void oracle_expand_distinct_range(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz,
+                                  const int *S, const float *T, const float *O, const int *Z, const float *B,
+                                  unsigned i0, unsigned i1, float *Bnew) {
     float *b = (float *)malloc(sizeof(float) * n);
     float *bp = (float *)malloc(sizeof(float) * n);
     float *btmp = (float *)malloc(sizeof(float) * n);
-    for (unsigned i = 0; i < r; i++) {
+    for (unsigned i = i0; i < i1; i++) {
         construct_belief(n, rz, Z, B, i, b);
         float *star = Bnew + (size_t)i * n;
         for (unsigned s = 0; s < n; s++) star[s] = 0.0f;
@@ -957,6 +958,11 @@ void oracle_expand_distinct(unsigned n, unsigned ns, unsigned m, unsigned z, uns
     free(b);
     free(bp);
     free(btmp);
+}
+
+void oracle_expand_distinct(unsigned n, unsigned ns, unsigned m, unsigned z, unsigned r, unsigned rz, const int *S,
+                            const float *T, const float *O, const int *Z, const float *B, float *Bnew) {
+    oracle_expand_distinct_range(n, ns, m, z, r, rz, S, T, O, Z, B, 0, r, Bnew);
 }
 
 /* pomdp_expand_pema_cpu, pomdp_expand_cpu.cpp:244-383 (policy Gamma [pr][n]).

@@ -460,6 +460,7 @@ def _exp_lib():
         L.oracle_expand_random_from_b0.argtypes = [ct.c_uint] * 6 + [_I, _F, _F, _I, _F, ct.c_uint, ct.c_uint, _F]
         L.oracle_expand_random_from_b0.restype = ct.c_uint
         L.oracle_expand_distinct.argtypes = [ct.c_uint] * 6 + [_I, _F, _F, _I, _F, _F]
+        L.oracle_expand_distinct_range.argtypes = [ct.c_uint] * 6 + [_I, _F, _F, _I, _F, ct.c_uint, ct.c_uint, _F]
         L.oracle_expand_pema.argtypes = [ct.c_uint] * 6 + [ct.c_float, _I, _F, _F, _F, _I, _F, ct.c_uint, _F, _F]
         L._exp_bound = True
     return L
@@ -507,6 +508,18 @@ def expand_distinct(model):
     L.oracle_expand_distinct(n, ns, m, z, r, rz, _p(S, _I), _p(T, _F), _p(O, _F), _p(Z, _I), _p(B, _F),
                              _p(out, _F))
     return out
+
+
+def expand_distinct_rows(model, i0, i1):
+    """Rows [i0, i1) of pomdp_expand_distinct_beliefs_cpu's new beliefs (the
+    unit the CPU baseline times)."""
+    L = _exp_lib()
+    S, T, O, R, Z, B = _arrays(model)
+    n, ns, m, z, r, rz = _dims(model)
+    out = np.zeros((r, n), np.float32)
+    L.oracle_expand_distinct_range(n, ns, m, z, r, rz, _p(S, _I), _p(T, _F), _p(O, _F), _p(Z, _I), _p(B, _F),
+                                   i0, i1, _p(out, _F))
+    return out[i0:i1]
 
 
 def expand_pema(model, Gamma):
