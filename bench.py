@@ -428,6 +428,71 @@ def run_expand(args):
                                         "sample": "512 beliefs of a seeded random expansion"}}}
 
 
+def run_value(args):
+    """V(b) and the action for the r=8192 beliefs of the n=4096 workload (dense)
+    over an 8192 x 4096 alpha set: pomdp_alpha_vectors_value_batched_gpu with
+    device-resident inputs, the host-array entry point end to end, and nova's
+    one-belief evaluation (oracle port) on a sample of beliefs on one thread;
+    the sampled results are checked bit for bit."""
+    import torch
+    from nova_gb300 import synth
+    from nova_gb300 import nova_pomdp_alpha_vectors as npav
+    from nova_gb300.pomdp_alpha_vectors import POMDPAlphaVectors
+    from oracle import oracle as orc
+    cfg = dict(synth.POMDP_CONFIGS["pbvi_n4096"])
+    model = synth.random_pomdp(**cfg, seed=args.seed)
+    n, r = cfg["n"], cfg["r"]
+    rng = np.random.default_rng(args.seed + 5)
+    G = rng.uniform(-20.0, 20.0, size=(r, n)).astype(np.float32)
+    pi = rng.integers(0, cfg["m"], size=r).astype(np.uint32)
+    B = np.zeros((r, n), np.float32)
+    for i in range(r):
+        B[i, model["Z"][i]] = model["B"][i]
+    dG, dPi, dB = (torch.as_tensor(x, device="cuda") for x in (G, pi.astype(np.int32), B))
+    dV = torch.empty(r, dtype=torch.float32, device="cuda")
+    dA = torch.empty(r, dtype=torch.int32, device="cuda")
+    f = npav._nova.pomdp_alpha_vectors_value_batched_gpu
+
+    def once():
+        rc = f(dG.data_ptr(), dPi.data_ptr(), r, n, dB.data_ptr(), r, dV.data_ptr(), dA.data_ptr())
+        if rc != 0:
+            raise RuntimeError("pomdp_alpha_vectors_value_batched_gpu failed: %d" % rc)
+
+    for _ in range(args.warmup):
+        once()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        once()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    pol = POMDPAlphaVectors()
+    assert npav._nova.pomdp_alpha_vectors_initialize(pol, n, cfg["m"], r) == 0
+    import ctypes as ct
+    ct.memmove(pol.Gamma, G.ctypes.data, G.nbytes)
+    ct.memmove(pol.pi, pi.ctypes.data, pi.nbytes)
+    t0 = time.perf_counter()
+    V, a = pol.value_and_action_batched(B)
+    t_e2e = time.perf_counter() - t0
+    sample = 32
+    t0 = time.perf_counter()
+    ref = [orc.alpha_value(G, pi, B[i]) for i in range(sample)]
+    t_cpu = time.perf_counter() - t0
+    ok = sum(int(np.float32(V[i]).view(np.uint32) == np.float32(ref[i][0]).view(np.uint32) and a[i] == ref[i][1])
+             for i in range(sample))
+    _, tc_peak, _ = measured_peaks()
+    flops = 2.0 * r * r * n
+    return {"workload": "value_n4096 (8192 dense beliefs x 8192 alphas x n=4096, seed=%d)" % args.seed,
+            "beliefs_per_s": r / (ms * 1e-3), "ms": ms, "fp32_tflops": flops / (ms * 1e-3) / 1e12,
+            "e2e": {"beliefs_per_s": r / t_e2e, "seconds": t_e2e,
+                    "api": "pomdp_alpha_vectors_value_and_action_batched (host arrays, wall clock)"},
+            "cpu_baseline": {"beliefs_per_s": sample / t_cpu, "cores": 1, "kind": "port",
+                             "sample": "%d beliefs of nova's value_and_action" % sample},
+            "bit_identical": "%d of %d sampled" % (ok, sample)}
+
+
 def run_mdp(args, dist_rank):
     """Bellman sweep n=2^20, m=8, ns=16 (memory-bound): GB/s of algorithmic bytes.
     Sweeps are timed through mdp_vi_execute_gpu (sweeps queued back to back):
@@ -491,6 +556,12 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.config == "value_n4096":
+        import torch
+        torch.cuda.set_device(local_rank)
+        if rank == 0:
+            print(json.dumps({"value": run_value(args)}))
         return
     if args.config == "expand_n512":
         import torch

@@ -111,6 +111,22 @@ NOVA_API int pomdp_pbvi_execute_batched_gpu(const POMDP *const *pomdps, POMDPPBV
  * fixed == 0 restores the clock. No reference counterpart. */
 NOVA_API int nova_gb300_expand_seed(unsigned int fixed, unsigned int seed);
 
+/* V(b) and the action for count dense beliefs at once (d_B [count][n]) over a
+ * device-resident policy (d_Gamma [r][n], d_pi [r]): each result has the bits
+ * of pomdp_alpha_vectors_value_and_action (pomdp_alpha_vectors.cpp:52-79):
+ * FP32 sums in state order, maximum from -1e10 with the lowest index on
+ * ties, action pi of that alpha. d_V [count], d_a [count]. Replaces the
+ * reference's one-belief-at-a-time host evaluation; no reference
+ * counterpart for the batch. */
+NOVA_API int pomdp_alpha_vectors_value_batched_gpu(const float *d_Gamma, const unsigned int *d_pi,
+        unsigned int r, unsigned int n, const float *d_B, unsigned int count, float *d_V,
+        unsigned int *d_a);
+
+/* The same with the policy and beliefs in host memory (policy as returned by
+ * get_policy, B [count][n] host); V [count], a [count] host. */
+NOVA_API int pomdp_alpha_vectors_value_and_action_batched(const POMDPAlphaVectors *policy,
+        const float *B, unsigned int count, float *V, unsigned int *a);
+
 /* Value iteration until the Bellman residual max_s |V'(s) - V(s)|, computed
  * in FP64 on the device after every sweep, drops below tol, or maxSweeps
  * sweeps ran. The reference's VI has no convergence test (mdp_vi_gpu.cu:163-221

@@ -21,3 +21,9 @@ _nova.pomdp_alpha_vectors_initialize.argtypes = (_A, ct.c_uint, ct.c_uint, ct.c_
 _nova.pomdp_alpha_vectors_value_and_action.argtypes = (_A, ct.POINTER(ct.c_float), ct.POINTER(ct.c_float),
                                                        ct.POINTER(ct.c_uint))
 _nova.pomdp_alpha_vectors_uninitialize.argtypes = (_A,)
+
+_nova.pomdp_alpha_vectors_value_and_action_batched.argtypes = (ct.POINTER(NovaPOMDPAlphaVectors),
+                                                               ct.POINTER(ct.c_float), ct.c_uint,
+                                                               ct.POINTER(ct.c_float), ct.POINTER(ct.c_uint))
+_nova.pomdp_alpha_vectors_value_batched_gpu.argtypes = (ct.c_void_p, ct.c_void_p, ct.c_uint, ct.c_uint,
+                                                        ct.c_void_p, ct.c_uint, ct.c_void_p, ct.c_void_p)

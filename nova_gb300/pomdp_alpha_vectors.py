@@ -55,3 +55,17 @@ class POMDPAlphaVectors(npav.NovaPOMDPAlphaVectors):
             print("Failed to compute the optimal value and action.")
             raise Exception()
         return Vb.value, a.value
+
+    def value_and_action_batched(self, B):
+        """ V(b) and the action for every row of B (count x n), each with the bits of
+            value_and_action, evaluated on the GPU (pomdp_alpha_vectors_value_and_action_batched). """
+        B = np.ascontiguousarray(np.asarray(B, dtype=np.float32).reshape(-1, self.n))
+        count = B.shape[0]
+        V = np.empty(count, np.float32)
+        a = np.empty(count, np.uint32)
+        result = npav._nova.pomdp_alpha_vectors_value_and_action_batched(
+            self, B.ctypes.data_as(ct.POINTER(ct.c_float)), count, V.ctypes.data_as(ct.POINTER(ct.c_float)),
+            a.ctypes.data_as(ct.POINTER(ct.c_uint)))
+        if result != 0:
+            raise RuntimeError("pomdp_alpha_vectors_value_and_action_batched failed with code %d" % result)
+        return V, a
