@@ -127,6 +127,14 @@ NOVA_API int pomdp_alpha_vectors_value_batched_gpu(const float *d_Gamma, const u
 NOVA_API int pomdp_alpha_vectors_value_and_action_batched(const POMDPAlphaVectors *policy,
         const float *B, unsigned int count, float *V, unsigned int *a);
 
+/* Load nova's raw comma-separated POMDP / MDP files (the layout read by
+ * FileLoader.load_raw_pomdp / load_raw_mdp, python/nova/file_loader.py:74-209)
+ * into a struct whose arrays are still null; the arrays are allocated as
+ * pomdp_initialize_cpu / mdp_initialize_cpu do. Of the file's k reward
+ * functions, rewardIndex is kept (the reference's default keeps the first). */
+NOVA_API int nova_load_raw_pomdp(const char *path, POMDP *pomdp, unsigned int rewardIndex);
+NOVA_API int nova_load_raw_mdp(const char *path, MDP *mdp, unsigned int rewardIndex);
+
 /* Value iteration until the Bellman residual max_s |V'(s) - V(s)|, computed
  * in FP64 on the device after every sweep, drops below tol, or maxSweeps
  * sweeps ran. The reference's VI has no convergence test (mdp_vi_gpu.cu:163-221

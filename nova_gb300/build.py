@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "lib", "libnova.so")
 
-SOURCES = ["runtime.cpp", "mdp_vi.cu", "mdp_vi_tiled.cu", "pbvi.cu", "pbvi_tc.cu", "pbvi_adjoint.cu", "pbvi_batched.cu", "expand.cu", "value_batched.cu", "perseus.cu", "value_noalloc.cu"]
+SOURCES = ["runtime.cpp", "mdp_vi.cu", "mdp_vi_tiled.cu", "pbvi.cu", "pbvi_tc.cu", "pbvi_adjoint.cu", "pbvi_batched.cu", "expand.cu", "value_batched.cu", "loaders.cpp", "perseus.cu", "value_noalloc.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "--default-stream", "per-thread", "-Xcompiler", "-fPIC,-ffp-contract=off",

@@ -101,5 +101,17 @@ class MDP(nm.NovaMDP):
         p.set_arrays(model["S"], model["T"], model["R"], model.get("goals"))
         return p
 
-    def load(self, filename, filetype='cassandra', scalarize=lambda x: x[0]):
-        raise NotImplementedError("nova-gb300 does not parse MDP files; fill the arrays with set_arrays()")
+    def load(self, filename, filetype='cassandra', scalarize=lambda x: x[0], rewardIndex=0):
+        """ Load an MDP file (mdp.py of the reference). 'raw' files are parsed by
+            nova_load_raw_mdp (C++), keeping reward function rewardIndex. """
+        if filetype != 'raw':
+            raise NotImplementedError("nova-gb300 parses raw files only; use set_arrays() for others")
+        if self.S:
+            raise RuntimeError("the MDP already holds arrays")
+        result = nm._nova.nova_load_raw_mdp(str(filename).encode(), self, int(rewardIndex))
+        if result != 0:
+            print("Failed to load file '%s'." % (filename))
+            raise Exception()
+        R = np.ctypeslib.as_array(self.R, shape=(self.n * self.m,))
+        self.Rmin = float(R.min())
+        self.Rmax = float(R.max())

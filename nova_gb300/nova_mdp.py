@@ -37,3 +37,4 @@ for _name in ("mdp_initialize_gpu", "mdp_uninitialize_gpu",
               "mdp_initialize_rewards_gpu", "mdp_uninitialize_rewards_gpu",
               "mdp_initialize_goals_gpu", "mdp_uninitialize_goals_gpu"):
     getattr(_nova, _name).argtypes = (_M,)
+_nova.nova_load_raw_mdp.argtypes = (ct.c_char_p, ct.POINTER(NovaMDP), ct.c_uint)

@@ -62,3 +62,4 @@ _nova.pomdp_sigma_cpu.argtypes = (_P, ct.c_uint, ct.POINTER(ct.c_float))
 _nova.pomdp_expand_random_gpu.argtypes = (_P, ct.c_uint, ct.c_uint, ct.POINTER(ct.c_uint),
                                           ct.POINTER(ct.POINTER(ct.c_float)))
 _nova.nova_gb300_expand_seed.argtypes = (ct.c_uint, ct.c_uint)
+_nova.nova_load_raw_pomdp.argtypes = (ct.c_char_p, _P, ct.c_uint)

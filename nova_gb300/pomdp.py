@@ -112,9 +112,22 @@ class POMDP(npm.NovaPOMDP):
         p.set_arrays(model["S"], model["T"], model["O"], model["R"], model["Z"], model["B"])
         return p
 
-    def load(self, filename, filetype='cassandra', scalarize=lambda x: x[0]):
-        """ Not provided: model files are parsed outside this library (see set_arrays). """
-        raise NotImplementedError("nova-gb300 does not parse POMDP files; fill the arrays with set_arrays()")
+    def load(self, filename, filetype='cassandra', scalarize=lambda x: x[0], rewardIndex=0):
+        """ Load a POMDP file (pomdp.py:149-200 of the reference). 'raw' files are parsed by
+            nova_load_raw_pomdp (C++), keeping reward function rewardIndex (the reference's
+            default scalarisation keeps the first; other scalarisations are not supported).
+            The 'cassandra' format is not parsed by this library. """
+        if filetype != 'raw':
+            raise NotImplementedError("nova-gb300 parses raw files only; use set_arrays() for others")
+        if self.S:
+            raise RuntimeError("the POMDP already holds arrays")
+        result = npm._nova.nova_load_raw_pomdp(str(filename).encode(), self, int(rewardIndex))
+        if result != 0:
+            print("Failed to load file '%s'." % (filename))
+            raise Exception()
+        R = np.ctypeslib.as_array(self.R, shape=(self.n * self.m,))
+        self.Rmin = float(R.min())
+        self.Rmax = float(R.max())
 
     def expand(self, method='random', numBeliefsToAdd=1000, pemaPolicy=None, pemaAlgorithm=None):
         """ Expand the belief points (pomdp.py:202-229 of the reference): 'random' trajectories

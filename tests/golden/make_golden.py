@@ -97,6 +97,35 @@ def two_state():
     return model
 
 
+def reference_loader():
+    sys.path.insert(0, os.path.join(REF_DIR, "python", "nova"))
+    import file_loader  # the reference's loader
+    return file_loader.FileLoader()
+
+
+def loader_fixtures():
+    import raw_files
+    mp = ragged(synth.random_pomdp(n=12, m=3, z=4, ns=3, r=6, rz=4, gamma=0.9, horizon=7, seed=51), seed=52)
+    path = os.path.join(HERE, "loader_pomdp.raw")
+    raw_files.write_raw_pomdp(mp, path, k=2)
+    fl = reference_loader()
+    fl.load_raw_pomdp(path)
+    np.savez_compressed(os.path.join(HERE, "loader_pomdp.npz"), n=fl.n, ns=fl.ns, m=fl.m, z=fl.z, r=fl.r, rz=fl.rz,
+                        horizon=fl.horizon, gamma=np.float32(fl.gamma), S=np.asarray(fl.S, np.int32),
+                        T=np.asarray(fl.T, np.float32), O=np.asarray(fl.O, np.float32),
+                        R=np.asarray(fl.R, np.float32), Z=np.asarray(fl.Z, np.int32), B=np.asarray(fl.B, np.float32))
+    md = synth.random_mdp(n=15, m=2, ns=4, gamma=0.95, horizon=9, seed=53)
+    path = os.path.join(HERE, "loader_mdp.raw")
+    raw_files.write_raw_mdp(md, path, k=3, s0=2, goals=(4, 11))
+    fl = reference_loader()
+    fl.load_raw_mdp(path)
+    np.savez_compressed(os.path.join(HERE, "loader_mdp.npz"), n=fl.n, ns=fl.ns, m=fl.m, horizon=fl.horizon,
+                        gamma=np.float32(fl.gamma), s0=fl.s0, goals=np.asarray(fl.goals, np.uint32),
+                        S=np.asarray(fl.S, np.int32), T=np.asarray(fl.T, np.float32),
+                        R=np.asarray(fl.R, np.float32), epsilon=np.float32(fl.epsilon))
+    print("wrote loader fixtures")
+
+
 def main():
     if not orc.ref_available():
         raise SystemExit("the reference library is not available (needs %s)" % REF_DIR)
@@ -148,6 +177,10 @@ def main():
     save("expand_pema", me, Z=Z, B=B, policyGamma=G, policyPi=pi)
     Z, B, sigma = orc.ref_sigma(me, 3)
     save("sigma_k3", me, Z=Z, B=B, sigma=np.float32(sigma), k=np.int64(3))
+
+    # Raw-file loaders: files written by raw_files.py, parsed by the
+    # reference's FileLoader; the parsed arrays are the fixture.
+    loader_fixtures()
 
     md = synth.random_mdp(n=1000, m=4, ns=8, gamma=0.95, horizon=50, seed=31)
     rmd = ragged(dict(md, Z=np.zeros((2, 2), np.int32), B=np.zeros((2, 2), np.float32)), seed=32)

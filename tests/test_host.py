@@ -2,6 +2,7 @@
 argument validation and error codes, policy containers, belief update,
 fault injection wiring."""
 import ctypes as ct
+import os
 
 import numpy as np
 import pytest
@@ -140,3 +141,72 @@ def test_fault_injection_hook_is_wired():
     assert L.pomdp_initialize_successors_gpu(p) == DEVICE_MALLOC
     assert not p.d_S
     L.nova_gb300_inject_fault(0, 0)
+
+
+# ---------------------------------------------------------------------------
+# Raw-file loaders (host code; no GPU)
+# ---------------------------------------------------------------------------
+
+def test_raw_pomdp_loader_matches_reference_loader():
+    from conftest import GOLDEN
+    from nova_gb300.pomdp import POMDP
+    g = np.load(os.path.join(GOLDEN, "loader_pomdp.npz"))
+    p = POMDP()
+    p.load(os.path.join(GOLDEN, "loader_pomdp.raw"), filetype="raw")
+    out = p.arrays()
+    for k in ("n", "ns", "m", "z", "r", "rz", "horizon"):
+        assert out[k] == int(g[k])
+    assert np.float32(out["gamma"]) == g["gamma"]
+    for k in ("S", "Z"):
+        np.testing.assert_array_equal(out[k], g[k])
+    for k in ("T", "O", "R", "B"):
+        np.testing.assert_array_equal(out[k].view(np.uint32), g[k].view(np.uint32))
+    assert p.Rmin == float(g["R"].min())
+
+
+def test_raw_mdp_loader_matches_reference_loader():
+    from conftest import GOLDEN
+    from nova_gb300.mdp import MDP
+    g = np.load(os.path.join(GOLDEN, "loader_mdp.npz"))
+    m = MDP()
+    m.load(os.path.join(GOLDEN, "loader_mdp.raw"), filetype="raw")
+    assert (m.n, m.ns, m.m, m.horizon, m.s0, m.ng) == (int(g["n"]), int(g["ns"]), int(g["m"]), int(g["horizon"]),
+                                                      int(g["s0"]), len(g["goals"]))
+    assert np.float32(m.gamma) == g["gamma"] and np.float32(m.epsilon) == g["epsilon"]
+    S = np.ctypeslib.as_array(m.S, shape=(m.n * m.m * m.ns,)).reshape(m.n, m.m, m.ns)
+    T = np.ctypeslib.as_array(m.T, shape=(m.n * m.m * m.ns,)).reshape(m.n, m.m, m.ns)
+    R = np.ctypeslib.as_array(m.R, shape=(m.n * m.m,)).reshape(m.n, m.m)
+    goals = np.ctypeslib.as_array(m.goals, shape=(m.ng,))
+    np.testing.assert_array_equal(S, g["S"])
+    np.testing.assert_array_equal(T.view(np.uint32), g["T"].view(np.uint32))
+    np.testing.assert_array_equal(R.view(np.uint32), g["R"].view(np.uint32))
+    np.testing.assert_array_equal(goals, g["goals"])
+
+
+def test_raw_loader_rejects_bad_files(tmp_path):
+    from nova_gb300.pomdp import POMDP
+    bad = tmp_path / "bad.raw"
+    bad.write_text("3,2,2,2,1,1,1,0,5,0.9\n0,1\n")
+    p = POMDP()
+    with pytest.raises(Exception):
+        p.load(str(bad), filetype="raw")
+    with pytest.raises(Exception):
+        POMDP().load(str(tmp_path / "missing.raw"), filetype="raw")
+
+
+@pytest.mark.skipif(not os.path.isfile("/root/reference/tests/tiger/tiger_pomdp.raw"),
+                    reason="reference fixtures not present")
+def test_raw_loader_on_reference_tiger_file():
+    import sys
+    from nova_gb300.pomdp import POMDP
+    sys.path.insert(0, "/root/reference/python/nova")
+    import file_loader
+    path = "/root/reference/tests/tiger/tiger_pomdp.raw"
+    fl = file_loader.FileLoader()
+    fl.load_raw_pomdp(path)
+    p = POMDP()
+    p.load(path, filetype="raw")
+    out = p.arrays()
+    for k, t in (("S", np.int32), ("T", np.float32), ("O", np.float32), ("R", np.float32), ("Z", np.int32),
+                 ("B", np.float32)):
+        np.testing.assert_array_equal(out[k], np.asarray(getattr(fl, k), t))
