@@ -84,59 +84,27 @@ __device__ __forceinline__ void load_pairs(uint4 (&buf)[kPairGroups], const uint
     }
 }
 
-// Level boundaries of (block, tile, warp): lane q <= L holds entry q of the
-// slice's L+1 boundaries (level q is [entry q, entry q+1)).
-__device__ __forceinline__ unsigned load_levels(const unsigned *__restrict__ levelStart, size_t sub, unsigned L,
-                                                unsigned lane) {
-    return lane <= L ? __ldg(levelStart + sub + lane) : 0u;
-}
-
-__device__ __forceinline__ void add_record(float *part, unsigned row, float prod) {
-    part[row] = fadd(part[row], prod);
-}
-
 // Apply one pair-group: records [g0, g0 + 64) of this warp's slice, lane l
-// holding records g0 + 2l and g0 + 2l + 1. Records outside [b0, b1) are
-// skipped. The group may span several levels; each level is one pass (rows
-// within a level are distinct), in level order; q carries the level of the
-// group's first record from group to group.
+// holding records g0 + 2l and g0 + 2l + 1; records outside [b0, b1) and
+// padding records are skipped. The plan keeps two records of one row at
+// least 64 positions apart, so the rows of a pair-group are distinct; groups
+// run in slice order, which is each row's successor order.
 __device__ __forceinline__ void apply_pairs(uint4 r, unsigned g0, unsigned b0, unsigned b1, unsigned lane,
-                                            unsigned levels, unsigned L, unsigned &q, float gamma,
-                                            const float *vtile, unsigned tileLen, float *part, unsigned rows) {
+                                            float gamma, const float *vtile, unsigned tileLen, float *part,
+                                            unsigned rows) {
     const unsigned p0 = g0 + 2u * lane, p1 = p0 + 1u;
     const unsigned row0 = r.x >> 16, off0 = r.x & 0xFFFFu;
     const unsigned row1 = r.z >> 16, off1 = r.z & 0xFFFFu;
-    const bool v0 = p0 >= b0 && p0 < b1 && row0 < rows && off0 < tileLen;
-    const bool v1 = p1 >= b0 && p1 < b1 && row1 < rows && off1 < tileLen;
-    float prod0 = 0.0f, prod1 = 0.0f;
-    if (v0) prod0 = fmul(fmul(gamma, __uint_as_float(r.y)), vtile[off0]);
-    if (v1) prod1 = fmul(fmul(gamma, __uint_as_float(r.w)), vtile[off1]);
-    const unsigned first = max(g0, b0);
-    const unsigned ge = min(g0 + 64u, b1);
-    while (q + 1 < L && __shfl_sync(0xffffffffu, levels, q + 1) <= first) q++;
-    unsigned hi = __shfl_sync(0xffffffffu, levels, q + 1);
-    if (hi >= ge) {
-        // One level: a lane's two records have distinct rows too.
-        if (v0) add_record(part, row0, prod0);
-        if (v1) add_record(part, row1, prod1);
-        __syncwarp();
-        return;
-    }
-    unsigned lo = first;
-    while (true) {
-        if (v0 && p0 >= lo && p0 < hi) add_record(part, row0, prod0);
-        if (v1 && p1 >= lo && p1 < hi) add_record(part, row1, prod1);
-        __syncwarp();
-        if (hi >= ge || q + 1 >= L) break;
-        q++;
-        lo = hi;
-        hi = __shfl_sync(0xffffffffu, levels, q + 1);
-    }
+    if (p0 >= b0 && p0 < b1 && row0 < rows && off0 < tileLen)
+        part[row0] = fadd(part[row0], fmul(fmul(gamma, __uint_as_float(r.y)), vtile[off0]));
+    if (p1 >= b0 && p1 < b1 && row1 < rows && off1 < tileLen)
+        part[row1] = fadd(part[row1], fmul(fmul(gamma, __uint_as_float(r.w)), vtile[off1]));
+    __syncwarp();
 }
 
 __global__ void __launch_bounds__(kThreads, 1) bellman_tiled_kernel(
-        unsigned n, unsigned m, float gamma, unsigned Vt, unsigned T, unsigned Sb, unsigned blocks, unsigned L,
-        const uint2 *__restrict__ rec, const unsigned *__restrict__ levelStart, const float *__restrict__ R,
+        unsigned n, unsigned m, float gamma, unsigned Vt, unsigned T, unsigned Sb, unsigned blocks,
+        const uint2 *__restrict__ rec, const unsigned *__restrict__ sliceStart, const float *__restrict__ R,
         const float *__restrict__ V, float *__restrict__ Vp, unsigned *__restrict__ pi, ViDeviceState *st,
         double tol, int early_exit) {
     if (early_exit && *(volatile unsigned *)&st->converged) return;  // uniform across the grid
@@ -151,48 +119,46 @@ __global__ void __launch_bounds__(kThreads, 1) bellman_tiled_kernel(
         const unsigned nsb = min(Sb, n - s0);
         const unsigned rows = nsb * m;
         for (unsigned i = tid; i < rows; i += blockDim.x) part[i] = __ldg(R + (size_t)s0 * m + i);
-        // Sub-bin (block, tile, warp) starts at levelStart[((blk*T + t)*kWarps + warp)*L].
-        const size_t sub0 = ((size_t)blk * T * kWarps + warp) * L;
-        const size_t tileStride = (size_t)kWarps * L;
-        unsigned lvCur = load_levels(levelStart, sub0, L, lane);
-        unsigned lvNext = T > 1 ? load_levels(levelStart, sub0 + tileStride, L, lane) : 0u;
+        // Slice (block, tile, warp) is sliceStart[(blk*T + t)*kWarps + warp] ..
+        // sliceStart[... + 1]; lanes 0 and 1 hold the two bounds.
+        const size_t sub0 = (size_t)blk * T * kWarps + warp;
+        unsigned bdCur = lane < 2 ? __ldg(sliceStart + sub0 + lane) : 0u;
+        unsigned bdNext = (T > 1 && lane < 2) ? __ldg(sliceStart + sub0 + kWarps + lane) : 0u;
         stage_tile(vt, V, n, 0, Vt);
         uint4 cur[kPairGroups], nxt[kPairGroups];
 #pragma unroll
         for (int k = 0; k < kPairGroups; k++) nxt[k] = make_uint4(0xFFFFFFFFu, 0u, 0xFFFFFFFFu, 0u);
-        load_pairs(cur, rec2, __shfl_sync(0xffffffffu, lvCur, 0) & ~1u, __shfl_sync(0xffffffffu, lvCur, L), lane);
+        load_pairs(cur, rec2, __shfl_sync(0xffffffffu, bdCur, 0) & ~1u, __shfl_sync(0xffffffffu, bdCur, 1), lane);
         cp_async_wait_all();
         __syncthreads();
         for (unsigned t = 0; t < T; t++) {
             const float *vcur = vt + (size_t)(t & 1) * Vt;
-            unsigned lvNext2 = 0u;
+            unsigned bdNext2 = 0u;
             if (t + 1 < T) {
                 // The other buffer held tile t-1; every warp passed the
                 // barrier that ended tile t-1, so it is free.
                 stage_tile(vt + (size_t)((t + 1) & 1) * Vt, V, n, t + 1, Vt);
-                load_pairs(nxt, rec2, __shfl_sync(0xffffffffu, lvNext, 0) & ~1u,
-                           __shfl_sync(0xffffffffu, lvNext, L), lane);
-                if (t + 2 < T) lvNext2 = load_levels(levelStart, sub0 + (size_t)(t + 2) * tileStride, L, lane);
+                load_pairs(nxt, rec2, __shfl_sync(0xffffffffu, bdNext, 0) & ~1u,
+                           __shfl_sync(0xffffffffu, bdNext, 1), lane);
+                if (t + 2 < T && lane < 2) bdNext2 = __ldg(sliceStart + sub0 + (size_t)(t + 2) * kWarps + lane);
             }
-            const unsigned b0 = __shfl_sync(0xffffffffu, lvCur, 0), b1 = __shfl_sync(0xffffffffu, lvCur, L);
+            const unsigned b0 = __shfl_sync(0xffffffffu, bdCur, 0), b1 = __shfl_sync(0xffffffffu, bdCur, 1);
             const unsigned a0 = b0 & ~1u;
             const unsigned tileLen = min(Vt, n - t * Vt);
-            unsigned q = 0;
             for (unsigned c0 = a0; c0 < b1; c0 += 64u * kPairGroups) {
                 if (c0 != a0) load_pairs(cur, rec2, c0, b1, lane);
 #pragma unroll
                 for (int k = 0; k < kPairGroups; k++) {
                     const unsigned g0 = c0 + 64u * k;
-                    if (g0 < b1)
-                        apply_pairs(cur[k], g0, b0, b1, lane, lvCur, L, q, gamma, vcur, tileLen, part, rows);
+                    if (g0 < b1) apply_pairs(cur[k], g0, b0, b1, lane, gamma, vcur, tileLen, part, rows);
                 }
             }
             cp_async_wait_all();
             __syncthreads();
 #pragma unroll
             for (int k = 0; k < kPairGroups; k++) cur[k] = nxt[k];
-            lvCur = lvNext;
-            lvNext = lvNext2;
+            bdCur = bdNext;
+            bdNext = bdNext2;
         }
         // Action scan of mdp_vi_cpu.cpp:55-58 (lowest action on ties).
         for (unsigned i = tid; i < nsb; i += blockDim.x) {
@@ -298,6 +264,75 @@ __global__ void vi_plan_fill_kernel(PlanGeometry g, unsigned blocks, const int *
     }
 }
 
+// Final layout. Slice sl = (block, tile, warp) holds levels 0..L-1, each
+// sorted by row. The run length of a row (the number of levels it appears
+// in) is found from the deepest level up; the final slice lists, level after
+// level, the rows of that level ordered by (run length descending, row), so
+// level q+1 is a prefix-aligned continuation of level q, and each level
+// after the first starts at least 64 records after the previous one (padding
+// records in between). Two records of one row are then always at least 64
+// positions apart: any 64 consecutive records have distinct rows.
+__global__ void vi_plan_len_kernel(unsigned nSlices, unsigned L, const unsigned *__restrict__ ls,
+                                   const uint2 *__restrict__ recL, unsigned char *__restrict__ len) {
+    const unsigned sl = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sl >= nSlices) return;
+    const size_t base = (size_t)sl * L;
+    for (int q = (int)L - 1; q >= 0; q--) {
+        const unsigned e0 = ls[base + q], e1 = ls[base + q + 1];
+        if (q == (int)L - 1) {
+            for (unsigned e = e0; e < e1; e++) len[e] = (unsigned char)L;
+            continue;
+        }
+        unsigned p = e1;  // level q+1 starts where level q ends
+        const unsigned p1 = ls[base + q + 2];
+        for (unsigned e = e0; e < e1; e++) {
+            const unsigned row = recL[e].x >> 16;
+            while (p < p1 && (recL[p].x >> 16) < row) p++;
+            len[e] = (p < p1 && (recL[p].x >> 16) == row) ? len[p] : (unsigned char)(q + 1);
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned slice_levels(const unsigned *ls, size_t base, unsigned L) {
+    unsigned q = 0;
+    while (q < L && ls[base + q + 1] > ls[base + q]) q++;
+    return q;
+}
+
+__global__ void vi_plan_size_kernel(unsigned nSlices, unsigned L, const unsigned *__restrict__ ls,
+                                    unsigned *__restrict__ size) {
+    const unsigned sl = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sl >= nSlices) return;
+    const size_t base = (size_t)sl * L;
+    const unsigned Ls = slice_levels(ls, base, L);
+    unsigned pos = 0;
+    for (unsigned q = 0; q < Ls; q++) {
+        const unsigned start = pos;
+        pos += ls[base + q + 1] - ls[base + q];
+        if (q + 1 < Ls) pos = max(pos, start + 64u);
+    }
+    size[sl] = pos;
+}
+
+__global__ void vi_plan_order_kernel(unsigned nSlices, unsigned L, const unsigned *__restrict__ ls,
+                                     const uint2 *__restrict__ recL, const unsigned char *__restrict__ len,
+                                     const unsigned *__restrict__ sliceStart, uint2 *__restrict__ rec) {
+    const unsigned sl = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sl >= nSlices) return;
+    const size_t base = (size_t)sl * L;
+    const unsigned Ls = slice_levels(ls, base, L);
+    uint2 *out = rec + sliceStart[sl];
+    unsigned pos = 0;
+    for (unsigned q = 0; q < Ls; q++) {
+        const unsigned start = pos;
+        const unsigned e0 = ls[base + q], e1 = ls[base + q + 1];
+        for (unsigned l = Ls; l > q; l--)
+            for (unsigned e = e0; e < e1; e++)
+                if (len[e] == l) out[pos++] = recL[e];
+        if (q + 1 < Ls) pos = max(pos, start + 64u);  // padding slots keep the sentinel
+    }
+}
+
 // Exclusive scan of in[0..N) into out[0..N] (out[N] = total) in three
 // launches: block sums, a one-block scan of those, then each block's scan.
 constexpr unsigned kScanChunk = 4096;  // elements per block (4 per thread)
@@ -390,10 +425,11 @@ bool try_alloc(T **p, size_t count) {
 void release(ViTilePlan *plan) {
     cudaFree(plan->rec);
     cudaFree(plan->levelStart);
+    cudaFree(plan->sliceStart);
     cudaFree(plan->counts);
     cudaFree(plan->flags);
     plan->rec = nullptr;
-    plan->levelStart = plan->counts = plan->flags = nullptr;
+    plan->levelStart = plan->sliceStart = plan->counts = plan->flags = nullptr;
 }
 
 int scan_counts(const unsigned *counts, unsigned long long N, unsigned *out, cudaStream_t stream, const char *fn) {
@@ -539,6 +575,56 @@ int vi_plan_build(ViTilePlan *plan, const MDP *mdp, const int *S, const float *T
     cudaFree(plan->counts);
     cudaFree(plan->flags);
     plan->counts = plan->flags = nullptr;
+
+    // Pass 4: the final layout (rows by run length, levels 64 records apart).
+    const unsigned nSlices = (unsigned)((unsigned long long)blocks * tiles * kWarps);
+    unsigned char *len = nullptr;
+    unsigned *sliceSize = nullptr;
+    uint2 *rec2 = nullptr;
+    if (!try_alloc(&len, (size_t)total + 1) || !try_alloc(&sliceSize, nSlices) ||
+            !try_alloc(&plan->sliceStart, (size_t)nSlices + 1)) {
+        cudaFree(len);
+        cudaFree(sliceSize);
+        release(plan);
+        return NOVA_SUCCESS;
+    }
+    const unsigned sliceBlocks = ceil_div(nSlices, 128);
+    vi_plan_len_kernel<<<sliceBlocks, 128, 0, stream>>>(nSlices, L, plan->levelStart, plan->rec, len);
+    rc = check_launch(fn, "sweep plan (run lengths)");
+    if (rc == NOVA_SUCCESS) {
+        vi_plan_size_kernel<<<sliceBlocks, 128, 0, stream>>>(nSlices, L, plan->levelStart, sliceSize);
+        rc = check_launch(fn, "sweep plan (slice sizes)");
+    }
+    if (rc == NOVA_SUCCESS) rc = scan_counts(sliceSize, nSlices, plan->sliceStart, stream, fn);
+    unsigned total2 = 0;
+    if (rc == NOVA_SUCCESS)
+        rc = d2h(&total2, plan->sliceStart + nSlices, sizeof(unsigned), fn, "the sweep plan size");
+    // Small slices pay a lot of padding; in automatic mode such models keep
+    // the per-row sweep.
+    if (rc == NOVA_SUCCESS && mode == NOVA_VI_TILING_AUTO && (double)total2 > 1.5 * (double)total)
+        rc = NOVA_ERROR_DEVICE_MALLOC;
+    if (rc == NOVA_SUCCESS && !try_alloc(&rec2, (size_t)total2 + 1)) rc = NOVA_ERROR_DEVICE_MALLOC;
+    if (rc == NOVA_SUCCESS && cudaMemsetAsync(rec2, 0xFF, ((size_t)total2 + 1) * sizeof(uint2), stream) != cudaSuccess) {
+        cudaGetLastError();
+        rc = NOVA_ERROR_KERNEL_EXECUTION;
+    }
+    if (rc == NOVA_SUCCESS) {
+        vi_plan_order_kernel<<<sliceBlocks, 128, 0, stream>>>(nSlices, L, plan->levelStart, plan->rec, len,
+                                                              plan->sliceStart, rec2);
+        rc = check_launch(fn, "sweep plan (order)");
+    }
+    if (rc == NOVA_SUCCESS) rc = sync_device(fn);
+    cudaFree(len);
+    cudaFree(sliceSize);
+    if (rc != NOVA_SUCCESS) {
+        cudaFree(rec2);
+        release(plan);
+        return rc == NOVA_ERROR_DEVICE_MALLOC ? NOVA_SUCCESS : rc;  // kGather
+    }
+    cudaFree(plan->rec);
+    cudaFree(plan->levelStart);
+    plan->levelStart = nullptr;
+    plan->rec = rec2;
     plan->tileStates = Vt;
     plan->tiles = tiles;
     plan->blockStates = Sb;
@@ -554,8 +640,8 @@ int vi_plan_build(ViTilePlan *plan, const MDP *mdp, const int *S, const float *T
 int vi_tiled_sweep(const ViTilePlan *plan, const MDP *mdp, const float *R, const float *V, float *Vp, unsigned *pi,
                    ViDeviceState *st, double tol, int early_exit, cudaStream_t stream, const char *fn) {
     bellman_tiled_kernel<<<plan->grid, kThreads, plan->smemBytes, stream>>>(
-        mdp->n, mdp->m, mdp->gamma, plan->tileStates, plan->tiles, plan->blockStates, plan->blocks, plan->levels,
-        plan->rec, plan->levelStart, R, V, Vp, pi, st, tol, early_exit);
+        mdp->n, mdp->m, mdp->gamma, plan->tileStates, plan->tiles, plan->blockStates, plan->blocks, plan->rec,
+        plan->sliceStart, R, V, Vp, pi, st, tol, early_exit);
     return check_launch(fn, "Bellman update (tiled)");
 }
 

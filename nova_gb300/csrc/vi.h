@@ -64,7 +64,8 @@ struct ViTilePlan {
     unsigned grid = 0;          // resident CTAs
     size_t smemBytes = 0;
     uint2 *rec = nullptr;          // [entries] {row << 16 | offset in tile, T bits}
-    unsigned *levelStart = nullptr;  // [blocks*tiles*32*levels + 1] first record of each sub-bin
+    unsigned *levelStart = nullptr;  // build scratch: first record of each (slice, level) sub-bin
+    unsigned *sliceStart = nullptr;  // [blocks*tiles*warps + 1] first record of each (block, tile, warp) slice
     unsigned *counts = nullptr;    // build scratch
     unsigned *flags = nullptr;     // build scratch: unsorted rows, out-of-range successor, longest run
     ~ViTilePlan();
