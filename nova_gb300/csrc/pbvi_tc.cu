@@ -10,8 +10,8 @@
 // (which changes every score of a row by the same amount), into BF16, and
 // the GEMM scores every row against every unique alpha on the tcgen05
 // tensor cores with FP32 accumulation in TMEM. The epilogue keeps, per row,
-// the 4 best (score, alpha) pairs and the best score it dropped; the scores
-// never reach HBM.
+// the 8 best (score, alpha) pairs of each list and the best score it
+// dropped; the scores never reach HBM.
 //
 // Exactness: for every row the kernel's score differs from the reference's
 // FP32 score (pomdp_pbvi_cpu.cpp:50-83) by at most
@@ -25,11 +25,13 @@
 // action) pair is rescanned exactly over all alphas. The chosen alphas are
 // therefore exactly the reference's.
 //
-// GEMM kernel: persistent, one CTA per SM, 6 warps: warp 0 issues TMA loads
+// GEMM kernel: persistent, one CTA per SM, 10 warps: warp 0 issues TMA loads
 // (SWIZZLE_128B tiles 128x64 of A and 256x64 of the alphas into a 4-stage
 // ring), warp 1 issues tcgen05.mma (M=128, N=256, K=16, cta_group::1) into
-// two 256-column TMEM accumulators, warps 2-5 drain TMEM with tcgen05.ld and
-// run the top-4 epilogue while the next tile accumulates. Work units are
+// two 256-column TMEM accumulators, warps 2-9 drain TMEM with tcgen05.ld
+// (two warps per lane quarter, alternate 32-column chunks) and run the top-8
+// epilogue, skipping scores that lie below the row's margin under the
+// running best, while the next tile accumulates. Work units are
 // (a*z+o, 128-row tile, alpha group); units that run concurrently share
 // their A tile and stream the same alphas, so both stay in L2. Every
 // mbarrier wait is bounded; on timeout the kernel records an error word,
@@ -73,7 +75,8 @@ constexpr int MAX_GROUPS = 8;
 constexpr unsigned kNoneU = 0xffffffffu;
 constexpr int A_STAGE_BYTES = BM * BK * 2;   // 16 KB
 constexpr int B_STAGE_BYTES = BN * BK * 2;   // 32 KB
-constexpr int GEMM_THREADS = 192;
+constexpr int EPI_WARPS = 8;          // two per TMEM lane quarter
+constexpr int GEMM_THREADS = 64 + 32 * EPI_WARPS;
 constexpr size_t GEMM_SMEM = (size_t)STAGES * (A_STAGE_BYTES + B_STAGE_BYTES) + 1024 + 256;
 constexpr long long kWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
 
@@ -271,10 +274,46 @@ struct Top8 {
     }
 };
 
+// Branch-free helpers over one 32-column chunk of a row's scores.
+__device__ __forceinline__ float chunk_max(const float (&v)[32]) {
+    float t[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) t[k] = fmaxf(v[2 * k], v[2 * k + 1]);
+#pragma unroll
+    for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+        for (int k = 0; k < w; k++) t[k] = fmaxf(t[2 * k], t[2 * k + 1]);
+    return t[0];
+}
+__device__ __forceinline__ unsigned chunk_mask(const float (&v)[32], float lim) {
+    unsigned t[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++)
+        t[k] = (v[2 * k] >= lim ? 1u << (2 * k) : 0u) | (v[2 * k + 1] >= lim ? 1u << (2 * k + 1) : 0u);
+#pragma unroll
+    for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+        for (int k = 0; k < w; k++) t[k] = t[2 * k] | t[2 * k + 1];
+    return t[0];
+}
+// v[c] for a run-time c without indexing the register array.
+__device__ __forceinline__ float chunk_select(const float (&v)[32], unsigned c) {
+    float t[16];
+#pragma unroll
+    for (int k = 0; k < 16; k++) t[k] = (c & 1u) ? v[2 * k + 1] : v[2 * k];
+    unsigned bit = 2u;
+#pragma unroll
+    for (int w = 8; w > 0; w >>= 1, bit <<= 1)
+#pragma unroll
+        for (int k = 0; k < w; k++) t[k] = (c & bit) ? t[2 * k + 1] : t[2 * k];
+    return t[0];
+}
+
 __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
         const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, uint32_t idesc,
         unsigned MZ, unsigned rPad, unsigned r, unsigned mTiles, unsigned nTiles, unsigned groups, unsigned nU,
-        unsigned kBlocks, float *__restrict__ candV, unsigned *__restrict__ candU, float *__restrict__ candX) {
+        unsigned kBlocks, const float *__restrict__ a1, const unsigned *__restrict__ scal,
+        float *__restrict__ candV, unsigned *__restrict__ candU, float *__restrict__ candX) {
     extern __shared__ uint8_t smemRaw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~(uintptr_t)1023);
     uint8_t *sA = smem;
@@ -289,7 +328,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
         }
         for (int a = 0; a < 2; a++) {
             mbar_init(smem_u32(&bar->accFull[a]), 1);
-            mbar_init(smem_u32(&bar->accEmpty[a]), 4);
+            mbar_init(smem_u32(&bar->accEmpty[a]), EPI_WARPS);
         }
         bar->abortFlag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -358,27 +397,63 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
         }
     } else {
         // ---- epilogue: TMEM -> registers -> running top-8 per row ----
+        // Eight warps: warps w and w+4 read the same TMEM lane quarter
+        // (w & 3), one row per thread, and take alternate 32-column chunks
+        // of every tile, each keeping its own list for the unit (list
+        // 2g + half of the row).
+        // A score below (running best - thr), thr being the row's margin as
+        // the merge computes it, lies below the merge's cut for every later
+        // best (the cut is fl(final best - thr) and rounding is monotonic):
+        // it can be neither a candidate nor the dropped score that sends the
+        // row to the exact scan, so it is skipped without touching the list.
+        // A chunk whose maximum is below the limit costs a few branch-free
+        // instructions; otherwise only its scores at or above the limit go
+        // through the list, one set bit of the chunk's mask at a time.
         const unsigned quarter = warp & 3u;   // TMEM lanes this warp may access
+        const unsigned half = (warp - 2u) >> 2;
         const unsigned rowInTile = quarter * 32u + lane;
+        const float escale = __uint_as_float(scal[2]);
+        const float qnan = __uint_as_float(0x7fc00000u);
         unsigned acc = 0, accPhase = 0;
         Top8 top;
         for (unsigned unit = blockIdx.x; unit < totalUnits && !*abortFlag; unit += gridDim.x) {
             unsigned ao, mt, g, nt0, nt1;
             decode_unit(unit, groups, mTiles, nTiles, ao, mt, g, nt0, nt1);
             top.reset();
+            const unsigned iRow = mt * BM + rowInTile;
+            // Same expression as the merge's margin. An infinite margin skips
+            // nothing; a NaN one skips everything, and the merge sends such
+            // rows to the exact scan whatever their lists hold.
+            const float thr = iRow < r ? 2.0f * a1[(size_t)ao * rPad + iRow] * escale : INFINITY;
+            float lim = -INFINITY;
             bool ok = true;
             for (unsigned nt = nt0; nt < nt1; nt++) {
                 if (!mbar_wait(smem_u32(&bar->accFull[acc]), accPhase, abortFlag)) { ok = false; break; }
                 tc_fence_after();
                 const uint32_t base = tmem + ((quarter * 32u) << 16) + acc * BN;
 #pragma unroll 1
-                for (unsigned ch = 0; ch < BN / 32; ch++) {
+                for (unsigned ch = half; ch < BN / 32; ch += 2) {
+                    __syncwarp();
                     float v[32];
                     tmem_ld32(base + ch * 32u, v);
                     const unsigned u0 = nt * BN + ch * 32u;
+                    if (u0 + 32u > nU) {   // columns past the unique alphas are skipped (NaN)
 #pragma unroll
-                    for (int c = 0; c < 32; c++)
-                        if (u0 + c < nU) top.push(v[c], u0 + c);
+                        for (int c = 0; c < 32; c++)
+                            if (u0 + c >= nU) v[c] = qnan;
+                    }
+                    if (chunk_max(v) >= lim) {
+                        unsigned mask = chunk_mask(v, lim);
+                        while (mask) {
+                            const unsigned c = __ffs(mask) - 1;
+                            mask &= mask - 1;
+                            const float x = chunk_select(v, c);
+                            if (x >= lim) {
+                                top.push(x, u0 + c);
+                                lim = top.v[0] - thr;
+                            }
+                        }
+                    }
                 }
                 tc_fence_before();
                 __syncwarp();
@@ -387,9 +462,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
                 if (acc == 0) accPhase ^= 1u;
             }
             if (!ok) break;
-            const unsigned i = mt * BM + rowInTile;
-            if (i < r) {
-                const size_t slot = ((size_t)ao * r + i) * MAX_GROUPS + g;
+            if (iRow < r) {
+                const size_t slot = ((size_t)ao * r + iRow) * MAX_GROUPS + 2u * g + half;
                 float *cv = candV + slot * TOPK;
                 unsigned *cu = candU + slot * TOPK;
 #pragma unroll
@@ -936,20 +1010,22 @@ int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, 
     // ---- GEMM ----
     CUtensorMap tmB;
     if ((rc = encode_map(tc, &tmB, tc->Gb, nPadRows, tc->nPad, BN, fn)) != NOVA_SUCCESS) return rc;
-    const unsigned groups = std::min<unsigned>(MAX_GROUPS, nTiles);
+    // Each alpha group leaves two lists per row (one per epilogue half).
+    const unsigned groups = std::min<unsigned>(MAX_GROUPS / 2, nTiles);
+    const unsigned lists = 2u * groups;
     const unsigned totalUnits = tc->MZ * tc->mTiles * groups;
     const unsigned grid = std::min<unsigned>(totalUnits, (unsigned)tc->numSMs);
     cudaEventRecord(tc->g0, eng.stream);
     tc_score_gemm_kernel<<<grid, GEMM_THREADS, GEMM_SMEM, eng.stream>>>(
         tc->tmA, tmB, make_idesc(fp16 ? 0u : 1u), tc->MZ, (unsigned)tc->rPad, md.r, tc->mTiles, nTiles, groups, nU,
-        (unsigned)(tc->nPad / BK), tc->candV, tc->candU, tc->candX);
+        (unsigned)(tc->nPad / BK), tc->a1, tc->scal, tc->candV, tc->candU, tc->candX);
     if ((rc = check_launch(fn, "tensor-core scoring")) != NOVA_SUCCESS) return rc;
     cudaEventRecord(tc->g1, eng.stream);
     // ---- merge, margin, exact re-score of near ties ----
     const size_t rows = (size_t)tc->MZ * md.r;
     cudaMemsetAsync(tc->rowFlag, 0, rows * sizeof(unsigned), eng.stream);
     tc_merge_kernel<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, eng.stream>>>(
-        md, eng.suppLen, eng.Proj, eng.projCols, eng.uniqJ, groups, tc->rPad, tc->a1, tc->a1raw, tc->scal, tc->candV,
+        md, eng.suppLen, eng.Proj, eng.projCols, eng.uniqJ, lists, tc->rPad, tc->a1, tc->a1raw, tc->scal, tc->candV,
         tc->candU,
         tc->candX, eng.ustar, eng.jstar, tc->rowFlag, tc->scal + 3, tc->badModel);
     if ((rc = check_launch(fn, "candidate merge")) != NOVA_SUCCESS) return rc;
