@@ -50,6 +50,7 @@ typedef struct NovaPBVIStats {
     float msDedup, msProject, msScore, msRescore, msActions, msAssemble, msTotal;
     float msGemm;                  /* the tensor-core scoring kernel alone (0 if not run) */
     unsigned int launches;         /* kernels this library launched for the update */
+    unsigned int tcGroups;         /* alpha groups of the tensor-core launch (0 if not run) */
 } NovaPBVIStats;
 
 NOVA_API int pomdp_pbvi_get_stats_gpu(const POMDPPBVIGPU *pbvi, NovaPBVIStats *stats);

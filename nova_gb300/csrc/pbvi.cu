@@ -970,6 +970,7 @@ int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsi
     cudaEventElapsedTime(&stats.msAssemble, ev[6], ev[4]);
     cudaEventElapsedTime(&stats.msTotal, ev[0], ev[4]);
     stats.launches = (unsigned)(launch_count() - launches0);
+    if (stats.tcGroups != 0) tc_tune_feedback(*this, stats.msScore + stats.msRescore, nU);
     const unsigned derr = tc_device_error();
     if (derr != 0) {
         NOVA_ERR(fn, "A device-side wait timed out; results of this update are invalid.");

@@ -108,6 +108,9 @@ int tc_build(BackupEngine &eng, const char *fn);
 int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, const unsigned **rowList,
              const char *fn);
 void tc_release(TcState *tc);
+// Feeds one tensor-core update's scoring time (GEMM, merge and the exact
+// scan it left) to the solver's alpha-group tuner.
+void tc_tune_feedback(BackupEngine &eng, float msScoring, unsigned nU);
 unsigned tc_device_error();
 
 }  // namespace nova_gb300

@@ -101,7 +101,23 @@ struct TcState {
     CUtensorMap tmA;
     cudaEvent_t g0 = nullptr, g1 = nullptr;
     int numSMs = 0;
+    // Alpha-group schedule. Fewer groups mean longer runs per list (fewer
+    // insertions in the epilogue) but fewer candidate lists per row (more
+    // rows left to the exact scan); the best count depends on the shape, so
+    // each solver times kGroupChoices on its first tensor-core updates
+    // (scoring plus the exact scan it leaves, per unique alpha) and keeps the
+    // fastest. Results are identical for every choice.
+    unsigned groupsFixed = 0;       // chosen count, 0 while tuning
+    unsigned tuneNext = 0;          // next trial
+    bool tuneWarm = false;          // the first tensor-core update (lazy set-up) is not timed
+    unsigned groupsUsed = 0;        // groups of the last launch
+    float tuneCost[3] = {0, 0, 0};
 };
+
+constexpr unsigned kGroupChoices[3] = {4u, 2u, 1u};
+// Deep contractions keep the epilogue hidden behind the MMAs; they use the
+// most lists (best resolution) without tuning.
+constexpr size_t kTuneMaxNPad = 2048;
 
 void tc_release(TcState *tc) {
     if (!tc) return;
@@ -407,8 +423,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
         // it can be neither a candidate nor the dropped score that sends the
         // row to the exact scan, so it is skipped without touching the list.
         // A chunk whose maximum is below the limit costs a few branch-free
-        // instructions; otherwise only its scores at or above the limit go
-        // through the list, one set bit of the chunk's mask at a time.
+        // instructions; otherwise the limit is raised to the chunk's maximum
+        // minus thr and only the chunk's scores at or above it go through
+        // the list, one set bit of the chunk's mask at a time.
         const unsigned quarter = warp & 3u;   // TMEM lanes this warp may access
         const unsigned half = (warp - 2u) >> 2;
         const unsigned rowInTile = quarter * 32u + lane;
@@ -425,7 +442,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
             // nothing; a NaN one skips everything, and the merge sends such
             // rows to the exact scan whatever their lists hold.
             const float thr = iRow < r ? 2.0f * a1[(size_t)ao * rPad + iRow] * escale : INFINITY;
-            float lim = -INFINITY;
+            float best = -INFINITY, lim = -INFINITY;
             bool ok = true;
             for (unsigned nt = nt0; nt < nt1; nt++) {
                 if (!mbar_wait(smem_u32(&bar->accFull[acc]), accPhase, abortFlag)) { ok = false; break; }
@@ -442,16 +459,18 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
                         for (int c = 0; c < 32; c++)
                             if (u0 + c >= nU) v[c] = qnan;
                     }
-                    if (chunk_max(v) >= lim) {
+                    const float mx = chunk_max(v);
+                    if (mx >= lim) {
+                        // The chunk's maximum raises the running best first,
+                        // so only its scores within thr of the new best are
+                        // listed (the list's first entry is that best).
+                        best = fmaxf(best, mx);
+                        lim = best - thr;
                         unsigned mask = chunk_mask(v, lim);
                         while (mask) {
                             const unsigned c = __ffs(mask) - 1;
                             mask &= mask - 1;
-                            const float x = chunk_select(v, c);
-                            if (x >= lim) {
-                                top.push(x, u0 + c);
-                                lim = top.v[0] - thr;
-                            }
+                            top.push(chunk_select(v, c), u0 + c);
                         }
                     }
                 }
@@ -1011,8 +1030,11 @@ int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, 
     CUtensorMap tmB;
     if ((rc = encode_map(tc, &tmB, tc->Gb, nPadRows, tc->nPad, BN, fn)) != NOVA_SUCCESS) return rc;
     // Each alpha group leaves two lists per row (one per epilogue half).
-    const unsigned groups = std::min<unsigned>(MAX_GROUPS / 2, nTiles);
+    if (tc->groupsFixed == 0 && tc->nPad > kTuneMaxNPad) tc->groupsFixed = kGroupChoices[0];
+    const unsigned want = tc->groupsFixed ? tc->groupsFixed : kGroupChoices[tc->tuneWarm ? tc->tuneNext : 0];
+    const unsigned groups = std::max(1u, std::min<unsigned>(want, nTiles));
     const unsigned lists = 2u * groups;
+    tc->groupsUsed = groups;
     const unsigned totalUnits = tc->MZ * tc->mTiles * groups;
     const unsigned grid = std::min<unsigned>(totalUnits, (unsigned)tc->numSMs);
     cudaEventRecord(tc->g0, eng.stream);
@@ -1059,7 +1081,23 @@ int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, 
     eng.stats.rowsMultiCand = h[3];
     eng.stats.candidates = h[4];
     cudaEventElapsedTime(&eng.stats.msGemm, tc->g0, tc->g1);
+    eng.stats.tcGroups = tc->groupsUsed;
     return NOVA_SUCCESS;
+}
+
+void tc_tune_feedback(BackupEngine &eng, float msScoring, unsigned nU) {
+    TcState *tc = eng.tc;
+    if (tc == nullptr || tc->groupsFixed != 0 || nU == 0) return;
+    if (!tc->tuneWarm) {
+        tc->tuneWarm = true;
+        return;
+    }
+    tc->tuneCost[tc->tuneNext] = msScoring / (float)nU;
+    if (++tc->tuneNext < 3) return;
+    unsigned best = 0;
+    for (unsigned k = 1; k < 3; k++)
+        if (tc->tuneCost[k] < tc->tuneCost[best]) best = k;
+    tc->groupsFixed = kGroupChoices[best];
 }
 
 }  // namespace nova_gb300

@@ -48,6 +48,7 @@ class NovaPBVIStats(ct.Structure):
                 ("msTotal", ct.c_float),
                 ("msGemm", ct.c_float),
                 ("launches", ct.c_uint),
+                ("tcGroups", ct.c_uint),
                 ]
 
 
