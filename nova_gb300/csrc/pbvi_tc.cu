@@ -70,8 +70,9 @@ constexpr int BM = 128;            // rows (beliefs) per tile
 constexpr int BN = 256;            // alphas per tile
 constexpr int BK = 64;             // K (states) per stage: 128 bytes of BF16
 constexpr int STAGES = 4;
-constexpr int TOPK = 8;
-constexpr int MAX_GROUPS = 8;
+constexpr int MAX_TOPK = 16;       // entries per candidate list (layout capacity)
+constexpr int MAX_LISTS = 8;       // candidate lists per row: two per alpha group
+constexpr int MAX_ENTRIES = MAX_LISTS * MAX_TOPK;
 constexpr unsigned kNoneU = 0xffffffffu;
 constexpr int A_STAGE_BYTES = BM * BK * 2;   // 16 KB
 constexpr int B_STAGE_BYTES = BN * BK * 2;   // 32 KB
@@ -90,9 +91,9 @@ struct TcState {
     uint16_t *Gb = nullptr;         // [capN][nPad] BF16 or FP16 bits of (alpha - c) * 2^gexp
     float *shift = nullptr;         // [n]
     unsigned *scal = nullptr;       // [0] gmax, [1] Gmax, [2] escale, [3..4] counters, [5] max half-range, [6] G scale (float bits)
-    float *candV = nullptr;         // [MZ][r][MAX_GROUPS][TOPK]
+    float *candV = nullptr;         // [MZ][r][MAX_LISTS][MAX_TOPK] (the first K entries of each list used)
     unsigned *candU = nullptr;
-    float *candX = nullptr;         // [MZ][r][MAX_GROUPS]
+    float *candX = nullptr;         // [MZ][r][MAX_LISTS]
     unsigned *rowFlag = nullptr;    // [MZ*r] rows needing the exact scan
     unsigned *rowList = nullptr;    // [MZ*r] their indices, compacted
     unsigned *chunkCount = nullptr; // [ceil(MZ*r / 4096)] flagged rows per chunk, then chunk offsets
@@ -101,20 +102,24 @@ struct TcState {
     CUtensorMap tmA;
     cudaEvent_t g0 = nullptr, g1 = nullptr;
     int numSMs = 0;
-    // Alpha-group schedule. Fewer groups mean longer runs per list (fewer
-    // insertions in the epilogue) but fewer candidate lists per row (more
-    // rows left to the exact scan); the best count depends on the shape, so
-    // each solver times kGroupChoices on its first tensor-core updates
-    // (scoring plus the exact scan it leaves, per unique alpha) and keeps the
-    // fastest. Results are identical for every choice.
-    unsigned groupsFixed = 0;       // chosen count, 0 while tuning
+    // Scoring schedule: alpha groups per row tile and entries per candidate
+    // list. Fewer groups and shorter lists make the epilogue cheaper; more
+    // room in the lists leaves fewer rows to the exact scan. The best choice
+    // depends on the shape, so each solver times kSchedules on its first
+    // tensor-core updates (scoring plus the exact scan it leaves, per unique
+    // alpha) and keeps the fastest. Results are identical for every choice.
+    int schedFixed = -1;            // chosen schedule, -1 while tuning
     unsigned tuneNext = 0;          // next trial
     bool tuneWarm = false;          // the first tensor-core update (lazy set-up) is not timed
     unsigned groupsUsed = 0;        // groups of the last launch
     float tuneCost[3] = {0, 0, 0};
 };
 
-constexpr unsigned kGroupChoices[3] = {4u, 2u, 1u};
+// Schedules: alpha groups per row tile and entries per candidate list.
+struct TcSchedule {
+    unsigned groups, topk;
+};
+constexpr TcSchedule kSchedules[3] = {{4u, 16u}, {4u, 8u}, {2u, 8u}};
 // Deep contractions keep the epilogue hidden behind the MMAs; they use the
 // most lists (best resolution) without tuning.
 constexpr size_t kTuneMaxNPad = 2048;
@@ -261,26 +266,27 @@ __device__ __forceinline__ void decode_unit(unsigned unit, unsigned groups, unsi
     nt1 = (unsigned)((unsigned long long)(g + 1) * nTiles / groups);
 }
 
-// Sorted top-8 of (score, alpha) in registers; `excl` is the best score
+// Sorted top-K of (score, alpha) in registers; `excl` is the best score
 // that fell off (or never entered) the list.
-struct Top8 {
-    float v[TOPK];
-    unsigned u[TOPK];
+template <int K>
+struct TopList {
+    float v[K];
+    unsigned u[K];
     float excl;
     __device__ __forceinline__ void reset() {
 #pragma unroll
-        for (int k = 0; k < TOPK; k++) { v[k] = -INFINITY; u[k] = kNoneU; }
+        for (int k = 0; k < K; k++) { v[k] = -INFINITY; u[k] = kNoneU; }
         excl = -INFINITY;
     }
     __device__ __forceinline__ void push(float x, unsigned idx) {
-        if (!(x > v[TOPK - 1])) {   // also drops NaN
+        if (!(x > v[K - 1])) {   // also drops NaN
             excl = fmaxf(excl, x);
             return;
         }
-        excl = fmaxf(excl, v[TOPK - 1]);
+        excl = fmaxf(excl, v[K - 1]);
         // insertion from the bottom; equal scores keep the earlier (lower) index first
 #pragma unroll
-        for (int k = TOPK - 1; k > 0; k--) {
+        for (int k = K - 1; k > 0; k--) {
             const bool shift = x > v[k - 1];
             const bool place = !shift && x > v[k];
             if (shift) { v[k] = v[k - 1]; u[k] = u[k - 1]; }
@@ -325,6 +331,7 @@ __device__ __forceinline__ float chunk_select(const float (&v)[32], unsigned c) 
     return t[0];
 }
 
+template <int K>
 __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
         const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, uint32_t idesc,
         unsigned MZ, unsigned rPad, unsigned r, unsigned mTiles, unsigned nTiles, unsigned groups, unsigned nU,
@@ -432,7 +439,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
         const float escale = __uint_as_float(scal[2]);
         const float qnan = __uint_as_float(0x7fc00000u);
         unsigned acc = 0, accPhase = 0;
-        Top8 top;
+        TopList<K> top;
         for (unsigned unit = blockIdx.x; unit < totalUnits && !*abortFlag; unit += gridDim.x) {
             unsigned ao, mt, g, nt0, nt1;
             decode_unit(unit, groups, mTiles, nTiles, ao, mt, g, nt0, nt1);
@@ -482,11 +489,11 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
             }
             if (!ok) break;
             if (iRow < r) {
-                const size_t slot = ((size_t)ao * r + iRow) * MAX_GROUPS + 2u * g + half;
-                float *cv = candV + slot * TOPK;
-                unsigned *cu = candU + slot * TOPK;
+                const size_t slot = ((size_t)ao * r + iRow) * MAX_LISTS + 2u * g + half;
+                float *cv = candV + slot * MAX_TOPK;
+                unsigned *cu = candU + slot * MAX_TOPK;
 #pragma unroll
-                for (int k = 0; k < TOPK; k++) { cv[k] = top.v[k]; cu[k] = top.u[k]; }
+                for (int k = 0; k < K; k++) { cv[k] = top.v[k]; cu[k] = top.u[k]; }
                 candX[slot] = top.excl;
             }
         }
@@ -702,11 +709,13 @@ __device__ __forceinline__ float proj_row_score(const float *__restrict__ P, siz
 
 // One warp per row; returns (in every lane) the number of candidates it
 // re-scored exactly, 0 when the row was settled without re-scoring or sent to
-// the exact scan.
+// the exact scan. The row's lists hold K entries each; entry e of the warp's
+// view is entry e / nLists of list e % nLists, so the lists' leading entries
+// (where the candidates are) spread over the lanes.
 __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevModel md,
                                               const unsigned *__restrict__ suppLen, const float *__restrict__ Proj,
-                                              size_t uCols, const unsigned *__restrict__ uniqJ, unsigned groups,
-                                              size_t rPad, const float *__restrict__ a1,
+                                              size_t uCols, const unsigned *__restrict__ uniqJ, unsigned nLists,
+                                              unsigned K, size_t rPad, const float *__restrict__ a1,
                                               const float *__restrict__ a1raw, const unsigned *__restrict__ scal,
                                               const float *__restrict__ candV, const unsigned *__restrict__ candU,
                                               const float *__restrict__ candX, unsigned *__restrict__ ustar,
@@ -714,14 +723,24 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
                                               const unsigned *__restrict__ badModel) {
     const unsigned ao = (unsigned)(row / md.r), i = (unsigned)(row % md.r);
     const unsigned a = ao / md.z, o = ao % md.z;
-    const size_t base = row * MAX_GROUPS * TOPK;
-    const unsigned nEnt = groups * TOPK;     // <= 64: each lane holds entries lane and lane + 32
-    float v0 = -INFINITY, v1 = -INFINITY;
-    unsigned u0 = kNoneU, u1 = kNoneU;
-    if (lane < nEnt) { u0 = candU[base + lane]; v0 = u0 == kNoneU ? -INFINITY : candV[base + lane]; }
-    if (lane + 32 < nEnt) { u1 = candU[base + lane + 32]; v1 = u1 == kNoneU ? -INFINITY : candV[base + lane + 32]; }
-    float x = lane < groups ? candX[row * MAX_GROUPS + lane] : -INFINITY;
-    float tmax = fmaxf(v0, v1);
+    const size_t base = row * MAX_ENTRIES;
+    const unsigned nEnt = nLists * K;     // <= 128: each lane holds entries lane + 32 j, j < 4
+    float v[4];
+    unsigned u[4];
+    float tmax = -INFINITY;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const unsigned e = lane + 32u * j;
+        v[j] = -INFINITY;
+        u[j] = kNoneU;
+        if (e < nEnt) {
+            const size_t idx = base + (size_t)(e % nLists) * MAX_TOPK + e / nLists;
+            u[j] = candU[idx];
+            if (u[j] != kNoneU) v[j] = candV[idx];
+        }
+        tmax = fmaxf(tmax, v[j]);
+    }
+    float x = lane < nLists ? candX[row * MAX_LISTS + lane] : -INFINITY;
     for (int off = 16; off > 0; off >>= 1) {
         tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, off));
         x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, off));
@@ -738,14 +757,23 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
         if (lane == 0) rowFlag[row] = 1u;
         return 0u;
     }
-    const bool c0 = u0 != kNoneU && v0 >= cut;
-    const bool c1 = u1 != kNoneU && v1 >= cut;
-    const unsigned m0 = __ballot_sync(0xffffffffu, c0), m1 = __ballot_sync(0xffffffffu, c1);
-    const unsigned count = __popc(m0) + __popc(m1);
+    bool c[4];
+    unsigned count = 0, first = kNoneU;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        c[j] = u[j] != kNoneU && v[j] >= cut;
+        const unsigned msk = __ballot_sync(0xffffffffu, c[j]);
+        count += __popc(msk);
+        if (first == kNoneU && msk) first = 32u * j + __ffs(msk) - 1;
+    }
     const size_t js = ((size_t)i * md.m + a) * md.z + o;
     if (count == 1) {
-        const unsigned src = m0 ? __ffs(m0) - 1 : __ffs(m1) - 1;
-        const unsigned uu = m0 ? __shfl_sync(0xffffffffu, u0, src) : __shfl_sync(0xffffffffu, u1, src);
+        const unsigned src = first & 31u, jj = first >> 5;
+        unsigned mine = u[0];
+#pragma unroll
+        for (int j = 1; j < 4; j++)
+            if (jj == (unsigned)j) mine = u[j];
+        const unsigned uu = __shfl_sync(0xffffffffu, mine, src);
         if (lane == 0) { ustar[js] = uu; jstar[js] = uniqJ[uu]; }
         return 0u;
     }
@@ -756,10 +784,12 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
     const float *bk = md.B + (size_t)i * md.rz;
     float best = -INFINITY;
     unsigned bu = kNoneU;
-    if (c0) { best = proj_row_score(P, uCols, u0, bk, sk, Li); bu = u0; }
-    if (c1) {
-        const float w = proj_row_score(P, uCols, u1, bk, sk, Li);
-        if (bu == kNoneU || w > best || (w == best && u1 < bu)) { best = w; bu = u1; }
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        if (c[j]) {
+            const float w = proj_row_score(P, uCols, u[j], bk, sk, Li);
+            if (bu == kNoneU || w > best || (w == best && u[j] < bu)) { best = w; bu = u[j]; }
+        }
     }
     for (int off = 16; off > 0; off >>= 1) {
         const float b2 = __shfl_xor_sync(0xffffffffu, best, off);
@@ -780,8 +810,8 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
 // Rows re-scored and candidates re-scored are counted per block in shared
 // memory, then added to the global counters once per block.
 __global__ void __launch_bounds__(256) tc_merge_kernel(DevModel md, const unsigned *__restrict__ suppLen, const float *__restrict__ Proj,
-                                size_t uCols, const unsigned *__restrict__ uniqJ, unsigned groups, size_t rPad,
-                                const float *__restrict__ a1, const float *__restrict__ a1raw,
+                                size_t uCols, const unsigned *__restrict__ uniqJ, unsigned nLists, unsigned K,
+                                size_t rPad, const float *__restrict__ a1, const float *__restrict__ a1raw,
                                 const unsigned *__restrict__ scal,
                                 const float *__restrict__ candV, const unsigned *__restrict__ candU,
                                 const float *__restrict__ candX, unsigned *__restrict__ ustar,
@@ -795,8 +825,8 @@ __global__ void __launch_bounds__(256) tc_merge_kernel(DevModel md, const unsign
     const size_t rows = (size_t)md.m * md.z * md.r;
     unsigned rescored = 0;
     if (row < rows)
-        rescored = merge_row(row, lane, md, suppLen, Proj, uCols, uniqJ, groups, rPad, a1, a1raw, scal, candV, candU,
-                             candX, ustar, jstar, rowFlag, badModel);
+        rescored = merge_row(row, lane, md, suppLen, Proj, uCols, uniqJ, nLists, K, rPad, a1, a1raw, scal, candV,
+                             candU, candX, ustar, jstar, rowFlag, badModel);
     if (lane == 0 && rescored) {
         atomicAdd(&blockCount[0], 1u);
         atomicAdd(&blockCount[1], rescored);
@@ -943,8 +973,8 @@ int tc_build(BackupEngine &eng, const char *fn) {
     const size_t aElems = (size_t)tc->MZ * tc->rPad * tc->nPad;
     size_t freeB = 0, totalB = 0;
     cudaMemGetInfo(&freeB, &totalB);
-    const size_t slots = (size_t)tc->MZ * md.r * MAX_GROUPS;
-    const size_t need = aElems * 2 + tc->capN * tc->nPad * 2 + slots * (TOPK * 8 + 4) + (size_t)tc->MZ * md.r * 4;
+    const size_t slots = (size_t)tc->MZ * md.r * MAX_LISTS;
+    const size_t need = aElems * 2 + tc->capN * tc->nPad * 2 + slots * (MAX_TOPK * 8 + 4) + (size_t)tc->MZ * md.r * 4;
     if (need + (256ull << 20) > freeB) {
         NOVA_ERR(fn, "Not enough device memory for the tensor-core operands; using exact scoring.");
         return NOVA_ERROR_DEVICE_MALLOC;
@@ -965,8 +995,8 @@ int tc_build(BackupEngine &eng, const char *fn) {
     if ((rc = dev_alloc(&tc->Gb, tc->capN * tc->nPad, fn, "the packed alphas")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->shift, md.n, fn, "the alpha shift")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->scal, 8, fn, "the scoring scalars")) != NOVA_SUCCESS) return rc;
-    if ((rc = dev_alloc(&tc->candV, slots * TOPK, fn, "the candidate scores")) != NOVA_SUCCESS) return rc;
-    if ((rc = dev_alloc(&tc->candU, slots * TOPK, fn, "the candidate alphas")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->candV, slots * MAX_TOPK, fn, "the candidate scores")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->candU, slots * MAX_TOPK, fn, "the candidate alphas")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->candX, slots, fn, "the dropped-score bounds")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->rowFlag, (size_t)tc->MZ * md.r, fn, "the exact-scan flags")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->rowList, (size_t)tc->MZ * md.r, fn, "the exact-scan rows")) != NOVA_SUCCESS) return rc;
@@ -980,7 +1010,9 @@ int tc_build(BackupEngine &eng, const char *fn) {
     tc->numSMs = prop.multiProcessorCount;
     cudaEventCreate(&tc->g0);
     cudaEventCreate(&tc->g1);
-    if (cudaFuncSetAttribute(tc_score_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM) !=
+    if (cudaFuncSetAttribute(tc_score_gemm_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(tc_score_gemm_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM) !=
             cudaSuccess) {
         cudaGetLastError();
         NOVA_ERR(fn, "Failed to configure the scoring kernel's shared memory.");
@@ -1030,15 +1062,16 @@ int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, 
     CUtensorMap tmB;
     if ((rc = encode_map(tc, &tmB, tc->Gb, nPadRows, tc->nPad, BN, fn)) != NOVA_SUCCESS) return rc;
     // Each alpha group leaves two lists per row (one per epilogue half).
-    if (tc->groupsFixed == 0 && tc->nPad > kTuneMaxNPad) tc->groupsFixed = kGroupChoices[0];
-    const unsigned want = tc->groupsFixed ? tc->groupsFixed : kGroupChoices[tc->tuneWarm ? tc->tuneNext : 0];
-    const unsigned groups = std::max(1u, std::min<unsigned>(want, nTiles));
+    if (tc->schedFixed < 0 && tc->nPad > kTuneMaxNPad) tc->schedFixed = 0;
+    const TcSchedule sched = kSchedules[tc->schedFixed >= 0 ? tc->schedFixed : (tc->tuneWarm ? (int)tc->tuneNext : 0)];
+    const unsigned groups = std::max(1u, std::min<unsigned>(sched.groups, nTiles));
     const unsigned lists = 2u * groups;
     tc->groupsUsed = groups;
     const unsigned totalUnits = tc->MZ * tc->mTiles * groups;
     const unsigned grid = std::min<unsigned>(totalUnits, (unsigned)tc->numSMs);
     cudaEventRecord(tc->g0, eng.stream);
-    tc_score_gemm_kernel<<<grid, GEMM_THREADS, GEMM_SMEM, eng.stream>>>(
+    auto gemm = sched.topk == 16u ? tc_score_gemm_kernel<16> : tc_score_gemm_kernel<8>;
+    gemm<<<grid, GEMM_THREADS, GEMM_SMEM, eng.stream>>>(
         tc->tmA, tmB, make_idesc(fp16 ? 0u : 1u), tc->MZ, (unsigned)tc->rPad, md.r, tc->mTiles, nTiles, groups, nU,
         (unsigned)(tc->nPad / BK), tc->a1, tc->scal, tc->candV, tc->candU, tc->candX);
     if ((rc = check_launch(fn, "tensor-core scoring")) != NOVA_SUCCESS) return rc;
@@ -1047,7 +1080,7 @@ int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, 
     const size_t rows = (size_t)tc->MZ * md.r;
     cudaMemsetAsync(tc->rowFlag, 0, rows * sizeof(unsigned), eng.stream);
     tc_merge_kernel<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, eng.stream>>>(
-        md, eng.suppLen, eng.Proj, eng.projCols, eng.uniqJ, lists, tc->rPad, tc->a1, tc->a1raw, tc->scal, tc->candV,
+        md, eng.suppLen, eng.Proj, eng.projCols, eng.uniqJ, lists, sched.topk, tc->rPad, tc->a1, tc->a1raw, tc->scal, tc->candV,
         tc->candU,
         tc->candX, eng.ustar, eng.jstar, tc->rowFlag, tc->scal + 3, tc->badModel);
     if ((rc = check_launch(fn, "candidate merge")) != NOVA_SUCCESS) return rc;
@@ -1087,7 +1120,7 @@ int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, 
 
 void tc_tune_feedback(BackupEngine &eng, float msScoring, unsigned nU) {
     TcState *tc = eng.tc;
-    if (tc == nullptr || tc->groupsFixed != 0 || nU == 0) return;
+    if (tc == nullptr || tc->schedFixed >= 0 || nU == 0) return;
     if (!tc->tuneWarm) {
         tc->tuneWarm = true;
         return;
@@ -1097,7 +1130,7 @@ void tc_tune_feedback(BackupEngine &eng, float msScoring, unsigned nU) {
     unsigned best = 0;
     for (unsigned k = 1; k < 3; k++)
         if (tc->tuneCost[k] < tc->tuneCost[best]) best = k;
-    tc->groupsFixed = kGroupChoices[best];
+    tc->schedFixed = (int)best;
 }
 
 }  // namespace nova_gb300
