@@ -646,16 +646,16 @@ def main():
         flops = [2.0 * r * u * n_pad * cfg["m"] * cfg["z"] for u, _ in gemm]
         achieved = sum(flops) / (sum(t for _, t in gemm) * 1e-3) / 1e12
         # DRAM traffic per launch: the ncu capture of the n=4096 small case
-        # (profiles/tc_score_gemm_n4096_small.md: 540.1 MB read + 20.2 MB
-        # written over 2048 work units) scaled by this launch's work units
+        # (profiles/tc_score_gemm_n4096_small.md: 593.8 MB read + 33.1 MB
+        # written over 1024 work units) scaled by this launch's work units
         # (m*z pairs x 128-row tiles x alpha groups); traffic grows with the
         # units, since each unit streams one A tile and writes one candidate set.
-        u_last = gemm[-1][0]
-        units = cfg["m"] * cfg["z"] * ((r + 127) // 128) * min(8, (u_last + 255) // 256)
-        traffic = (540.1e6 + 20.2e6) / 2048.0 * units
+        groups = [s["tcGroups"] for s in stats if s["msGemm"] > 0][-1]
+        units = cfg["m"] * cfg["z"] * ((r + 127) // 128) * max(1, groups)
+        traffic = (593.8e6 + 33.1e6) / 1024.0 * units
         roofline = {"bound": "tensor", "achieved": achieved, "peak": tc_peak, "unit": "TFLOP/s",
                     "frac": achieved / tc_peak, "traffic": traffic,
-                    "traffic_note": "bytes per launch, scaled from an ncu capture of a 2048-unit launch to %d units"
+                    "traffic_note": "bytes per launch, scaled from an ncu capture of a 1024-unit launch to %d units"
                                     % units,
                     "kernel": "tcgen05 FP16 scoring GEMM (kind::f16, FP32 accumulate in TMEM) with fused top-8 epilogue",
                     "flops_per_launch": flops[-1], "peak_source": peak_kind}
