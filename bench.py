@@ -657,7 +657,7 @@ def main():
                     "frac": achieved / tc_peak, "traffic": traffic,
                     "traffic_note": "bytes per launch, scaled from an ncu capture of a 1024-unit launch to %d units"
                                     % units,
-                    "kernel": "tcgen05 FP16 scoring GEMM (kind::f16, FP32 accumulate in TMEM) with fused top-8 epilogue",
+                    "kernel": "tcgen05 FP16 scoring GEMM (kind::f16, FP32 accumulate in TMEM) with fused candidate-list epilogue",
                     "flops_per_launch": flops[-1], "peak_source": peak_kind}
     else:
         roofline = {"bound": "tensor", "achieved": None, "peak": tc_peak, "unit": "TFLOP/s", "frac": None,
