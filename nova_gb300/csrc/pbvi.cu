@@ -518,6 +518,94 @@ __global__ void __launch_bounds__(256) proj_kernel(DevModel md, const unsigned *
     }
 }
 
+// The same values in the state-contiguous layout [m][z][uRows][sCols]. One
+// block per (a, 8 consecutive states) and column range of the alphas
+// (blockIdx.y): warp w owns state s0 + w and its lanes two alphas of a
+// 64-alpha chunk (coalesced reads of the transposed alphas; the state's
+// coefficients broadcast from shared memory). The chunk's results go through
+// shared memory so that each (o, u) column segment of the 8 states is written
+// as one 32-byte sector. The blocks of one column range run together, so its
+// part of the transposed alphas stays in L2.
+constexpr unsigned kProjTileS = 8;
+constexpr unsigned kStateMajorMinStates = 2048;
+template <int ZC>
+__global__ void __launch_bounds__(256) proj_state_major_kernel(DevModel md, const unsigned *__restrict__ succLen,
+                                                               const float *__restrict__ C1,
+                                                               const float *__restrict__ Gt, size_t gtCols,
+                                                               unsigned nU, float *__restrict__ Proj, size_t uRows,
+                                                               size_t sCols, unsigned uRange) {
+    extern __shared__ float smem[];
+    float *Cs = smem;                                                     // [8][ns][ZC]
+    float *Out = Cs + (size_t)kProjTileS * md.ns * ZC;                    // [ZC][64][9]
+    int *Ss = reinterpret_cast<int *>(Out + (size_t)ZC * 64 * (kProjTileS + 1));  // [8][ns]
+    const unsigned tilesS = (md.n + kProjTileS - 1) / kProjTileS;
+    const unsigned a = blockIdx.x / tilesS, s0 = (blockIdx.x % tilesS) * kProjTileS;
+    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned s = s0 + warp;
+    const bool live = s < md.n;
+    const unsigned L = live ? succLen[(size_t)s * md.m + a] : 0u;
+    const float gamma = md.gamma;
+    for (unsigned e = lane; e < L; e += 32) Ss[warp * md.ns + e] = md.S[((size_t)s * md.m + a) * md.ns + e];
+    for (unsigned o0 = 0; o0 < md.z; o0 += ZC) {
+        __syncthreads();
+        if (live) {
+            const float *crow = C1 + (((size_t)a * md.n + s) * md.ns) * md.z + o0;
+            float *cw = Cs + (size_t)warp * md.ns * ZC;
+            for (unsigned e = lane; e < L * ZC; e += 32) {
+                const unsigned l = e / ZC, q = e % ZC;
+                cw[e] = (o0 + q < md.z) ? crow[(size_t)l * md.z + q] : 0.0f;
+            }
+        }
+        __syncthreads();
+        const unsigned zc = min((unsigned)ZC, md.z - o0);
+        const float *cw = Cs + (size_t)warp * md.ns * ZC;
+        const int *sw = Ss + warp * md.ns;
+        const unsigned uBegin = blockIdx.y * uRange, uEnd = min(nU, uBegin + uRange);
+        for (unsigned u0 = uBegin; u0 < uEnd; u0 += 64) {
+            const unsigned ua = u0 + lane, ub = ua + 32;
+            const bool va = live && ua < uEnd, vb = live && ub < uEnd;
+            float acc0[ZC], acc1[ZC];
+#pragma unroll
+            for (int q = 0; q < ZC; q++) { acc0[q] = 0.0f; acc1[q] = 0.0f; }
+            for (unsigned l = 0; l < L; l++) {
+                const float *grow = Gt + (size_t)sw[l] * gtCols;
+                const float g0 = va ? grow[ua] : 0.0f;
+                const float g1 = vb ? grow[ub] : 0.0f;
+                const float4 *c4 = reinterpret_cast<const float4 *>(cw + l * ZC);
+#pragma unroll
+                for (int q4 = 0; q4 < ZC / 4; q4++) {
+                    const float4 c = c4[q4];
+                    acc0[4 * q4 + 0] = fadd(acc0[4 * q4 + 0], fmul(c.x, g0));
+                    acc1[4 * q4 + 0] = fadd(acc1[4 * q4 + 0], fmul(c.x, g1));
+                    acc0[4 * q4 + 1] = fadd(acc0[4 * q4 + 1], fmul(c.y, g0));
+                    acc1[4 * q4 + 1] = fadd(acc1[4 * q4 + 1], fmul(c.y, g1));
+                    acc0[4 * q4 + 2] = fadd(acc0[4 * q4 + 2], fmul(c.z, g0));
+                    acc1[4 * q4 + 2] = fadd(acc1[4 * q4 + 2], fmul(c.z, g1));
+                    acc0[4 * q4 + 3] = fadd(acc0[4 * q4 + 3], fmul(c.w, g0));
+                    acc1[4 * q4 + 3] = fadd(acc1[4 * q4 + 3], fmul(c.w, g1));
+                }
+            }
+            __syncthreads();  // the previous chunk's columns have been written out
+#pragma unroll
+            for (int q = 0; q < ZC; q++) {
+                Out[((size_t)q * 64 + lane) * (kProjTileS + 1) + warp] = fmul(acc0[q], gamma);
+                Out[((size_t)q * 64 + lane + 32) * (kProjTileS + 1) + warp] = fmul(acc1[q], gamma);
+            }
+            __syncthreads();
+            // 8 threads per (o, u) column segment: s0 .. s0+7.
+            const unsigned ds = threadIdx.x % kProjTileS;
+            const unsigned sOut = s0 + ds;
+            for (unsigned c = threadIdx.x / kProjTileS; c < zc * 64u; c += blockDim.x / kProjTileS) {
+                const unsigned q = c / 64, du = c % 64;
+                const unsigned u = u0 + du;
+                if (u < uEnd && sOut < md.n)
+                    Proj[(((size_t)a * md.z + o0 + q) * uRows + u) * sCols + sOut] =
+                        Out[((size_t)q * 64 + du) * (kProjTileS + 1) + ds];
+            }
+        }
+    }
+}
+
 // Exact scan of whole (a*z+o, belief) rows over the unique alphas using the
 // projection table: value(u) = sum_k fl(Proj[ao][s_k][u] * B[i,k]) in
 // support order (pomdp_pbvi_cpu.cpp:50-83), argmax with the lowest index on
@@ -527,7 +615,7 @@ __global__ void __launch_bounds__(256) proj_kernel(DevModel md, const unsigned *
 // after the first merges with the running best of the earlier ones, which
 // hold lower indices (so ties keep the earlier alpha).
 __global__ void __launch_bounds__(256) scan_rows_kernel(DevModel md, const unsigned *__restrict__ suppLen,
-                                                        const float *__restrict__ Proj, size_t uCols, unsigned u0,
+                                                        const ProjView pv, unsigned u0,
                                                         unsigned u1, const unsigned *__restrict__ rowList,
                                                         unsigned nRows, float *__restrict__ runV,
                                                         unsigned *__restrict__ runU, int first) {
@@ -547,12 +635,12 @@ __global__ void __launch_bounds__(256) scan_rows_kernel(DevModel md, const unsig
             sk[k] = (unsigned)md.Z[(size_t)i * md.rz + k];
         }
         __syncthreads();
-        const float *P = Proj + (size_t)ao * md.n * uCols;
+        const float *P = pv.slab(ao);
         float best = NOVA_FLT_MIN;
         unsigned bu = kNone;
         for (unsigned u = u0 + threadIdx.x; u < u1; u += blockDim.x) {
             float v = 0.0f;
-            for (unsigned k = 0; k < Li; k++) v = fadd(v, fmul(__ldg(P + (size_t)sk[k] * uCols + u), bk[k]));
+            for (unsigned k = 0; k < Li; k++) v = fadd(v, fmul(__ldg(P + pv.at(sk[k], u)), bk[k]));
             if (v > best) { best = v; bu = u; }
         }
         for (int off = 16; off > 0; off >>= 1) {
@@ -613,7 +701,7 @@ __global__ void sentinel_fixup_kernel(DevModel md, const unsigned *__restrict__ 
 // Action values from the projection table (one warp per (belief, action)):
 // alpha_a(s_k) = R(s_k,a) + sum_o Proj[a][o][s_k][u*], value = sum_k alpha * b_k.
 __global__ void action_value_proj_kernel(DevModel md, const unsigned *__restrict__ suppLen,
-                                         const float *__restrict__ Proj, size_t uCols,
+                                         const ProjView pv,
                                          const unsigned *__restrict__ ustar, float *__restrict__ actVal) {
     const unsigned warpGlobal = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const unsigned lane = threadIdx.x & 31;
@@ -630,7 +718,7 @@ __global__ void action_value_proj_kernel(DevModel md, const unsigned *__restrict
             float alpha = md.R[(size_t)s * md.m + a];
             for (unsigned o = 0; o < md.z; o++) {
                 const unsigned u = ustar[(size_t)ia * md.z + o];
-                alpha = fadd(alpha, Proj[(((size_t)a * md.z + o) * md.n + s) * uCols + u]);
+                alpha = fadd(alpha, pv.slab(a * md.z + o)[pv.at(s, u)]);
             }
             p = fmul(alpha, md.B[(size_t)i * md.rz + k]);
         }
@@ -645,7 +733,7 @@ __global__ void action_value_proj_kernel(DevModel md, const unsigned *__restrict
 // (pomdp_pbvi_cpu.cpp:128-145, 88-101) with its additions in observation
 // order. One block per belief; each thread issues a chunk of independent
 // loads before the sequential additions.
-__global__ void __launch_bounds__(256) assemble_proj_kernel(DevModel md, const float *__restrict__ Proj, size_t uCols,
+__global__ void __launch_bounds__(256) assemble_proj_kernel(DevModel md, const ProjView pv,
                                                             const unsigned *__restrict__ ustar,
                                                             const float *__restrict__ actVal, float *__restrict__ dst,
                                                             unsigned *__restrict__ pi) {
@@ -668,20 +756,20 @@ __global__ void __launch_bounds__(256) assemble_proj_kernel(DevModel md, const f
     const unsigned *us = ustar + ((size_t)i * md.m + a) * md.z;
     for (unsigned o = threadIdx.x; o < md.z; o += blockDim.x) ush[o] = us[o];
     __syncthreads();
-    const float *P = Proj + (size_t)a * md.z * md.n * uCols;
-    const size_t oStride = (size_t)md.n * uCols;
+    const float *P = pv.slab(a * md.z);
+    const size_t oStride = pv.slice;
     for (unsigned s = threadIdx.x; s < md.n; s += blockDim.x) {
         float alpha = md.R[(size_t)s * md.m + a];
-        const float *Ps = P + (size_t)s * uCols;
+        const float *Ps = P + s * pv.sStride;
         unsigned o = 0;
         for (; o + 8 <= md.z; o += 8) {
             float v[8];
 #pragma unroll
-            for (int q = 0; q < 8; q++) v[q] = __ldg(Ps + (size_t)(o + q) * oStride + ush[o + q]);
+            for (int q = 0; q < 8; q++) v[q] = __ldg(Ps + (size_t)(o + q) * oStride + ush[o + q] * pv.uStride);
 #pragma unroll
             for (int q = 0; q < 8; q++) alpha = fadd(alpha, v[q]);
         }
-        for (; o < md.z; o++) alpha = fadd(alpha, __ldg(Ps + (size_t)o * oStride + ush[o]));
+        for (; o < md.z; o++) alpha = fadd(alpha, __ldg(Ps + (size_t)o * oStride + ush[o] * pv.uStride));
         dst[(size_t)i * md.n + s] = alpha;
     }
 }
@@ -812,13 +900,15 @@ int BackupEngine::exact_score(const unsigned *itemList, unsigned nItems, unsigne
 bool BackupEngine::ensure_proj(unsigned nU) {
     if (projUnavailable) return false;
     const size_t cols = round_up(std::max(nU, 1u), 32);
-    const size_t need = (size_t)md.m * md.z * md.n * cols;
+    const size_t sCols = round_up(md.n, kProjTileS);
+    projSCols = sCols;
+    const size_t need = (size_t)md.m * md.z * sCols * cols;
     if (need <= projCap) {
         projCols = cols;
         return true;
     }
-    // Capacity for the largest possible alpha set, allocated once.
-    const size_t full = (size_t)md.m * md.z * md.n * round_up(md.r, 32);
+    // Capacity for the largest possible alpha set in either layout, allocated once.
+    const size_t full = (size_t)md.m * md.z * sCols * round_up(md.r, 32);
     size_t freeB = 0, totalB = 0;
     cudaMemGetInfo(&freeB, &totalB);
     cudaFree(Proj);
@@ -836,6 +926,25 @@ bool BackupEngine::ensure_proj(unsigned nU) {
 }
 
 int BackupEngine::project(unsigned nU, const char *fn) {
+    if (projStateMajor) {
+        const unsigned zc = md.z >= 16 ? 32u : 8u;
+        const size_t smem = ((size_t)kProjTileS * md.ns * zc + (size_t)zc * 64 * (kProjTileS + 1)) * sizeof(float) +
+                            (size_t)kProjTileS * md.ns * sizeof(int);
+        // Column ranges of about 32 MB of the transposed alphas (multiples of 64).
+        const unsigned uRange =
+            (unsigned)std::max<size_t>(64, ((32ull << 20) / ((size_t)md.n * sizeof(float))) / 64 * 64);
+        const dim3 blocks(md.m * ceil_div(md.n, kProjTileS), ceil_div(std::max(nU, 1u), uRange));
+        if (zc == 32) {
+            cudaFuncSetAttribute(proj_state_major_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            proj_state_major_kernel<32><<<blocks, 256, smem, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj,
+                                                                       projCols, projSCols, uRange);
+        } else {
+            cudaFuncSetAttribute(proj_state_major_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            proj_state_major_kernel<8><<<blocks, 256, smem, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj,
+                                                                      projCols, projSCols, uRange);
+        }
+        return check_launch(fn, "projection table");
+    }
     const size_t smem32 = (size_t)md.ns * 32 * sizeof(float) + md.ns * sizeof(int);
     const unsigned blocks = md.m * md.n;
     if (md.z >= 16 && smem32 <= 200 * 1024) {
@@ -867,7 +976,7 @@ int BackupEngine::scan_rows(const unsigned *rowList, unsigned nRows, unsigned nU
     const unsigned grid = std::min(nRows, 152u * 16u);
     for (size_t u0 = 0; u0 < std::max(nU, 1u); u0 += chunk) {
         const unsigned u1 = (unsigned)std::min<size_t>(nU, u0 + chunk);
-        scan_rows_kernel<<<grid, 256, 2 * md.rz * sizeof(float), stream>>>(md, suppLen, Proj, projCols, (unsigned)u0,
+        scan_rows_kernel<<<grid, 256, 2 * md.rz * sizeof(float), stream>>>(md, suppLen, proj_view(), (unsigned)u0,
                                                                           u1, rowList, nRows, scanV, scanU,
                                                                           u0 == 0 ? 1 : 0);
         if ((rc = check_launch(fn, "exact row scan")) != NOVA_SUCCESS) return rc;
@@ -897,7 +1006,7 @@ int BackupEngine::assemble(const float *src, float *dst, unsigned *pi, int onlyB
         itemList = items;
     }
     if (useProjNow && onlyBelief < 0)
-        action_value_proj_kernel<<<ceil_div((size_t)nItems * 32, 256), 256, 0, stream>>>(md, suppLen, Proj, projCols,
+        action_value_proj_kernel<<<ceil_div((size_t)nItems * 32, 256), 256, 0, stream>>>(md, suppLen, proj_view(),
                                                                                          ustar, actVal);
     else
         action_value_kernel<<<ceil_div((size_t)nItems * 32, 256), 256, 0, stream>>>(md, succLen, suppLen, C3, src,
@@ -905,7 +1014,7 @@ int BackupEngine::assemble(const float *src, float *dst, unsigned *pi, int onlyB
     if ((rc = check_launch(fn, "action values")) != NOVA_SUCCESS) return rc;
     if (onlyBelief < 0) cudaEventRecord(ev[6], stream);
     if (useProjNow && onlyBelief < 0)
-        assemble_proj_kernel<<<nBeliefs, 256, md.z * sizeof(unsigned), stream>>>(md, Proj, projCols, ustar, actVal,
+        assemble_proj_kernel<<<nBeliefs, 256, md.z * sizeof(unsigned), stream>>>(md, proj_view(), ustar, actVal,
                                                                                   dst, pi);
     else
         assemble_kernel<<<nBeliefs, 256, md.z * sizeof(unsigned), stream>>>(md, succLen, C3, src, jstar, actVal,
@@ -931,9 +1040,20 @@ int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsi
     // with it. Without room, every (belief, action) pair is scored from the
     // alphas directly.
     useProjNow = ensure_proj(nU);
-    if (useProjNow && (rc = project(nU, fn)) != NOVA_SUCCESS) return rc;
     const bool wantTc = (scoring == NOVA_SCORING_BF16 || scoring == NOVA_SCORING_FP16) && useProjNow &&
                         tc_supported(md) && nU >= kTcMinUnique && !tcUnavailable;
+    // Tensor-core updates of large models read the table by candidate and by
+    // chosen alpha (assembly reads whole columns) and leave almost no row to
+    // the exact scan, so they use the state-contiguous layout; the exact scan
+    // reads whole rows and keeps the alpha-contiguous one, as do smaller
+    // models, whose tensor-core updates leave more rows to it.
+    {
+        const unsigned zc = md.z >= 16 ? 32u : 8u;
+        const size_t smemSM = ((size_t)kProjTileS * md.ns * zc + (size_t)zc * 64 * (kProjTileS + 1)) * sizeof(float) +
+                              (size_t)kProjTileS * md.ns * sizeof(int);
+        projStateMajor = wantTc && md.n > kStateMajorMinStates && smemSM <= 200 * 1024;
+    }
+    if (useProjNow && (rc = project(nU, fn)) != NOVA_SUCCESS) return rc;
     if (wantTc && tc == nullptr && tc_build(*this, fn) != NOVA_SUCCESS) tcUnavailable = true;
     cudaEventRecord(ev[2], stream);
     if (wantTc && tc != nullptr) {

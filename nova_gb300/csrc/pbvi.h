@@ -28,6 +28,19 @@ struct DevModel {
 
 struct TcState;  // tensor-core scoring state (pbvi_tc.cu)
 
+// Addressing of the projection table: the value for (a*z+o, s, u) is
+// base[ao * slice + s * sStride + u * uStride]. Two layouts are used:
+// alpha-contiguous rows [m][z][n][uCols] (sStride = uCols, uStride = 1),
+// read row-wise by the exact scan, and state-contiguous columns
+// [m][z][uRows][sCols] (sStride = 1, uStride = sCols), read column-wise by
+// the assembly of the chosen alphas.
+struct ProjView {
+    const float *base;
+    size_t slice, sStride, uStride;
+    __host__ __device__ __forceinline__ const float *slab(unsigned ao) const { return base + (size_t)ao * slice; }
+    __host__ __device__ __forceinline__ size_t at(unsigned s, unsigned u) const { return s * sStride + u * uStride; }
+};
+
 // Exact-order kernel workspace and tables.
 struct BackupEngine {
     DevModel md{};
@@ -45,8 +58,10 @@ struct BackupEngine {
     size_t gtCols = 0;
     unsigned *jstar = nullptr;           // [r][m][z] chosen alpha per (belief, action, observation)
     unsigned *ustar = nullptr;           // [r][m][z] the same choice as a unique-alpha index
-    float *Proj = nullptr;               // [m][z][n][projCols] exact projections of the unique alphas
-    size_t projCap = 0, projCols = 0;
+    float *Proj = nullptr;               // exact projections of the unique alphas (layout: ProjView)
+    size_t projCap = 0, projCols = 0;    // projCols: alpha columns (rows in the state-contiguous layout)
+    bool projStateMajor = false;         // this update's table is state-contiguous
+    size_t projSCols = 0;                // states per column in the state-contiguous layout (n rounded to 8)
     bool projUnavailable = false, useProjNow = false;
     float *scanV = nullptr;              // running best of the chunked row scan
     unsigned *scanU = nullptr;
@@ -84,6 +99,10 @@ struct BackupEngine {
     // Projection table for nU unique alphas (false if it does not fit).
     bool ensure_proj(unsigned nU);
     int project(unsigned nU, const char *fn);
+    ProjView proj_view() const {
+        if (projStateMajor) return ProjView{Proj, projCols * projSCols, 1, projSCols};
+        return ProjView{Proj, (size_t)md.n * projCols, projCols, 1};
+    }
     // Exact scan of (a*z+o)*r + i rows over the projection table (all rows if rowList is null).
     int scan_rows(const unsigned *rowList, unsigned nRows, unsigned nU, const char *fn);
     // Work list of `count` consecutive items starting at `first`.

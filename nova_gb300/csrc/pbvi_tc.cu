@@ -692,18 +692,18 @@ __global__ void tc_escale_kernel(unsigned *scal, float U, float gN) {
 // score(u) = sum_k fl(Proj[s_k][u] * b_k) in support order
 // (pomdp_pbvi_cpu.cpp:50-83). Eight table entries are fetched before their
 // eight ordered additions, so the gathers overlap.
-__device__ __forceinline__ float proj_row_score(const float *__restrict__ P, size_t uCols, unsigned u,
+__device__ __forceinline__ float proj_row_score(const float *__restrict__ P, const ProjView &pv, unsigned u,
                                                 const float *__restrict__ bk, const int *__restrict__ sk, unsigned Li) {
     float v = 0.0f;
     unsigned k = 0;
     for (; k + 8 <= Li; k += 8) {
-        float pv[8];
+        float pq[8];
 #pragma unroll
-        for (int q = 0; q < 8; q++) pv[q] = P[(size_t)sk[k + q] * uCols + u];
+        for (int q = 0; q < 8; q++) pq[q] = P[pv.at((unsigned)sk[k + q], u)];
 #pragma unroll
-        for (int q = 0; q < 8; q++) v = fadd(v, fmul(pv[q], bk[k + q]));
+        for (int q = 0; q < 8; q++) v = fadd(v, fmul(pq[q], bk[k + q]));
     }
-    for (; k < Li; k++) v = fadd(v, fmul(P[(size_t)sk[k] * uCols + u], bk[k]));
+    for (; k < Li; k++) v = fadd(v, fmul(P[pv.at((unsigned)sk[k], u)], bk[k]));
     return v;
 }
 
@@ -713,8 +713,8 @@ __device__ __forceinline__ float proj_row_score(const float *__restrict__ P, siz
 // view is entry e / nLists of list e % nLists, so the lists' leading entries
 // (where the candidates are) spread over the lanes.
 __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevModel md,
-                                              const unsigned *__restrict__ suppLen, const float *__restrict__ Proj,
-                                              size_t uCols, const unsigned *__restrict__ uniqJ, unsigned nLists,
+                                              const unsigned *__restrict__ suppLen, const ProjView pv,
+                                              const unsigned *__restrict__ uniqJ, unsigned nLists,
                                               unsigned K, size_t rPad, const float *__restrict__ a1,
                                               const float *__restrict__ a1raw, const unsigned *__restrict__ scal,
                                               const float *__restrict__ candV, const unsigned *__restrict__ candU,
@@ -778,7 +778,7 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
         return 0u;
     }
     // Several candidates: each lane re-scores its own in the exact order.
-    const float *P = Proj + (size_t)ao * md.n * uCols;
+    const float *P = pv.slab(ao);
     const unsigned Li = suppLen[i];
     const int *sk = md.Z + (size_t)i * md.rz;
     const float *bk = md.B + (size_t)i * md.rz;
@@ -787,7 +787,7 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
 #pragma unroll
     for (int j = 0; j < 4; j++) {
         if (c[j]) {
-            const float w = proj_row_score(P, uCols, u[j], bk, sk, Li);
+            const float w = proj_row_score(P, pv, u[j], bk, sk, Li);
             if (bu == kNoneU || w > best || (w == best && u[j] < bu)) { best = w; bu = u[j]; }
         }
     }
@@ -809,8 +809,8 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
 
 // Rows re-scored and candidates re-scored are counted per block in shared
 // memory, then added to the global counters once per block.
-__global__ void __launch_bounds__(256) tc_merge_kernel(DevModel md, const unsigned *__restrict__ suppLen, const float *__restrict__ Proj,
-                                size_t uCols, const unsigned *__restrict__ uniqJ, unsigned nLists, unsigned K,
+__global__ void __launch_bounds__(256) tc_merge_kernel(DevModel md, const unsigned *__restrict__ suppLen,
+                                const ProjView pv, const unsigned *__restrict__ uniqJ, unsigned nLists, unsigned K,
                                 size_t rPad, const float *__restrict__ a1, const float *__restrict__ a1raw,
                                 const unsigned *__restrict__ scal,
                                 const float *__restrict__ candV, const unsigned *__restrict__ candU,
@@ -825,7 +825,7 @@ __global__ void __launch_bounds__(256) tc_merge_kernel(DevModel md, const unsign
     const size_t rows = (size_t)md.m * md.z * md.r;
     unsigned rescored = 0;
     if (row < rows)
-        rescored = merge_row(row, lane, md, suppLen, Proj, uCols, uniqJ, nLists, K, rPad, a1, a1raw, scal, candV,
+        rescored = merge_row(row, lane, md, suppLen, pv, uniqJ, nLists, K, rPad, a1, a1raw, scal, candV,
                              candU, candX, ustar, jstar, rowFlag, badModel);
     if (lane == 0 && rescored) {
         atomicAdd(&blockCount[0], 1u);
@@ -1080,7 +1080,7 @@ int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, 
     const size_t rows = (size_t)tc->MZ * md.r;
     cudaMemsetAsync(tc->rowFlag, 0, rows * sizeof(unsigned), eng.stream);
     tc_merge_kernel<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, eng.stream>>>(
-        md, eng.suppLen, eng.Proj, eng.projCols, eng.uniqJ, lists, sched.topk, tc->rPad, tc->a1, tc->a1raw, tc->scal, tc->candV,
+        md, eng.suppLen, eng.proj_view(), eng.uniqJ, lists, sched.topk, tc->rPad, tc->a1, tc->a1raw, tc->scal, tc->candV,
         tc->candU,
         tc->candX, eng.ustar, eng.jstar, tc->rowFlag, tc->scal + 3, tc->badModel);
     if ((rc = check_launch(fn, "candidate merge")) != NOVA_SUCCESS) return rc;
