@@ -136,6 +136,16 @@ NOVA_API int pomdp_alpha_vectors_value_and_action_batched(const POMDPAlphaVector
 NOVA_API int nova_load_raw_pomdp(const char *path, POMDP *pomdp, unsigned int rewardIndex);
 NOVA_API int nova_load_raw_mdp(const char *path, MDP *mdp, unsigned int rewardIndex);
 
+/* Cassandra-format POMDP file into an uninitialized POMDP (host arrays, as
+ * pomdp_initialize_cpu allocates them), with the rules of the reference's
+ * FileLoader.load_cassandra (python/nova/file_loader.py:211-588): one belief
+ * (r = 1) from start / start include / start exclude, successor lists in
+ * statement order, R(s,a) the mean of each reward statement's numbers, the
+ * horizon from the reward range. Rmin and Rmax (may be NULL) receive the
+ * extreme rewards in double precision, as the reference's loader keeps them.
+ * NOVA_ERROR_INVALID_DATA where the reference fails to load the file. */
+NOVA_API int nova_load_cassandra_pomdp(const char *path, POMDP *pomdp, double *Rmin, double *Rmax);
+
 /* Value iteration until the Bellman residual max_s |V'(s) - V(s)|, computed
  * in FP64 on the device after every sweep, drops below tol, or maxSweeps
  * sweeps ran. The reference's VI has no convergence test (mdp_vi_gpu.cu:163-221

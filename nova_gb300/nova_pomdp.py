@@ -63,3 +63,4 @@ _nova.pomdp_expand_random_gpu.argtypes = (_P, ct.c_uint, ct.c_uint, ct.POINTER(c
                                           ct.POINTER(ct.POINTER(ct.c_float)))
 _nova.nova_gb300_expand_seed.argtypes = (ct.c_uint, ct.c_uint)
 _nova.nova_load_raw_pomdp.argtypes = (ct.c_char_p, _P, ct.c_uint)
+_nova.nova_load_cassandra_pomdp.argtypes = (ct.c_char_p, _P, ct.POINTER(ct.c_double), ct.POINTER(ct.c_double))

@@ -113,14 +113,26 @@ class POMDP(npm.NovaPOMDP):
         return p
 
     def load(self, filename, filetype='cassandra', scalarize=lambda x: x[0], rewardIndex=0):
-        """ Load a POMDP file (pomdp.py:149-200 of the reference). 'raw' files are parsed by
-            nova_load_raw_pomdp (C++), keeping reward function rewardIndex (the reference's
-            default scalarisation keeps the first; other scalarisations are not supported).
-            The 'cassandra' format is not parsed by this library. """
-        if filetype != 'raw':
-            raise NotImplementedError("nova-gb300 parses raw files only; use set_arrays() for others")
+        """ Load a POMDP file (pomdp.py:149-200 of the reference). 'cassandra' files are
+            parsed by nova_load_cassandra_pomdp (C++, the rules of file_loader.py:211-588);
+            'raw' files by nova_load_raw_pomdp (C++), keeping reward function rewardIndex (the
+            reference's default scalarisation keeps the first; other scalarisations are not
+            supported). """
+        if filetype not in ('cassandra', 'raw'):
+            print("Invalid file type '%s'." % (filetype))
+            raise Exception()
         if self.S:
             raise RuntimeError("the POMDP already holds arrays")
+        if filetype == 'cassandra':
+            rmin, rmax = ct.c_double(0.0), ct.c_double(0.0)
+            result = npm._nova.nova_load_cassandra_pomdp(str(filename).encode(), self, ct.byref(rmin),
+                                                         ct.byref(rmax))
+            if result != 0:
+                print("Failed to load file '%s'." % (filename))
+                raise Exception()
+            self.Rmin = rmin.value
+            self.Rmax = rmax.value
+            return
         result = npm._nova.nova_load_raw_pomdp(str(filename).encode(), self, int(rewardIndex))
         if result != 0:
             print("Failed to load file '%s'." % (filename))

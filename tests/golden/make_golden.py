@@ -126,6 +126,40 @@ def loader_fixtures():
     print("wrote loader fixtures")
 
 
+def cassandra_fixtures():
+    """Synthetic Cassandra-format files (cassandra_files.py) read by the
+    reference's FileLoader.load_cassandra; numpy's removed np.float alias,
+    which its reward statements call, is provided as Python's float."""
+    import cassandra_files
+    if not hasattr(np, "float"):
+        np.float = float
+    for name, writer in cassandra_files.WRITERS.items():
+        path = os.path.join(HERE, name + ".pomdp")
+        writer(path)
+        fl = reference_loader()
+        try:
+            fl.load_cassandra(path)
+            # POMDP.load (pomdp.py:149-200) then needs every array and passes
+            # the sizes to pomdp_initialize_cpu, whose checks
+            # (pomdp_model_cpu.cpp:37-43) are applied here.
+            ok = all(getattr(fl, k) is not None for k in ("S", "T", "O", "R", "Z", "B")) and \
+                fl.n >= fl.ns >= 1 and min(fl.m, fl.z, fl.r, fl.rz) >= 1 and \
+                0.0 <= np.float32(fl.gamma) <= 1.0 and 1 <= fl.horizon < 2 ** 32
+        except Exception:
+            ok = False
+        if not ok:
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), ok=np.int64(0))
+            print("wrote", name, "(the reference fails to load it)")
+            continue
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), ok=np.int64(1), n=fl.n, ns=fl.ns, m=fl.m, z=fl.z,
+                            r=fl.r, rz=fl.rz, horizon=fl.horizon, gamma=np.float64(fl.gamma),
+                            Rmin=np.float64(fl.Rmin), Rmax=np.float64(fl.Rmax), S=np.asarray(fl.S, np.int32),
+                            T=np.asarray(fl.T, np.float32), O=np.asarray(fl.O, np.float32),
+                            R=np.asarray(fl.R, np.float32), Z=np.asarray(fl.Z, np.int32),
+                            B=np.asarray(fl.B, np.float32))
+        print("wrote", name, "n=%d ns=%d m=%d z=%d rz=%d horizon=%d" % (fl.n, fl.ns, fl.m, fl.z, fl.rz, fl.horizon))
+
+
 def main():
     if not orc.ref_available():
         raise SystemExit("the reference library is not available (needs %s)" % REF_DIR)
@@ -181,6 +215,7 @@ def main():
     # Raw-file loaders: files written by raw_files.py, parsed by the
     # reference's FileLoader; the parsed arrays are the fixture.
     loader_fixtures()
+    cassandra_fixtures()
 
     md = synth.random_mdp(n=1000, m=4, ns=8, gamma=0.95, horizon=50, seed=31)
     rmd = ragged(dict(md, Z=np.zeros((2, 2), np.int32), B=np.zeros((2, 2), np.float32)), seed=32)

@@ -210,3 +210,74 @@ def test_raw_loader_on_reference_tiger_file():
     for k, t in (("S", np.int32), ("T", np.float32), ("O", np.float32), ("R", np.float32), ("Z", np.int32),
                  ("B", np.float32)):
         np.testing.assert_array_equal(out[k], np.asarray(getattr(fl, k), t))
+
+
+# ---------------------------------------------------------------------------
+# Cassandra-format loader (host code; no GPU)
+# ---------------------------------------------------------------------------
+
+CASSANDRA_FIXTURES = ["cass_named", "cass_counts", "cass_exclude", "cass_single_start", "cass_start_uniform",
+                      "cass_no_reward", "cass_long_rows"]
+
+
+def _check_cassandra(p, g):
+    out = p.arrays()
+    for k in ("n", "ns", "m", "z", "r", "rz", "horizon"):
+        assert out[k] == int(g[k]), k
+    assert np.float32(out["gamma"]) == np.float32(g["gamma"])
+    for k in ("S", "Z"):
+        np.testing.assert_array_equal(out[k], np.asarray(g[k], np.int32).reshape(out[k].shape))
+    for k in ("T", "O", "R", "B"):
+        np.testing.assert_array_equal(out[k].view(np.uint32),
+                                      np.asarray(g[k], np.float32).reshape(out[k].shape).view(np.uint32))
+    assert p.Rmin == float(g["Rmin"]) and p.Rmax == float(g["Rmax"])
+
+
+@pytest.mark.parametrize("name", CASSANDRA_FIXTURES)
+def test_cassandra_loader_matches_reference_loader(name):
+    """Synthetic files (tests/golden/cassandra_files.py) against the arrays the
+    reference's FileLoader.load_cassandra produced for them; files the
+    reference fails to load must fail here too."""
+    from conftest import GOLDEN
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    p = POMDP()
+    path = os.path.join(GOLDEN, name + ".pomdp")
+    if int(g["ok"]) == 0:
+        with pytest.raises(Exception):
+            p.load(path, filetype="cassandra")
+        assert not p.S
+        return
+    p.load(path, filetype="cassandra")
+    _check_cassandra(p, g)
+
+
+def test_cassandra_loader_rejects_missing_file(tmp_path):
+    with pytest.raises(Exception):
+        POMDP().load(str(tmp_path / "missing.pomdp"), filetype="cassandra")
+    with pytest.raises(Exception):
+        POMDP().load(str(tmp_path / "missing.pomdp"), filetype="xml")
+
+
+_REF_DOMAINS = "/root/reference/tests/benchmarks/algorithms/domains"
+
+
+@pytest.mark.skipif(not os.path.isdir(_REF_DOMAINS), reason="reference domain files not present")
+@pytest.mark.parametrize("name", ["4x3_95", "aloha_10", "drive_san_francisco", "hallway2", "mit", "paint_95",
+                                  "shuttle_95", "tag", "tiger_95", "tiger_grid"])
+def test_cassandra_loader_on_reference_domains(name):
+    """The reference's own benchmark domains, loaded by its Python loader
+    (numpy's removed np.float alias provided as float) and by ours."""
+    import importlib.util
+    if not hasattr(np, "float"):
+        np.float = float
+    spec = importlib.util.spec_from_file_location("ref_file_loader", "/root/reference/python/nova/file_loader.py")
+    fl = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(fl)
+    path = os.path.join(_REF_DOMAINS, name + ".pomdp")
+    L = fl.FileLoader()
+    L.load_cassandra(path)
+    p = POMDP()
+    p.load(path, filetype="cassandra")
+    g = dict(n=L.n, ns=L.ns, m=L.m, z=L.z, r=L.r, rz=L.rz, horizon=L.horizon, gamma=L.gamma, S=L.S, T=L.T, O=L.O,
+             R=L.R, Z=L.Z, B=L.B, Rmin=L.Rmin, Rmax=L.Rmax)
+    _check_cassandra(p, g)
