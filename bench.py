@@ -335,12 +335,12 @@ def run_batch(args):
         pomdps.append(p)
     total = float(sum(md["r"] for md in models) * H)
 
-    def timed(mode, threads, horizon=H):
+    def timed(mode, threads, horizon=H, graph=False):
         for p in pomdps:
             p.horizon = horizon
         torch.cuda.synchronize()
         t = time.perf_counter()
-        pols = solve_batched(pomdps, scoring=mode, hostThreads=threads)
+        pols = solve_batched(pomdps, scoring=mode, hostThreads=threads, graph=graph)
         torch.cuda.synchronize()
         return time.perf_counter() - t, pols
 
@@ -348,18 +348,24 @@ def run_batch(args):
     t_fp16, pol_fp16 = timed(npp.SCORING_FP16, args.batch_threads)
     g16 = [(p.gamma_array(), p.pi_array()) for p in pol_fp16]
     del pol_fp16
+    t_graph, pol_graph = timed(npp.SCORING_FP16, args.batch_threads, graph=True)
+    g_gr = [(p.gamma_array(), p.pi_array()) for p in pol_graph]
+    del pol_graph
     t_bf16, pol_bf16 = timed(npp.SCORING_BF16, args.batch_threads)
     g_bf = [(p.gamma_array(), p.pi_array()) for p in pol_bf16]
     del pol_bf16
     t_plain, pol_plain = timed(npp.SCORING_EXACT, 1)
     identical = 0
-    for (G16, p16), (Gb, pb), pol in zip(g16, g_bf, pol_plain):
+    for (G16, p16), (Gb, pb), (Gg, pg), pol in zip(g16, g_bf, g_gr, pol_plain):
         G, pi = pol.gamma_array(), pol.pi_array()
         identical += int(np.array_equal(G16.view(np.uint32), G.view(np.uint32)) and np.array_equal(p16, pi) and
-                         np.array_equal(Gb.view(np.uint32), G.view(np.uint32)) and np.array_equal(pb, pi))
+                         np.array_equal(Gb.view(np.uint32), G.view(np.uint32)) and np.array_equal(pb, pi) and
+                         np.array_equal(Gg.view(np.uint32), G.view(np.uint32)) and np.array_equal(pg, pi))
     return {"metric": "belief-backups/s summed over a batch of 256 random POMDPs", "unit": "belief-backups/s",
             "value": total / t_fp16, "horizon": H, "host_threads": args.batch_threads,
             "fp16_batched_s": t_fp16, "bf16_batched": {"value": total / t_bf16, "seconds": t_bf16},
+            "fp16_batched_graph": {"value": total / t_graph, "seconds": t_graph,
+                                   "note": "horizon loops replayed as CUDA graphs after schedule tuning"},
             "plain_fp32_one_by_one": {"value": total / t_plain, "seconds": t_plain},
             "policies_bit_identical": "%d of 256" % identical,
             "belief_backups": total, "generation_s": gen_s,

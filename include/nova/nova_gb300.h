@@ -39,6 +39,17 @@ NOVA_NS_BEGIN
  * All modes give bit-identical results. */
 NOVA_API int pomdp_pbvi_set_scoring_gpu(POMDPPBVIGPU *pbvi, unsigned int mode);
 
+/* Graph mode for later pomdp_pbvi_update_gpu calls on this solver (default
+ * off). Once the solver scores on the tensor cores with a fixed schedule (its
+ * first tensor-core updates tune it), each update replays a CUDA graph of the
+ * whole backup: every alpha is scored as its own (no duplicate removal, the
+ * same argmax by the lowest index), the exact scan is sized on the device,
+ * and nothing is read back to the host inside the update; one graph per
+ * direction (Gamma -> GammaPrime and back) is captured on first use. Updates
+ * stay synchronous and give the same results; their statistics keep only the
+ * horizon, scoring mode, alpha count and kernel count. */
+NOVA_API int pomdp_pbvi_set_graph_gpu(POMDPPBVIGPU *pbvi, unsigned int enable);
+
 /* Per-update counters of the last pomdp_pbvi_update_gpu on this solver. */
 typedef struct NovaPBVIStats {
     unsigned int horizon;          /* currentHorizon after the update */
@@ -103,6 +114,14 @@ NOVA_API int pomdp_pbvi_adjoint_gpu(const POMDP *pomdp, unsigned int horizon,
  * Returns the first failing solve's code (the others still run). No
  * reference counterpart. */
 NOVA_API int pomdp_pbvi_execute_batched_gpu(const POMDP *const *pomdps, POMDPPBVIGPU *const *solvers,
+        POMDPAlphaVectors *const *policies, unsigned int count, unsigned int scoring,
+        unsigned int hostThreads);
+
+/* As pomdp_pbvi_execute_batched_gpu with every solver in graph mode
+ * (pomdp_pbvi_set_graph_gpu): after its first tensor-core updates, each
+ * solve's horizon loop replays two captured CUDA graphs. Same results. No
+ * reference counterpart. */
+NOVA_API int pomdp_pbvi_execute_batched_graph_gpu(const POMDP *const *pomdps, POMDPPBVIGPU *const *solvers,
         POMDPAlphaVectors *const *policies, unsigned int count, unsigned int scoring,
         unsigned int hostThreads);
 

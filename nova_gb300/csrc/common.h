@@ -31,6 +31,7 @@ int h2d(void *dst, const void *src, size_t bytes, const char *fn, const char *wh
 int d2h(void *dst, const void *src, size_t bytes, const char *fn, const char *what);
 int check_launch(const char *fn, const char *what);  // call once after every kernel launch
 unsigned long long launch_count();
+void add_launches(long long delta);  // kernels run by a graph replay (negative: captured, not run)
 int sync_device(const char *fn);
 
 template <typename T>

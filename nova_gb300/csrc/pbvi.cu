@@ -25,6 +25,8 @@
 
 #include "pbvi.h"
 
+#include <mutex>
+
 #include <vector>
 #include <algorithm>
 
@@ -617,7 +619,8 @@ __global__ void __launch_bounds__(256) proj_state_major_kernel(DevModel md, cons
 __global__ void __launch_bounds__(256) scan_rows_kernel(DevModel md, const unsigned *__restrict__ suppLen,
                                                         const ProjView pv, unsigned u0,
                                                         unsigned u1, const unsigned *__restrict__ rowList,
-                                                        unsigned nRows, float *__restrict__ runV,
+                                                        unsigned nRows, const unsigned *__restrict__ nRowsDev,
+                                                        float *__restrict__ runV,
                                                         unsigned *__restrict__ runU, int first) {
     extern __shared__ float sh[];
     float *bk = sh;                                              // [rz]
@@ -625,6 +628,7 @@ __global__ void __launch_bounds__(256) scan_rows_kernel(DevModel md, const unsig
     __shared__ float redV[8];
     __shared__ unsigned redU[8];
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (nRowsDev) nRows = min(nRows, *nRowsDev);
     for (unsigned w = blockIdx.x; w < nRows; w += gridDim.x) {
         const unsigned row = rowList ? rowList[w] : w;
         const unsigned ao = row / md.r, i = row % md.r;
@@ -667,9 +671,11 @@ __global__ void __launch_bounds__(256) scan_rows_kernel(DevModel md, const unsig
 
 // Final choice of each scanned row (kNone where nothing beat the sentinel).
 __global__ void scan_finish_kernel(DevModel md, const unsigned *__restrict__ rowList, unsigned nRows,
+                                   const unsigned *__restrict__ nRowsDev,
                                    const unsigned *__restrict__ runU, const unsigned *__restrict__ uniqJ,
                                    unsigned *__restrict__ ustar, unsigned *__restrict__ jstar) {
     const unsigned w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nRowsDev) nRows = min(nRows, *nRowsDev);
     if (w >= nRows) return;
     const unsigned row = rowList ? rowList[w] : w;
     const unsigned ao = row / md.r, i = row % md.r;
@@ -780,6 +786,8 @@ __global__ void __launch_bounds__(256) assemble_proj_kernel(DevModel md, const P
 
 BackupEngine::~BackupEngine() {
     cudaDeviceSynchronize();
+    for (auto &g : graph)
+        if (g) cudaGraphExecDestroy(g);
     if (tc) tc_release(tc);
     cudaFree(succLen); cudaFree(suppLen); cudaFree(C1); cudaFree(C3);
     cudaFree(hash); cudaFree(rep); cudaFree(uniqJ); cudaFree(nUniqueDev); cudaFree(Gt);
@@ -934,12 +942,17 @@ int BackupEngine::project(unsigned nU, const char *fn) {
         const unsigned uRange =
             (unsigned)std::max<size_t>(64, ((32ull << 20) / ((size_t)md.n * sizeof(float))) / 64 * 64);
         const dim3 blocks(md.m * ceil_div(md.n, kProjTileS), ceil_div(std::max(nU, 1u), uRange));
+        if (!projAttrDone) {
+            cudaFuncSetAttribute(proj_state_major_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(proj_state_major_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(proj_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(proj_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            projAttrDone = true;
+        }
         if (zc == 32) {
-            cudaFuncSetAttribute(proj_state_major_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             proj_state_major_kernel<32><<<blocks, 256, smem, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj,
                                                                        projCols, projSCols, uRange);
         } else {
-            cudaFuncSetAttribute(proj_state_major_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             proj_state_major_kernel<8><<<blocks, 256, smem, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj,
                                                                       projCols, projSCols, uRange);
         }
@@ -947,20 +960,24 @@ int BackupEngine::project(unsigned nU, const char *fn) {
     }
     const size_t smem32 = (size_t)md.ns * 32 * sizeof(float) + md.ns * sizeof(int);
     const unsigned blocks = md.m * md.n;
+    if (!projAttrDone) {
+        cudaFuncSetAttribute(proj_state_major_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(proj_state_major_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(proj_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(proj_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        projAttrDone = true;
+    }
     if (md.z >= 16 && smem32 <= 200 * 1024) {
-        if (smem32 > 48 * 1024)
-            cudaFuncSetAttribute(proj_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32);
         proj_kernel<32><<<blocks, 256, smem32, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj, projCols);
     } else {
         const size_t smem8 = (size_t)md.ns * 8 * sizeof(float) + md.ns * sizeof(int);
-        if (smem8 > 48 * 1024)
-            cudaFuncSetAttribute(proj_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem8);
         proj_kernel<8><<<blocks, 256, smem8, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj, projCols);
     }
     return check_launch(fn, "projection table");
 }
 
-int BackupEngine::scan_rows(const unsigned *rowList, unsigned nRows, unsigned nU, const char *fn) {
+int BackupEngine::scan_rows(const unsigned *rowList, unsigned nRows, unsigned nU, const char *fn,
+                            const unsigned *nRowsDev) {
     if (nRows == 0) return NOVA_SUCCESS;
     int rc;
     if ((size_t)nRows > scanCap) {
@@ -977,11 +994,12 @@ int BackupEngine::scan_rows(const unsigned *rowList, unsigned nRows, unsigned nU
     for (size_t u0 = 0; u0 < std::max(nU, 1u); u0 += chunk) {
         const unsigned u1 = (unsigned)std::min<size_t>(nU, u0 + chunk);
         scan_rows_kernel<<<grid, 256, 2 * md.rz * sizeof(float), stream>>>(md, suppLen, proj_view(), (unsigned)u0,
-                                                                          u1, rowList, nRows, scanV, scanU,
-                                                                          u0 == 0 ? 1 : 0);
+                                                                          u1, rowList, nRows, nRowsDev, scanV,
+                                                                          scanU, u0 == 0 ? 1 : 0);
         if ((rc = check_launch(fn, "exact row scan")) != NOVA_SUCCESS) return rc;
     }
-    scan_finish_kernel<<<ceil_div(nRows, 256), 256, 0, stream>>>(md, rowList, nRows, scanU, uniqJ, ustar, jstar);
+    scan_finish_kernel<<<ceil_div(nRows, 256), 256, 0, stream>>>(md, rowList, nRows, nRowsDev, scanU, uniqJ, ustar,
+                                                                 jstar);
     if ((rc = check_launch(fn, "exact row scan (finish)")) != NOVA_SUCCESS) return rc;
     sentinel_fixup_kernel<<<ceil_div((size_t)md.r * md.m, 256), 256, 0, stream>>>(md, uniqJ, ustar, jstar);
     return check_launch(fn, "sentinel fixup");
@@ -1012,7 +1030,7 @@ int BackupEngine::assemble(const float *src, float *dst, unsigned *pi, int onlyB
         action_value_kernel<<<ceil_div((size_t)nItems * 32, 256), 256, 0, stream>>>(md, succLen, suppLen, C3, src,
                                                                                     jstar, itemList, nItems, actVal);
     if ((rc = check_launch(fn, "action values")) != NOVA_SUCCESS) return rc;
-    if (onlyBelief < 0) cudaEventRecord(ev[6], stream);
+    if (onlyBelief < 0 && !capturing) cudaEventRecord(ev[6], stream);
     if (useProjNow && onlyBelief < 0)
         assemble_proj_kernel<<<nBeliefs, 256, md.z * sizeof(unsigned), stream>>>(md, proj_view(), ustar, actVal,
                                                                                   dst, pi);
@@ -1026,6 +1044,7 @@ int BackupEngine::assemble(const float *src, float *dst, unsigned *pi, int onlyB
 int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsigned *pi, const char *fn) {
     int rc;
     memset(&stats, 0, sizeof(stats));
+    identityUniq = false;  // the dedup below rewrites uniqJ
     const unsigned long long launches0 = launch_count();
     cudaEventRecord(ev[0], stream);
     unsigned nU = 0;
@@ -1097,6 +1116,33 @@ int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsi
         return NOVA_ERROR_KERNEL_EXECUTION;
     }
     return NOVA_SUCCESS;
+}
+
+bool BackupEngine::fixed_ready() const {
+    return tc != nullptr && !tcUnavailable && tc_schedule_fixed(*this) && Proj != nullptr && !projUnavailable &&
+           projCap >= (size_t)md.m * md.z * std::max(projSCols, (size_t)md.n) * round_up(md.r, 32) &&
+           scanCap >= (size_t)md.m * md.z * md.r && identityUniq &&
+           (scoring == NOVA_SCORING_BF16 || scoring == NOVA_SCORING_FP16);
+}
+
+int BackupEngine::backup_fixed(const float *src, float *dst, unsigned *pi, const char *fn) {
+    int rc;
+    const unsigned nU = md.r;
+    dim3 grid(ceil_div(nU, 32), ceil_div(md.n, 32));
+    gather_transpose_kernel<<<grid, dim3(32, 8), 0, stream>>>(src, md.n, uniqJ, nU, Gt, gtCols);
+    if ((rc = check_launch(fn, "alpha transpose")) != NOVA_SUCCESS) return rc;
+    useProjNow = ensure_proj(nU);
+    if (!useProjNow) return NOVA_ERROR_KERNEL_EXECUTION;
+    {
+        const unsigned zc = md.z >= 16 ? 32u : 8u;
+        const size_t smemSM = ((size_t)kProjTileS * md.ns * zc + (size_t)zc * 64 * (kProjTileS + 1)) * sizeof(float) +
+                              (size_t)kProjTileS * md.ns * sizeof(int);
+        projStateMajor = md.n > kStateMajorMinStates && smemSM <= 200 * 1024;
+    }
+    if ((rc = project(nU, fn)) != NOVA_SUCCESS) return rc;
+    if ((rc = tc_score_launch(*this, src, nU, false, fn)) != NOVA_SUCCESS) return rc;
+    if ((rc = scan_rows(tc_row_list(*this), md.m * md.z * md.r, nU, fn, itemCount)) != NOVA_SUCCESS) return rc;
+    return assemble(src, dst, pi, -1, nullptr, nullptr, fn);
 }
 
 // Selections of the last backup: for belief i, the action a = pi[i] whose
@@ -1307,6 +1353,126 @@ static int ensure_built(PbviGpuWorkspace *ws, const POMDP *pomdp, const char *fn
     return NOVA_SUCCESS;
 }
 
+// Graph mode: once the solver scores on the tensor cores with a fixed
+// schedule, an update is the replay of a CUDA graph of backup_fixed (no host
+// read-back inside), captured once per direction Gamma -> GammaPrime and
+// GammaPrime -> Gamma on a private stream and launched on the solver's
+// stream; the call still returns after the update is complete.
+//
+// A capture must not overlap a device-wide synchronisation or allocation
+// in another host thread (the batched solve runs many solvers at once), so
+// captures hold capture_lock() exclusively and every other update, and the
+// batched solve's other calls, hold it shared.
+std::shared_mutex &nova_gb300::capture_lock() {
+    static std::shared_mutex m;
+    return m;
+}
+
+static bool graph_wanted(const BackupEngine &e) {
+    return e.graphMode && e.tc != nullptr && !e.tcUnavailable && tc_schedule_fixed(e) && e.Proj != nullptr &&
+           !e.projUnavailable && (e.scoring == NOVA_SCORING_BF16 || e.scoring == NOVA_SCORING_FP16);
+}
+
+static int graph_dir(const BackupEngine &e, const float *src) {
+    return src == e.graphSrc[0] ? 0 : src == e.graphSrc[1] ? 1 : (e.graph[0] == nullptr ? 0 : 1);
+}
+
+static bool graph_needs_capture(const BackupEngine &e, const float *src) {
+    const int dir = graph_dir(e, src);
+    return !e.identityUniq || e.graph[dir] == nullptr || e.graphSrc[dir] != src;
+}
+
+// Under capture_lock() held exclusively.
+static int graph_prepare(BackupEngine &e, const float *src, float *dst, unsigned *pi, const char *fn) {
+    int rc;
+    if (!e.identityUniq) {
+        if ((rc = e.fill_items(0, e.md.r, fn)) != NOVA_SUCCESS) return rc;
+        if (cudaMemcpyAsync(e.uniqJ, e.items, (size_t)e.md.r * sizeof(unsigned), cudaMemcpyDeviceToDevice,
+                            e.stream) != cudaSuccess) {
+            cudaGetLastError();
+            return NOVA_ERROR_KERNEL_EXECUTION;
+        }
+        e.identityUniq = true;
+    }
+    const size_t rows = (size_t)e.md.m * e.md.z * e.md.r;
+    if (e.scanCap < rows) {
+        cudaFree(e.scanV); cudaFree(e.scanU);
+        e.scanV = nullptr; e.scanU = nullptr; e.scanCap = 0;
+        if ((rc = dev_alloc(&e.scanV, rows, fn, "the scan maxima")) != NOVA_SUCCESS) return rc;
+        if ((rc = dev_alloc(&e.scanU, rows, fn, "the scan arg-maxima")) != NOVA_SUCCESS) return rc;
+        e.scanCap = rows;
+    }
+    if (!e.fixed_ready()) {
+        e.graphMode = false;
+        return NOVA_SUCCESS;
+    }
+    const int dir = graph_dir(e, src);
+    if (e.graph[dir] != nullptr && e.graphSrc[dir] == src) return NOVA_SUCCESS;
+    if (e.graph[dir]) { cudaGraphExecDestroy(e.graph[dir]); e.graph[dir] = nullptr; }
+    if ((rc = sync_device(fn)) != NOVA_SUCCESS) return rc;
+    cudaStream_t cs = nullptr;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        e.graphMode = false;  // stay with ordinary updates
+        return NOVA_SUCCESS;
+    }
+    const cudaStream_t saved = e.stream;
+    e.stream = cs;
+    e.capturing = true;
+    const unsigned long long l0 = launch_count();
+    cudaGraph_t g = nullptr;
+    bool ok = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+        rc = e.backup_fixed(src, dst, pi, fn);
+        ok = cudaStreamEndCapture(cs, &g) == cudaSuccess && rc == NOVA_SUCCESS && g != nullptr;
+    }
+    const long long captured = (long long)(launch_count() - l0);
+    add_launches(-captured);  // captured, not run
+    e.stream = saved;
+    e.capturing = false;
+    cudaGraphExec_t exec = nullptr;
+    if (ok) ok = cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    if (!ok) {
+        cudaGetLastError();
+        e.graphMode = false;  // ordinary updates from now on
+        return NOVA_SUCCESS;
+    }
+    e.graph[dir] = exec;
+    e.graphSrc[dir] = src;
+    e.graphLaunches[dir] = (unsigned)captured;
+    return NOVA_SUCCESS;
+}
+
+// Under capture_lock() held shared.
+static int graph_replay(BackupEngine &e, const float *src, bool *done, const char *fn) {
+    *done = false;
+    if (!graph_wanted(e) || graph_needs_capture(e, src)) return NOVA_SUCCESS;
+    const int dir = graph_dir(e, src);
+    memset(&e.stats, 0, sizeof(e.stats));
+    if (cudaGraphLaunch(e.graph[dir], e.stream) != cudaSuccess) {
+        cudaGetLastError();
+        NOVA_ERR(fn, "Failed to launch the update graph.");
+        return NOVA_ERROR_KERNEL_EXECUTION;
+    }
+    add_launches(e.graphLaunches[dir]);
+    if (cudaStreamSynchronize(e.stream) != cudaSuccess) {
+        cudaGetLastError();
+        NOVA_ERR(fn, "The update graph failed.");
+        return NOVA_ERROR_KERNEL_EXECUTION;
+    }
+    if (tc_device_error() != 0) {
+        NOVA_ERR(fn, "A device-side wait timed out; results of this update are invalid.");
+        return NOVA_ERROR_KERNEL_EXECUTION;
+    }
+    e.stats.scoring = e.scoring;
+    e.stats.uniqueAlphas = e.md.r;
+    e.stats.launches = e.graphLaunches[dir];
+    *done = true;
+    return NOVA_SUCCESS;
+}
+
 extern "C" int pomdp_pbvi_update_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi) {
     static const char *fn = "pomdp_pbvi_update_gpu";
     if (pomdp_shape_invalid(pomdp) || pbvi == nullptr || pomdp->d_S == nullptr || pomdp->d_T == nullptr ||
@@ -1320,15 +1486,27 @@ extern "C" int pomdp_pbvi_update_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi) {
         NOVA_ERR(fn, "The solver is not initialized (call pomdp_pbvi_initialize_gpu).");
         return NOVA_ERROR_INVALID_DATA;
     }
+    std::shared_lock<std::shared_mutex> lock(nova_gb300::capture_lock());
     int rc = ensure_built(ws, pomdp, fn);
     if (rc != NOVA_SUCCESS) return rc;
     const bool even = (pbvi->currentHorizon % 2u) == 0u;
     const float *src = even ? pbvi->d_Gamma : pbvi->d_GammaPrime;
     float *dst = even ? pbvi->d_GammaPrime : pbvi->d_Gamma;
-    rc = ws->eng.backup_all(src, pomdp->r, dst, pbvi->d_pi, fn);
-    if (rc != NOVA_SUCCESS) return rc;
+    BackupEngine &e = ws->eng;
+    if (graph_wanted(e) && graph_needs_capture(e, src)) {
+        lock.unlock();
+        {
+            std::unique_lock<std::shared_mutex> excl(nova_gb300::capture_lock());
+            rc = graph_prepare(e, src, dst, pbvi->d_pi, fn);
+        }
+        lock.lock();
+        if (rc != NOVA_SUCCESS) return rc;
+    }
+    bool byGraph = false;
+    if ((rc = graph_replay(e, src, &byGraph, fn)) != NOVA_SUCCESS) return rc;
+    if (!byGraph && (rc = e.backup_all(src, pomdp->r, dst, pbvi->d_pi, fn)) != NOVA_SUCCESS) return rc;
     pbvi->currentHorizon++;
-    ws->eng.stats.horizon = pbvi->currentHorizon;
+    e.stats.horizon = pbvi->currentHorizon;
     return NOVA_SUCCESS;
 }
 
@@ -1382,6 +1560,20 @@ extern "C" int pomdp_pbvi_execute_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi, PO
     rc = pomdp_pbvi_get_policy_gpu(pomdp, pbvi, policy);
     if (rc != NOVA_SUCCESS) return rc;
     return pomdp_pbvi_uninitialize_gpu(pomdp, pbvi);
+}
+
+extern "C" int pomdp_pbvi_set_graph_gpu(POMDPPBVIGPU *pbvi, unsigned int enable) {
+    if (pbvi == nullptr) {
+        NOVA_ERR("pomdp_pbvi_set_graph_gpu", "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    PbviGpuWorkspace *ws = pbvi_gpu_ws(pbvi);
+    if (ws == nullptr) {
+        NOVA_ERR("pomdp_pbvi_set_graph_gpu", "The solver is not initialized.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    ws->eng.graphMode = enable != 0;
+    return NOVA_SUCCESS;
 }
 
 extern "C" int pomdp_pbvi_set_scoring_gpu(POMDPPBVIGPU *pbvi, unsigned int mode) {

@@ -6,6 +6,8 @@
 
 #include "common.h"
 
+#include <shared_mutex>
+
 #include <nova/pomdp/pomdp.h>
 #include <nova/nova_gb300.h>
 
@@ -104,7 +106,25 @@ struct BackupEngine {
         return ProjView{Proj, (size_t)md.n * projCols, projCols, 1};
     }
     // Exact scan of (a*z+o)*r + i rows over the projection table (all rows if rowList is null).
-    int scan_rows(const unsigned *rowList, unsigned nRows, unsigned nU, const char *fn);
+    // With nRowsDev the row count is read on the device (nRows is then its upper bound).
+    int scan_rows(const unsigned *rowList, unsigned nRows, unsigned nU, const char *fn,
+                  const unsigned *nRowsDev = nullptr);
+    // One update without host read-backs, for graph capture: every alpha
+    // is scored as its own (uniqJ must be the identity), tensor-core
+    // scoring with the solver's fixed schedule, the exact scan sized on the
+    // device. Same results as backup_all.
+    int backup_fixed(const float *src, float *dst, unsigned *pi, const char *fn);
+    // Ready for backup_fixed: tensor-core scoring built with a fixed
+    // schedule, the projection table allocated for all r alphas.
+    bool fixed_ready() const;
+    // Graphs of backup_fixed, one per direction (Gamma -> GammaPrime and back).
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    const float *graphSrc[2] = {nullptr, nullptr};
+    unsigned graphLaunches[2] = {0, 0};
+    bool graphMode = false;
+    bool identityUniq = false;     // uniqJ holds 0 .. r-1
+    bool capturing = false;        // launches are being captured, not run
+    bool projAttrDone = false;     // shared-memory attributes of the projection kernels set
     // Work list of `count` consecutive items starting at `first`.
     int fill_items(unsigned first, unsigned count, const char *fn);
     // Write the last backup's selections (action per belief, alpha per
@@ -115,6 +135,10 @@ struct BackupEngine {
                  unsigned *actionOut, const char *fn);
 };
 
+// Held exclusively while an update graph is captured, shared by everything
+// else that may run beside a capture in another host thread.
+std::shared_mutex &capture_lock();
+
 // Tensor-core scoring (pbvi_tc.cu). tc_supported: the shapes fit the GEMM.
 bool tc_supported(const DevModel &md);
 // Builds the BF16 operand tables once; returns NOVA_SUCCESS or an error.
@@ -124,6 +148,12 @@ int tc_build(BackupEngine &eng, const char *fn);
 // is proven, and appends the (belief, action) items that need the exact full
 // scan to *rowList / *nRows as (a*z+o)*r + i row indices (a device list
 // owned by the tensor-core state, sized for every row).
+// The launches of tc_score without its read-back: the flagged rows and their
+// count stay on the device (eng.tc rowList, eng.itemCount); `timed` records
+// the GEMM events.
+int tc_score_launch(BackupEngine &eng, const float *src, unsigned nU, bool timed, const char *fn);
+bool tc_schedule_fixed(const BackupEngine &eng);
+const unsigned *tc_row_list(const BackupEngine &eng);
 int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, const unsigned **rowList,
              const char *fn);
 void tc_release(TcState *tc);

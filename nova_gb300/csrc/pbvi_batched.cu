@@ -9,9 +9,12 @@
 // different host threads run concurrently on the device.
 
 #include "common.h"
+#include "pbvi.h"
 
 #include <algorithm>
 #include <atomic>
+#include <mutex>
+#include <shared_mutex>
 #include <thread>
 #include <vector>
 
@@ -26,20 +29,31 @@ using nova::POMDPAlphaVectors;
 
 namespace {
 
-int solve_one(const POMDP *pomdp, POMDPPBVIGPU *pbvi, POMDPAlphaVectors *policy, unsigned scoring) {
-    int rc = pomdp_pbvi_initialize_gpu(pomdp, pbvi);
-    if (rc != NOVA_SUCCESS) return rc;
-    if ((rc = pomdp_pbvi_set_scoring_gpu(pbvi, scoring)) != NOVA_SUCCESS) {
-        pomdp_pbvi_uninitialize_gpu(pomdp, pbvi);
-        return rc;
-    }
-    while (pbvi->currentHorizon < pomdp->horizon) {
-        rc = pomdp_pbvi_update_gpu(pomdp, pbvi);
-        if (rc != NOVA_SUCCESS) {
+// Calls other than the updates (which lock for themselves) hold the capture
+// lock shared, so that no allocation or device synchronisation of this
+// thread overlaps another solver's graph capture.
+int solve_one(const POMDP *pomdp, POMDPPBVIGPU *pbvi, POMDPAlphaVectors *policy, unsigned scoring, bool graph) {
+    using Shared = std::shared_lock<std::shared_mutex>;
+    int rc;
+    {
+        Shared lock(nova_gb300::capture_lock());
+        rc = pomdp_pbvi_initialize_gpu(pomdp, pbvi);
+        if (rc != NOVA_SUCCESS) return rc;
+        if ((rc = pomdp_pbvi_set_scoring_gpu(pbvi, scoring)) != NOVA_SUCCESS ||
+                (rc = pomdp_pbvi_set_graph_gpu(pbvi, graph ? 1u : 0u)) != NOVA_SUCCESS) {
             pomdp_pbvi_uninitialize_gpu(pomdp, pbvi);
             return rc;
         }
     }
+    while (pbvi->currentHorizon < pomdp->horizon) {
+        rc = pomdp_pbvi_update_gpu(pomdp, pbvi);
+        if (rc != NOVA_SUCCESS) {
+            Shared lock(nova_gb300::capture_lock());
+            pomdp_pbvi_uninitialize_gpu(pomdp, pbvi);
+            return rc;
+        }
+    }
+    Shared lock(nova_gb300::capture_lock());
     rc = pomdp_pbvi_get_policy_gpu(pomdp, pbvi, policy);
     const int rc2 = pomdp_pbvi_uninitialize_gpu(pomdp, pbvi);
     return rc != NOVA_SUCCESS ? rc : rc2;
@@ -47,10 +61,9 @@ int solve_one(const POMDP *pomdp, POMDPPBVIGPU *pbvi, POMDPAlphaVectors *policy,
 
 }  // namespace
 
-extern "C" int pomdp_pbvi_execute_batched_gpu(const POMDP *const *pomdps, POMDPPBVIGPU *const *solvers,
-                                              POMDPAlphaVectors *const *policies, unsigned int count,
-                                              unsigned int scoring, unsigned int hostThreads) {
-    static const char *fn = "pomdp_pbvi_execute_batched_gpu";
+static int execute_batched(const POMDP *const *pomdps, POMDPPBVIGPU *const *solvers,
+                           POMDPAlphaVectors *const *policies, unsigned int count, unsigned int scoring,
+                           unsigned int hostThreads, bool graph, const char *fn) {
     if (pomdps == nullptr || solvers == nullptr || policies == nullptr || count == 0 ||
             (scoring != NOVA_SCORING_EXACT && scoring != NOVA_SCORING_BF16 && scoring != NOVA_SCORING_FP16)) {
         NOVA_ERR(fn, "Invalid arguments.");
@@ -94,7 +107,7 @@ extern "C" int pomdp_pbvi_execute_batched_gpu(const POMDP *const *pomdps, POMDPP
         }
         for (unsigned k = next.fetch_add(1); k < count; k = next.fetch_add(1)) {
             const unsigned p = order[k];
-            const int rc = solve_one(pomdps[p], solvers[p], policies[p], scoring);
+            const int rc = solve_one(pomdps[p], solvers[p], policies[p], scoring, graph);
             if (rc != NOVA_SUCCESS) {
                 int expected = NOVA_SUCCESS;
                 firstError.compare_exchange_strong(expected, rc);
@@ -106,4 +119,18 @@ extern "C" int pomdp_pbvi_execute_batched_gpu(const POMDP *const *pomdps, POMDPP
     worker();
     for (auto &t : pool) t.join();
     return firstError.load();
+}
+
+extern "C" int pomdp_pbvi_execute_batched_gpu(const POMDP *const *pomdps, POMDPPBVIGPU *const *solvers,
+                                              POMDPAlphaVectors *const *policies, unsigned int count,
+                                              unsigned int scoring, unsigned int hostThreads) {
+    return execute_batched(pomdps, solvers, policies, count, scoring, hostThreads, false,
+                           "pomdp_pbvi_execute_batched_gpu");
+}
+
+extern "C" int pomdp_pbvi_execute_batched_graph_gpu(const POMDP *const *pomdps, POMDPPBVIGPU *const *solvers,
+                                                    POMDPAlphaVectors *const *policies, unsigned int count,
+                                                    unsigned int scoring, unsigned int hostThreads) {
+    return execute_batched(pomdps, solvers, policies, count, scoring, hostThreads, true,
+                           "pomdp_pbvi_execute_batched_graph_gpu");
 }

@@ -1022,8 +1022,7 @@ int tc_build(BackupEngine &eng, const char *fn) {
     return sync_device(fn);
 }
 
-int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, const unsigned **rowList,
-             const char *fn) {
+int tc_score_launch(BackupEngine &eng, const float *src, unsigned nU, bool timed, const char *fn) {
     int rc;
     if (!eng.tc && (rc = tc_build(eng, fn)) != NOVA_SUCCESS) return rc;
     TcState *tc = eng.tc;
@@ -1069,13 +1068,13 @@ int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, 
     tc->groupsUsed = groups;
     const unsigned totalUnits = tc->MZ * tc->mTiles * groups;
     const unsigned grid = std::min<unsigned>(totalUnits, (unsigned)tc->numSMs);
-    cudaEventRecord(tc->g0, eng.stream);
+    if (timed) cudaEventRecord(tc->g0, eng.stream);
     auto gemm = sched.topk == 16u ? tc_score_gemm_kernel<16> : tc_score_gemm_kernel<8>;
     gemm<<<grid, GEMM_THREADS, GEMM_SMEM, eng.stream>>>(
         tc->tmA, tmB, make_idesc(fp16 ? 0u : 1u), tc->MZ, (unsigned)tc->rPad, md.r, tc->mTiles, nTiles, groups, nU,
         (unsigned)(tc->nPad / BK), tc->a1, tc->scal, tc->candV, tc->candU, tc->candX);
     if ((rc = check_launch(fn, "tensor-core scoring")) != NOVA_SUCCESS) return rc;
-    cudaEventRecord(tc->g1, eng.stream);
+    if (timed) cudaEventRecord(tc->g1, eng.stream);
     // ---- merge, margin, exact re-score of near ties ----
     const size_t rows = (size_t)tc->MZ * md.r;
     cudaMemsetAsync(tc->rowFlag, 0, rows * sizeof(unsigned), eng.stream);
@@ -1095,6 +1094,18 @@ int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, 
                                                                   tc->rowList);
         if ((rc = check_launch(fn, "exact-scan list (write)")) != NOVA_SUCCESS) return rc;
     }
+    return NOVA_SUCCESS;
+}
+
+bool tc_schedule_fixed(const BackupEngine &eng) { return eng.tc != nullptr && eng.tc->schedFixed >= 0; }
+
+const unsigned *tc_row_list(const BackupEngine &eng) { return eng.tc ? eng.tc->rowList : nullptr; }
+
+int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, const unsigned **rowList,
+             const char *fn) {
+    int rc;
+    if ((rc = tc_score_launch(eng, src, nU, true, fn)) != NOVA_SUCCESS) return rc;
+    TcState *tc = eng.tc;
     unsigned h[8];
     unsigned cnt = 0;
     if (cudaMemcpyAsync(h, tc->scal, sizeof(h), cudaMemcpyDeviceToHost, eng.stream) != cudaSuccess ||

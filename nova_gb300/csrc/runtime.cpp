@@ -95,6 +95,8 @@ static std::atomic<unsigned long long> g_launches{0};
 
 unsigned long long launch_count() { return g_launches.load(); }
 
+void add_launches(long long delta) { g_launches.fetch_add((unsigned long long)delta); }
+
 int check_launch(const char *fn, const char *what) {
     g_launches.fetch_add(1);
     cudaError_t e = cudaGetLastError();

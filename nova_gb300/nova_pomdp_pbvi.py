@@ -70,6 +70,7 @@ for _suffix, _S in (("cpu", _C), ("gpu", _G)):
 
 _nova.nova_gb300_kernel_launches.restype = ct.c_ulonglong
 _nova.pomdp_pbvi_set_scoring_gpu.argtypes = (_G, ct.c_uint)
+_nova.pomdp_pbvi_set_graph_gpu.argtypes = (_G, ct.c_uint)
 _nova.pomdp_pbvi_get_stats_gpu.argtypes = (_G, ct.POINTER(NovaPBVIStats))
 _nova.pomdp_pbvi_value_gpu.argtypes = (_P, _G, ct.POINTER(ct.c_float), ct.POINTER(ct.c_double),
                                        ct.POINTER(ct.c_uint))
@@ -83,3 +84,4 @@ from . import nova_pomdp_alpha_vectors as _npav  # noqa: E402
 _nova.pomdp_pbvi_execute_batched_gpu.argtypes = (ct.POINTER(_P), ct.POINTER(_G),
                                                  ct.POINTER(ct.POINTER(_npav.NovaPOMDPAlphaVectors)), ct.c_uint,
                                                  ct.c_uint, ct.c_uint)
+_nova.pomdp_pbvi_execute_batched_graph_gpu.argtypes = _nova.pomdp_pbvi_execute_batched_gpu.argtypes

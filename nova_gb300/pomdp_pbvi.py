@@ -108,6 +108,13 @@ class POMDPPBVIGPU(npp.NovaPOMDPPBVIGPU):
         if result != 0:
             raise RuntimeError("pomdp_pbvi_set_scoring_gpu failed with code %d" % result)
 
+    def set_graph(self, enable=True):
+        """ Graph mode for later updates (pomdp_pbvi_set_graph_gpu): once the tensor-core
+            schedule is tuned, each update replays a captured CUDA graph. """
+        result = npp._nova.pomdp_pbvi_set_graph_gpu(self, 1 if enable else 0)
+        if result != 0:
+            raise RuntimeError("pomdp_pbvi_set_graph_gpu failed with code %d" % result)
+
     def update(self):
         """ One backup of every belief (pomdp_pbvi_update_gpu). """
         result = npp._nova.pomdp_pbvi_update_gpu(self.pomdpPtr, self)
@@ -152,10 +159,12 @@ class POMDPPBVIGPU(npp.NovaPOMDPPBVIGPU):
         return "currentHorizon: %i\n\nnumThreads: %i\n\n" % (self.currentHorizon, self.numThreads)
 
 
-def solve_batched(pomdps, scoring=npp.SCORING_FP16, hostThreads=0, GammaInitials=None):
+def solve_batched(pomdps, scoring=npp.SCORING_FP16, hostThreads=0, GammaInitials=None, graph=False):
     """ Solve independent POMDPs (each already copied to the device with
-    initialize_gpu) with pomdp_pbvi_execute_batched_gpu; returns one
-    POMDPAlphaVectors per POMDP, as each POMDPPBVIGPU(p).solve() would. """
+    initialize_gpu) with pomdp_pbvi_execute_batched_gpu (graph=True:
+    pomdp_pbvi_execute_batched_graph_gpu, horizon loops replayed as CUDA
+    graphs); returns one POMDPAlphaVectors per POMDP, as each
+    POMDPPBVIGPU(p).solve() would. """
     from . import pomdp_alpha_vectors as pav
     count = len(pomdps)
     solvers, bufs = [], []
@@ -173,8 +182,9 @@ def solve_batched(pomdps, scoring=npp.SCORING_FP16, hostThreads=0, GammaInitials
     A = (ct.POINTER(npp._npav.NovaPOMDPAlphaVectors) * count)(*[ct.cast(ct.pointer(a),
                                                                          ct.POINTER(npp._npav.NovaPOMDPAlphaVectors))
                                                                  for a in policies])
-    result = npp._nova.pomdp_pbvi_execute_batched_gpu(P, G, A, count, int(scoring), int(hostThreads))
+    entry = npp._nova.pomdp_pbvi_execute_batched_graph_gpu if graph else npp._nova.pomdp_pbvi_execute_batched_gpu
+    result = entry(P, G, A, count, int(scoring), int(hostThreads))
     _ = bufs
     if result != 0:
-        raise RuntimeError("pomdp_pbvi_execute_batched_gpu failed with code %d" % result)
+        raise RuntimeError("batched solve failed with code %d" % result)
     return policies

@@ -43,3 +43,45 @@ def test_batched_rejects_repeated_solver():
         ct.cast(ct.pointer(a1), ct.POINTER(npp._npav.NovaPOMDPAlphaVectors)),
         ct.cast(ct.pointer(a2), ct.POINTER(npp._npav.NovaPOMDPAlphaVectors)))
     assert npp._nova.pomdp_pbvi_execute_batched_gpu(P, G, A, 2, npp.SCORING_FP16, 2) != 0
+
+
+def test_batched_graph_solves_equal_reference():
+    """Graph mode (horizon loops replayed as CUDA graphs once the tensor-core
+    schedule is tuned) gives nova's results."""
+    models = synth.batch_pomdps(count=8, seed=11, n_range=(16, 96), r_range=(64, 200), m_range=(2, 4),
+                                z_range=(2, 5), horizon=12)
+    pomdps = []
+    for md in models:
+        p = POMDP.from_arrays(md)
+        p.initialize_gpu()
+        pomdps.append(p)
+    policies = solve_batched(pomdps, scoring=npp.SCORING_FP16, hostThreads=4, graph=True)
+    for md, pol in zip(models, policies):
+        G, pi = orc.pbvi_solve(md)
+        np.testing.assert_array_equal(bits(pol.gamma_array()), bits(G))
+        np.testing.assert_array_equal(pol.pi_array(), pi)
+
+
+@pytest.mark.parametrize("n", [150, 2100])
+def test_graph_updates_equal_reference(n):
+    """Single solver in graph mode: updates after the schedule is fixed are
+    graph replays (no per-update timings, kernels counted), with nova's
+    results; n = 2100 uses the state-contiguous projection table."""
+    from nova_gb300.pomdp_pbvi import POMDPPBVIGPU
+    md = synth.random_pomdp(n=n, m=2, z=4, ns=8, r=256, rz=16, gamma=0.95, horizon=9, seed=21)
+    p = POMDP.from_arrays(md)
+    p.initialize_gpu()
+    s = POMDPPBVIGPU(p)
+    s.set_scoring(npp.SCORING_FP16)
+    s.set_graph(True)
+    replays = 0
+    for _ in range(md["horizon"]):
+        s.update()
+        st = s.stats()
+        if st["msTotal"] == 0.0 and st["launches"] > 0:
+            replays += 1
+    assert replays >= 2
+    pol = s.get_policy()
+    G, pi = orc.pbvi_solve(md)
+    np.testing.assert_array_equal(bits(pol.gamma_array()), bits(G))
+    np.testing.assert_array_equal(pol.pi_array(), pi)
