@@ -1062,15 +1062,16 @@ int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsi
     const bool wantTc = (scoring == NOVA_SCORING_BF16 || scoring == NOVA_SCORING_FP16) && useProjNow &&
                         tc_supported(md) && nU >= kTcMinUnique && !tcUnavailable;
     // Tensor-core updates of large models read the table by candidate and by
-    // chosen alpha (assembly reads whole columns) and leave almost no row to
-    // the exact scan, so they use the state-contiguous layout; the exact scan
-    // reads whole rows and keeps the alpha-contiguous one, as do smaller
-    // models, whose tensor-core updates leave more rows to it.
+    // chosen alpha (assembly reads whole columns) and, in FP16, leave almost
+    // no row to the exact scan, so they use the state-contiguous layout; the
+    // exact scan reads whole rows and keeps the alpha-contiguous one, as do
+    // smaller models and updates after one that left more than 1 % of its
+    // rows to the scan (BF16's wider margin does).
     {
         const unsigned zc = md.z >= 16 ? 32u : 8u;
         const size_t smemSM = ((size_t)kProjTileS * md.ns * zc + (size_t)zc * 64 * (kProjTileS + 1)) * sizeof(float) +
                               (size_t)kProjTileS * md.ns * sizeof(int);
-        projStateMajor = wantTc && md.n > kStateMajorMinStates && smemSM <= 200 * 1024;
+        projStateMajor = wantTc && state_major_wanted(smemSM);
     }
     if (useProjNow && (rc = project(nU, fn)) != NOVA_SUCCESS) return rc;
     if (wantTc && tc == nullptr && tc_build(*this, fn) != NOVA_SUCCESS) tcUnavailable = true;
@@ -1082,6 +1083,7 @@ int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsi
         cudaEventRecord(ev[5], stream);
         stats.scoring = scoring;
         stats.rowsOverflow = nRows;
+        lastScanFrac = (float)nRows / (float)((size_t)md.m * md.z * md.r);
         if ((rc = scan_rows(rowList, nRows, nU, fn)) != NOVA_SUCCESS) return rc;
     } else if (useProjNow) {
         cudaEventRecord(ev[5], stream);
@@ -1118,6 +1120,11 @@ int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsi
     return NOVA_SUCCESS;
 }
 
+bool BackupEngine::state_major_wanted(size_t smemSM) const {
+    return md.n > kStateMajorMinStates && smemSM <= 200 * 1024 && scoring == NOVA_SCORING_FP16 &&
+           lastScanFrac <= 0.01f;
+}
+
 bool BackupEngine::fixed_ready() const {
     return tc != nullptr && !tcUnavailable && tc_schedule_fixed(*this) && Proj != nullptr && !projUnavailable &&
            projCap >= (size_t)md.m * md.z * std::max(projSCols, (size_t)md.n) * round_up(md.r, 32) &&
@@ -1137,7 +1144,7 @@ int BackupEngine::backup_fixed(const float *src, float *dst, unsigned *pi, const
         const unsigned zc = md.z >= 16 ? 32u : 8u;
         const size_t smemSM = ((size_t)kProjTileS * md.ns * zc + (size_t)zc * 64 * (kProjTileS + 1)) * sizeof(float) +
                               (size_t)kProjTileS * md.ns * sizeof(int);
-        projStateMajor = md.n > kStateMajorMinStates && smemSM <= 200 * 1024;
+        projStateMajor = state_major_wanted(smemSM);
     }
     if ((rc = project(nU, fn)) != NOVA_SUCCESS) return rc;
     if ((rc = tc_score_launch(*this, src, nU, false, fn)) != NOVA_SUCCESS) return rc;

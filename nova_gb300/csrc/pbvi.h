@@ -125,6 +125,8 @@ struct BackupEngine {
     bool identityUniq = false;     // uniqJ holds 0 .. r-1
     bool capturing = false;        // launches are being captured, not run
     bool projAttrDone = false;     // shared-memory attributes of the projection kernels set
+    float lastScanFrac = 0.0f;     // share of rows the last tensor-core update left to the exact scan
+    bool state_major_wanted(size_t smemSM) const;
     // Work list of `count` consecutive items starting at `first`.
     int fill_items(unsigned first, unsigned count, const char *fn);
     // Write the last backup's selections (action per belief, alpha per
