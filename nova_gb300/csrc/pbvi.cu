@@ -522,24 +522,25 @@ __global__ void __launch_bounds__(256) proj_kernel(DevModel md, const unsigned *
 
 // The same values in the state-contiguous layout [m][z][uRows][sCols]. One
 // block per (a, 8 consecutive states) and column range of the alphas
-// (blockIdx.y): warp w owns state s0 + w and its lanes two alphas of a
-// 64-alpha chunk (coalesced reads of the transposed alphas; the state's
+// (blockIdx.y): warp w owns state s0 + w and its lanes UPL alphas each of a
+// (32*UPL)-alpha chunk (coalesced reads of the transposed alphas; the state's
 // coefficients broadcast from shared memory). The chunk's results go through
 // shared memory so that each (o, u) column segment of the 8 states is written
 // as one 32-byte sector. The blocks of one column range run together, so its
 // part of the transposed alphas stays in L2.
 constexpr unsigned kProjTileS = 8;
 constexpr unsigned kStateMajorMinStates = 2048;
-template <int ZC>
-__global__ void __launch_bounds__(256) proj_state_major_kernel(DevModel md, const unsigned *__restrict__ succLen,
-                                                               const float *__restrict__ C1,
-                                                               const float *__restrict__ Gt, size_t gtCols,
-                                                               unsigned nU, float *__restrict__ Proj, size_t uRows,
-                                                               size_t sCols, unsigned uRange) {
+constexpr int kProjUPL = 2;  // alphas per lane of the state-contiguous projection
+template <int ZC, int UPL>
+__global__ void __launch_bounds__(256, UPL == 1 ? 3 : 2) proj_state_major_kernel(
+        DevModel md, const unsigned *__restrict__ succLen, const float *__restrict__ C1,
+        const float *__restrict__ Gt, size_t gtCols, unsigned nU, float *__restrict__ Proj, size_t uRows,
+        size_t sCols, unsigned uRange) {
+    constexpr unsigned CH = 32 * UPL;  // alphas per chunk
     extern __shared__ float smem[];
     float *Cs = smem;                                                     // [8][ns][ZC]
-    float *Out = Cs + (size_t)kProjTileS * md.ns * ZC;                    // [ZC][64][9]
-    int *Ss = reinterpret_cast<int *>(Out + (size_t)ZC * 64 * (kProjTileS + 1));  // [8][ns]
+    float *Out = Cs + (size_t)kProjTileS * md.ns * ZC;                    // [ZC][CH][9]
+    int *Ss = reinterpret_cast<int *>(Out + (size_t)ZC * CH * (kProjTileS + 1));  // [8][ns]
     const unsigned tilesS = (md.n + kProjTileS - 1) / kProjTileS;
     const unsigned a = blockIdx.x / tilesS, s0 = (blockIdx.x % tilesS) * kProjTileS;
     const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -563,46 +564,49 @@ __global__ void __launch_bounds__(256) proj_state_major_kernel(DevModel md, cons
         const float *cw = Cs + (size_t)warp * md.ns * ZC;
         const int *sw = Ss + warp * md.ns;
         const unsigned uBegin = blockIdx.y * uRange, uEnd = min(nU, uBegin + uRange);
-        for (unsigned u0 = uBegin; u0 < uEnd; u0 += 64) {
-            const unsigned ua = u0 + lane, ub = ua + 32;
-            const bool va = live && ua < uEnd, vb = live && ub < uEnd;
-            float acc0[ZC], acc1[ZC];
+        for (unsigned u0 = uBegin; u0 < uEnd; u0 += CH) {
+            bool v[UPL];
 #pragma unroll
-            for (int q = 0; q < ZC; q++) { acc0[q] = 0.0f; acc1[q] = 0.0f; }
+            for (int j = 0; j < UPL; j++) v[j] = live && u0 + lane + 32u * j < uEnd;
+            float acc[UPL][ZC];
+#pragma unroll
+            for (int j = 0; j < UPL; j++)
+#pragma unroll
+                for (int q = 0; q < ZC; q++) acc[j][q] = 0.0f;
             for (unsigned l = 0; l < L; l++) {
-                const float *grow = Gt + (size_t)sw[l] * gtCols;
-                const float g0 = va ? grow[ua] : 0.0f;
-                const float g1 = vb ? grow[ub] : 0.0f;
+                const float *grow = Gt + (size_t)sw[l] * gtCols + u0 + lane;
+                float g[UPL];
+#pragma unroll
+                for (int j = 0; j < UPL; j++) g[j] = v[j] ? grow[32 * j] : 0.0f;
                 const float4 *c4 = reinterpret_cast<const float4 *>(cw + l * ZC);
 #pragma unroll
                 for (int q4 = 0; q4 < ZC / 4; q4++) {
                     const float4 c = c4[q4];
-                    acc0[4 * q4 + 0] = fadd(acc0[4 * q4 + 0], fmul(c.x, g0));
-                    acc1[4 * q4 + 0] = fadd(acc1[4 * q4 + 0], fmul(c.x, g1));
-                    acc0[4 * q4 + 1] = fadd(acc0[4 * q4 + 1], fmul(c.y, g0));
-                    acc1[4 * q4 + 1] = fadd(acc1[4 * q4 + 1], fmul(c.y, g1));
-                    acc0[4 * q4 + 2] = fadd(acc0[4 * q4 + 2], fmul(c.z, g0));
-                    acc1[4 * q4 + 2] = fadd(acc1[4 * q4 + 2], fmul(c.z, g1));
-                    acc0[4 * q4 + 3] = fadd(acc0[4 * q4 + 3], fmul(c.w, g0));
-                    acc1[4 * q4 + 3] = fadd(acc1[4 * q4 + 3], fmul(c.w, g1));
+#pragma unroll
+                    for (int j = 0; j < UPL; j++) {
+                        acc[j][4 * q4 + 0] = fadd(acc[j][4 * q4 + 0], fmul(c.x, g[j]));
+                        acc[j][4 * q4 + 1] = fadd(acc[j][4 * q4 + 1], fmul(c.y, g[j]));
+                        acc[j][4 * q4 + 2] = fadd(acc[j][4 * q4 + 2], fmul(c.z, g[j]));
+                        acc[j][4 * q4 + 3] = fadd(acc[j][4 * q4 + 3], fmul(c.w, g[j]));
+                    }
                 }
             }
             __syncthreads();  // the previous chunk's columns have been written out
 #pragma unroll
-            for (int q = 0; q < ZC; q++) {
-                Out[((size_t)q * 64 + lane) * (kProjTileS + 1) + warp] = fmul(acc0[q], gamma);
-                Out[((size_t)q * 64 + lane + 32) * (kProjTileS + 1) + warp] = fmul(acc1[q], gamma);
-            }
+            for (int q = 0; q < ZC; q++)
+#pragma unroll
+                for (int j = 0; j < UPL; j++)
+                    Out[((size_t)q * CH + lane + 32 * j) * (kProjTileS + 1) + warp] = fmul(acc[j][q], gamma);
             __syncthreads();
             // 8 threads per (o, u) column segment: s0 .. s0+7.
             const unsigned ds = threadIdx.x % kProjTileS;
             const unsigned sOut = s0 + ds;
-            for (unsigned c = threadIdx.x / kProjTileS; c < zc * 64u; c += blockDim.x / kProjTileS) {
-                const unsigned q = c / 64, du = c % 64;
+            for (unsigned c = threadIdx.x / kProjTileS; c < zc * CH; c += blockDim.x / kProjTileS) {
+                const unsigned q = c / CH, du = c % CH;
                 const unsigned u = u0 + du;
                 if (u < uEnd && sOut < md.n)
                     Proj[(((size_t)a * md.z + o0 + q) * uRows + u) * sCols + sOut] =
-                        Out[((size_t)q * 64 + du) * (kProjTileS + 1) + ds];
+                        Out[((size_t)q * CH + du) * (kProjTileS + 1) + ds];
             }
         }
     }
@@ -936,24 +940,24 @@ bool BackupEngine::ensure_proj(unsigned nU) {
 int BackupEngine::project(unsigned nU, const char *fn) {
     if (projStateMajor) {
         const unsigned zc = md.z >= 16 ? 32u : 8u;
-        const size_t smem = ((size_t)kProjTileS * md.ns * zc + (size_t)zc * 64 * (kProjTileS + 1)) * sizeof(float) +
-                            (size_t)kProjTileS * md.ns * sizeof(int);
+        const size_t smem = ((size_t)kProjTileS * md.ns * zc + (size_t)zc * 32 * kProjUPL * (kProjTileS + 1)) *
+                                sizeof(float) + (size_t)kProjTileS * md.ns * sizeof(int);
         // Column ranges of about 32 MB of the transposed alphas (multiples of 64).
-        const unsigned uRange =
-            (unsigned)std::max<size_t>(64, ((32ull << 20) / ((size_t)md.n * sizeof(float))) / 64 * 64);
+        const unsigned uRange = (unsigned)std::max<size_t>(
+            32 * kProjUPL, ((32ull << 20) / ((size_t)md.n * sizeof(float))) / (32 * kProjUPL) * (32 * kProjUPL));
         const dim3 blocks(md.m * ceil_div(md.n, kProjTileS), ceil_div(std::max(nU, 1u), uRange));
         if (!projAttrDone) {
-            cudaFuncSetAttribute(proj_state_major_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-            cudaFuncSetAttribute(proj_state_major_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(proj_state_major_kernel<32, kProjUPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(proj_state_major_kernel<8, kProjUPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
             cudaFuncSetAttribute(proj_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
             cudaFuncSetAttribute(proj_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
             projAttrDone = true;
         }
         if (zc == 32) {
-            proj_state_major_kernel<32><<<blocks, 256, smem, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj,
+            proj_state_major_kernel<32, kProjUPL><<<blocks, 256, smem, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj,
                                                                        projCols, projSCols, uRange);
         } else {
-            proj_state_major_kernel<8><<<blocks, 256, smem, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj,
+            proj_state_major_kernel<8, kProjUPL><<<blocks, 256, smem, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj,
                                                                       projCols, projSCols, uRange);
         }
         return check_launch(fn, "projection table");
@@ -961,8 +965,8 @@ int BackupEngine::project(unsigned nU, const char *fn) {
     const size_t smem32 = (size_t)md.ns * 32 * sizeof(float) + md.ns * sizeof(int);
     const unsigned blocks = md.m * md.n;
     if (!projAttrDone) {
-        cudaFuncSetAttribute(proj_state_major_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(proj_state_major_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(proj_state_major_kernel<32, kProjUPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(proj_state_major_kernel<8, kProjUPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cudaFuncSetAttribute(proj_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cudaFuncSetAttribute(proj_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         projAttrDone = true;
@@ -1069,8 +1073,8 @@ int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsi
     // rows to the scan (BF16's wider margin does).
     {
         const unsigned zc = md.z >= 16 ? 32u : 8u;
-        const size_t smemSM = ((size_t)kProjTileS * md.ns * zc + (size_t)zc * 64 * (kProjTileS + 1)) * sizeof(float) +
-                              (size_t)kProjTileS * md.ns * sizeof(int);
+        const size_t smemSM = ((size_t)kProjTileS * md.ns * zc + (size_t)zc * 32 * kProjUPL * (kProjTileS + 1)) *
+                                  sizeof(float) + (size_t)kProjTileS * md.ns * sizeof(int);
         projStateMajor = wantTc && state_major_wanted(smemSM);
     }
     if (useProjNow && (rc = project(nU, fn)) != NOVA_SUCCESS) return rc;
@@ -1142,8 +1146,8 @@ int BackupEngine::backup_fixed(const float *src, float *dst, unsigned *pi, const
     if (!useProjNow) return NOVA_ERROR_KERNEL_EXECUTION;
     {
         const unsigned zc = md.z >= 16 ? 32u : 8u;
-        const size_t smemSM = ((size_t)kProjTileS * md.ns * zc + (size_t)zc * 64 * (kProjTileS + 1)) * sizeof(float) +
-                              (size_t)kProjTileS * md.ns * sizeof(int);
+        const size_t smemSM = ((size_t)kProjTileS * md.ns * zc + (size_t)zc * 32 * kProjUPL * (kProjTileS + 1)) *
+                                  sizeof(float) + (size_t)kProjTileS * md.ns * sizeof(int);
         projStateMajor = state_major_wanted(smemSM);
     }
     if ((rc = project(nU, fn)) != NOVA_SUCCESS) return rc;
