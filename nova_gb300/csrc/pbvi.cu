@@ -454,6 +454,29 @@ __global__ void argmax_fp64_kernel(const double *__restrict__ v, unsigned rows, 
 // Projection table: Proj[a][o][s][u] = gamma * sum_l fl(O(a,S,o) T(s,a,l)) * alpha_u(S)
 // ---------------------------------------------------------------------------
 
+// Packed pairs of FP32 values (element 0 in the low word): the sm_100-family
+// f32x2 multiply rounds each element exactly as the scalar multiply.
+__device__ __forceinline__ unsigned long long pack_f32x2(float lo, float hi) {
+    unsigned long long d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+    return d;
+}
+__device__ __forceinline__ unsigned long long mul_f32x2(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long fma_f32x2(unsigned long long a, unsigned long long b,
+                                                       unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ float f32x2_part(unsigned long long v, int hi) {
+    return __uint_as_float(hi ? (unsigned)(v >> 32) : (unsigned)v);
+}
+
+
 // The reference recomputes this value (its Vtk after `Vtk *= gamma`,
 // pomdp_pbvi_cpu.cpp:66-74 and :89-98) for every belief that has s in its
 // support; it depends only on (a, o, s, alpha), so it is computed once per
@@ -465,8 +488,9 @@ template <int ZC>
 __global__ void __launch_bounds__(256) proj_kernel(DevModel md, const unsigned *__restrict__ succLen,
                                                    const float *__restrict__ C1, const float *__restrict__ Gt,
                                                    size_t gtCols, unsigned nU, float *__restrict__ Proj,
-                                                   size_t uCols) {
+                                                   size_t uCols, float one) {
     extern __shared__ float smem[];
+    const unsigned long long one2 = pack_f32x2(one, one);
     float *Cs = smem;                                           // [ns][ZC]
     int *Ss = reinterpret_cast<int *>(Cs + (size_t)md.ns * ZC); // [ns]
     const unsigned a = blockIdx.x / md.n, s = blockIdx.x % md.n;
@@ -488,32 +512,32 @@ __global__ void __launch_bounds__(256) proj_kernel(DevModel md, const unsigned *
         for (unsigned u0 = 0; u0 < nU; u0 += 2 * blockDim.x) {
             const unsigned ua = u0 + threadIdx.x, ub = ua + blockDim.x;
             const bool va = ua < nU, vb = ub < nU;
-            float acc0[ZC], acc1[ZC];
+            // Observation pairs (q, q+1) per instruction, with the exact
+            // f32x2 form of fadd(acc, fmul(c, g)) described at
+            // proj_state_major_kernel.
+            unsigned long long acc0[ZC / 2], acc1[ZC / 2];
 #pragma unroll
-            for (int q = 0; q < ZC; q++) { acc0[q] = 0.0f; acc1[q] = 0.0f; }
+            for (int q = 0; q < ZC / 2; q++) { acc0[q] = 0ull; acc1[q] = 0ull; }
             for (unsigned l = 0; l < L; l++) {
                 const float *grow = Gt + (size_t)Ss[l] * gtCols;
                 const float g0 = va ? grow[ua] : 0.0f;
                 const float g1 = vb ? grow[ub] : 0.0f;
-                const float4 *c4 = reinterpret_cast<const float4 *>(Cs + l * ZC);
+                const unsigned long long gg0 = pack_f32x2(g0, g0), gg1 = pack_f32x2(g1, g1);
+                const ulonglong2 *c2 = reinterpret_cast<const ulonglong2 *>(Cs + l * ZC);
 #pragma unroll
                 for (int q4 = 0; q4 < ZC / 4; q4++) {
-                    const float4 c = c4[q4];
-                    acc0[4 * q4 + 0] = fadd(acc0[4 * q4 + 0], fmul(c.x, g0));
-                    acc1[4 * q4 + 0] = fadd(acc1[4 * q4 + 0], fmul(c.x, g1));
-                    acc0[4 * q4 + 1] = fadd(acc0[4 * q4 + 1], fmul(c.y, g0));
-                    acc1[4 * q4 + 1] = fadd(acc1[4 * q4 + 1], fmul(c.y, g1));
-                    acc0[4 * q4 + 2] = fadd(acc0[4 * q4 + 2], fmul(c.z, g0));
-                    acc1[4 * q4 + 2] = fadd(acc1[4 * q4 + 2], fmul(c.z, g1));
-                    acc0[4 * q4 + 3] = fadd(acc0[4 * q4 + 3], fmul(c.w, g0));
-                    acc1[4 * q4 + 3] = fadd(acc1[4 * q4 + 3], fmul(c.w, g1));
+                    const ulonglong2 c = c2[q4];
+                    acc0[2 * q4 + 0] = fma_f32x2(mul_f32x2(c.x, gg0), one2, acc0[2 * q4 + 0]);
+                    acc1[2 * q4 + 0] = fma_f32x2(mul_f32x2(c.x, gg1), one2, acc1[2 * q4 + 0]);
+                    acc0[2 * q4 + 1] = fma_f32x2(mul_f32x2(c.y, gg0), one2, acc0[2 * q4 + 1]);
+                    acc1[2 * q4 + 1] = fma_f32x2(mul_f32x2(c.y, gg1), one2, acc1[2 * q4 + 1]);
                 }
             }
 #pragma unroll
             for (int q = 0; q < ZC; q++) {
                 if ((unsigned)q < zc) {
-                    if (va) out[(size_t)q * oStride + ua] = fmul(acc0[q], gamma);
-                    if (vb) out[(size_t)q * oStride + ub] = fmul(acc1[q], gamma);
+                    if (va) out[(size_t)q * oStride + ua] = fmul(f32x2_part(acc0[q / 2], q & 1), gamma);
+                    if (vb) out[(size_t)q * oStride + ub] = fmul(f32x2_part(acc1[q / 2], q & 1), gamma);
                 }
             }
         }
@@ -535,8 +559,9 @@ template <int ZC, int UPL>
 __global__ void __launch_bounds__(256, UPL == 1 ? 3 : 2) proj_state_major_kernel(
         DevModel md, const unsigned *__restrict__ succLen, const float *__restrict__ C1,
         const float *__restrict__ Gt, size_t gtCols, unsigned nU, float *__restrict__ Proj, size_t uRows,
-        size_t sCols, unsigned uRange) {
+        size_t sCols, unsigned uRange, float one) {
     constexpr unsigned CH = 32 * UPL;  // alphas per chunk
+    const unsigned long long one2 = pack_f32x2(one, one);
     extern __shared__ float smem[];
     float *Cs = smem;                                                     // [8][ns][ZC]
     float *Out = Cs + (size_t)kProjTileS * md.ns * ZC;                    // [ZC][CH][9]
@@ -568,26 +593,47 @@ __global__ void __launch_bounds__(256, UPL == 1 ? 3 : 2) proj_state_major_kernel
             bool v[UPL];
 #pragma unroll
             for (int j = 0; j < UPL; j++) v[j] = live && u0 + lane + 32u * j < uEnd;
-            float acc[UPL][ZC];
+            // Two observations (q, q+1) per instruction: an f32x2 multiply
+            // (each element rounded as the scalar multiply rounds it), then
+            // the sum as an f32x2 fused multiply-add of the product by 1.0:
+            // p * 1 is exact, so fma(p, 1, acc) is the correctly rounded
+            // acc + p. (A plain f32x2 add that consumes an f32x2 product is
+            // contracted by the compiler into one fused multiply-add, which
+            // would skip the product's rounding; the factor 1.0 arrives as a
+            // kernel argument, so it cannot be folded away.)
+            unsigned long long acc[UPL][ZC / 2];
 #pragma unroll
             for (int j = 0; j < UPL; j++)
 #pragma unroll
-                for (int q = 0; q < ZC; q++) acc[j][q] = 0.0f;
+                for (int q = 0; q < ZC / 2; q++) acc[j][q] = 0ull;
+            // The next successor's alpha values are loaded before this one's
+            // products (the last iteration reloads its own), so the gathers
+            // overlap the arithmetic.
+            float gn[UPL];
+            if (L > 0) {
+                const float *grow = Gt + (size_t)sw[0] * gtCols + u0 + lane;
+#pragma unroll
+                for (int j = 0; j < UPL; j++) gn[j] = v[j] ? grow[32 * j] : 0.0f;
+            }
             for (unsigned l = 0; l < L; l++) {
-                const float *grow = Gt + (size_t)sw[l] * gtCols + u0 + lane;
                 float g[UPL];
 #pragma unroll
-                for (int j = 0; j < UPL; j++) g[j] = v[j] ? grow[32 * j] : 0.0f;
-                const float4 *c4 = reinterpret_cast<const float4 *>(cw + l * ZC);
+                for (int j = 0; j < UPL; j++) g[j] = gn[j];
+                const unsigned ln = l + 1 < L ? l + 1 : l;
+                const float *grow = Gt + (size_t)sw[ln] * gtCols + u0 + lane;
+#pragma unroll
+                for (int j = 0; j < UPL; j++) gn[j] = v[j] ? grow[32 * j] : 0.0f;
+                unsigned long long gg[UPL];
+#pragma unroll
+                for (int j = 0; j < UPL; j++) gg[j] = pack_f32x2(g[j], g[j]);
+                const ulonglong2 *c2 = reinterpret_cast<const ulonglong2 *>(cw + l * ZC);
 #pragma unroll
                 for (int q4 = 0; q4 < ZC / 4; q4++) {
-                    const float4 c = c4[q4];
+                    const ulonglong2 c = c2[q4];
 #pragma unroll
                     for (int j = 0; j < UPL; j++) {
-                        acc[j][4 * q4 + 0] = fadd(acc[j][4 * q4 + 0], fmul(c.x, g[j]));
-                        acc[j][4 * q4 + 1] = fadd(acc[j][4 * q4 + 1], fmul(c.y, g[j]));
-                        acc[j][4 * q4 + 2] = fadd(acc[j][4 * q4 + 2], fmul(c.z, g[j]));
-                        acc[j][4 * q4 + 3] = fadd(acc[j][4 * q4 + 3], fmul(c.w, g[j]));
+                        acc[j][2 * q4 + 0] = fma_f32x2(mul_f32x2(c.x, gg[j]), one2, acc[j][2 * q4 + 0]);
+                        acc[j][2 * q4 + 1] = fma_f32x2(mul_f32x2(c.y, gg[j]), one2, acc[j][2 * q4 + 1]);
                     }
                 }
             }
@@ -596,7 +642,8 @@ __global__ void __launch_bounds__(256, UPL == 1 ? 3 : 2) proj_state_major_kernel
             for (int q = 0; q < ZC; q++)
 #pragma unroll
                 for (int j = 0; j < UPL; j++)
-                    Out[((size_t)q * CH + lane + 32 * j) * (kProjTileS + 1) + warp] = fmul(acc[j][q], gamma);
+                    Out[((size_t)q * CH + lane + 32 * j) * (kProjTileS + 1) + warp] =
+                        fmul(f32x2_part(acc[j][q / 2], q & 1), gamma);
             __syncthreads();
             // 8 threads per (o, u) column segment: s0 .. s0+7.
             const unsigned ds = threadIdx.x % kProjTileS;
@@ -955,10 +1002,10 @@ int BackupEngine::project(unsigned nU, const char *fn) {
         }
         if (zc == 32) {
             proj_state_major_kernel<32, kProjUPL><<<blocks, 256, smem, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj,
-                                                                       projCols, projSCols, uRange);
+                                                                       projCols, projSCols, uRange, 1.0f);
         } else {
             proj_state_major_kernel<8, kProjUPL><<<blocks, 256, smem, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj,
-                                                                      projCols, projSCols, uRange);
+                                                                      projCols, projSCols, uRange, 1.0f);
         }
         return check_launch(fn, "projection table");
     }
@@ -972,10 +1019,10 @@ int BackupEngine::project(unsigned nU, const char *fn) {
         projAttrDone = true;
     }
     if (md.z >= 16 && smem32 <= 200 * 1024) {
-        proj_kernel<32><<<blocks, 256, smem32, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj, projCols);
+        proj_kernel<32><<<blocks, 256, smem32, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj, projCols, 1.0f);
     } else {
         const size_t smem8 = (size_t)md.ns * 8 * sizeof(float) + md.ns * sizeof(int);
-        proj_kernel<8><<<blocks, 256, smem8, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj, projCols);
+        proj_kernel<8><<<blocks, 256, smem8, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj, projCols, 1.0f);
     }
     return check_launch(fn, "projection table");
 }
