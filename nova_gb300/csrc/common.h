@@ -81,5 +81,31 @@ namespace nova_gb300 {
 // every product and every sum, and matching those bits requires the same.
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+
+// Packed pairs of FP32 values (element 0 in the low word): the sm_100-family
+// f32x2 multiply rounds each element exactly as the scalar multiply. For the
+// sum use fma_f32x2(p, one, acc) with one = 1.0 passed in at run time: p * 1
+// is exact, so the result is the correctly rounded acc + p, whereas an
+// add.rn.f32x2 that consumes an f32x2 product is contracted by the compiler
+// into one fused multiply-add (the product's rounding skipped).
+__device__ __forceinline__ unsigned long long pack_f32x2(float lo, float hi) {
+    unsigned long long d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+    return d;
+}
+__device__ __forceinline__ unsigned long long mul_f32x2(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long fma_f32x2(unsigned long long a, unsigned long long b,
+                                                       unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ float f32x2_part(unsigned long long v, int hi) {
+    return __uint_as_float(hi ? (unsigned)(v >> 32) : (unsigned)v);
+}
 }  // namespace nova_gb300
 #endif

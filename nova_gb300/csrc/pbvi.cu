@@ -454,27 +454,6 @@ __global__ void argmax_fp64_kernel(const double *__restrict__ v, unsigned rows, 
 // Projection table: Proj[a][o][s][u] = gamma * sum_l fl(O(a,S,o) T(s,a,l)) * alpha_u(S)
 // ---------------------------------------------------------------------------
 
-// Packed pairs of FP32 values (element 0 in the low word): the sm_100-family
-// f32x2 multiply rounds each element exactly as the scalar multiply.
-__device__ __forceinline__ unsigned long long pack_f32x2(float lo, float hi) {
-    unsigned long long d;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
-    return d;
-}
-__device__ __forceinline__ unsigned long long mul_f32x2(unsigned long long a, unsigned long long b) {
-    unsigned long long d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ unsigned long long fma_f32x2(unsigned long long a, unsigned long long b,
-                                                       unsigned long long c) {
-    unsigned long long d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-__device__ __forceinline__ float f32x2_part(unsigned long long v, int hi) {
-    return __uint_as_float(hi ? (unsigned)(v >> 32) : (unsigned)v);
-}
 
 
 // The reference recomputes this value (its Vtk after `Vtk *= gamma`,

@@ -12,7 +12,8 @@
 // thread owns a 4 x 4 block of (belief, alpha) sums and adds its terms in
 // state order with separately rounded products and sums, so each V_i has the
 // reference's bits; tiles of 32 states of both operands are staged in shared
-// memory. The epilogue keeps, per belief and alpha tile, the best V and its
+// memory. Two alphas per instruction: f32x2 products, summed with the exact
+// f32x2 form (fma of the product by a run-time 1.0). The epilogue keeps, per belief and alpha tile, the best V and its
 // lowest index; a second pass merges the tiles in alpha order.
 
 #include "common.h"
@@ -36,7 +37,8 @@ constexpr unsigned kNone = 0xffffffffu;
 __global__ void __launch_bounds__(kThreads) value_tiles_kernel(const float *__restrict__ G, unsigned r, unsigned n,
                                                                const float *__restrict__ Bd, unsigned count,
                                                                float *__restrict__ partV,
-                                                               unsigned *__restrict__ partI, unsigned aTiles) {
+                                                               unsigned *__restrict__ partI, unsigned aTiles,
+                                                               float one) {
     // State-major tiles, belief (alpha) contiguous; rows padded by 4 floats so
     // the staging stores spread over the banks and rows stay 16-byte aligned.
     __shared__ __align__(16) float sB[TK][TB + 4];
@@ -44,11 +46,10 @@ __global__ void __launch_bounds__(kThreads) value_tiles_kernel(const float *__re
     const unsigned tid = threadIdx.x;
     const unsigned tx = tid % 16, ty = tid / 16;  // alpha group, belief group
     const unsigned b0 = blockIdx.y * TB, a0 = blockIdx.x * TA;
-    float acc[4][4];
+    const unsigned long long one2 = pack_f32x2(one, one);
+    unsigned long long acc2[4][2];  // (alpha 4tx+2p, 4tx+2p+1) per belief row i
 #pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++) acc[i][j] = 0.0f;
+    for (int i = 0; i < 4; i++) { acc2[i][0] = 0ull; acc2[i][1] = 0ull; }
     for (unsigned k0 = 0; k0 < n; k0 += TK) {
         // Stage TK states of TB beliefs and TA alphas (zeros past the ends,
         // which are never added: the state loop stops at n, and rows past
@@ -76,16 +77,22 @@ __global__ void __launch_bounds__(kThreads) value_tiles_kernel(const float *__re
         const unsigned kEnd = min(TK, n - k0);
         for (unsigned kk = 0; kk < kEnd; kk++) {
             const float4 bv = *reinterpret_cast<const float4 *>(&sB[kk][4 * ty]);
-            const float4 gv = *reinterpret_cast<const float4 *>(&sG[kk][4 * tx]);
+            const ulonglong2 gv = *reinterpret_cast<const ulonglong2 *>(&sG[kk][4 * tx]);
             const float bq[4] = {bv.x, bv.y, bv.z, bv.w};
-            const float gq[4] = {gv.x, gv.y, gv.z, gv.w};
 #pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int j = 0; j < 4; j++) acc[i][j] = fadd(acc[i][j], fmul(gq[j], bq[i]));
+            for (int i = 0; i < 4; i++) {
+                const unsigned long long bb = pack_f32x2(bq[i], bq[i]);
+                acc2[i][0] = fma_f32x2(mul_f32x2(gv.x, bb), one2, acc2[i][0]);
+                acc2[i][1] = fma_f32x2(mul_f32x2(gv.y, bb), one2, acc2[i][1]);
+            }
         }
         __syncthreads();
     }
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = f32x2_part(acc2[i][j / 2], j & 1);
     // Best alpha of this tile per belief: the 16 threads of a belief group
     // hold 4 alphas each; reduce with shuffles (max value, then lowest index).
 #pragma unroll
@@ -139,7 +146,8 @@ static int value_batched(const float *dG, const unsigned *dPi, unsigned r, unsig
         cudaFree(partV);
         return rc;
     }
-    value_tiles_kernel<<<dim3(aTiles, ceil_div(count, TB)), kThreads>>>(dG, r, n, dB, count, partV, partI, aTiles);
+    value_tiles_kernel<<<dim3(aTiles, ceil_div(count, TB)), kThreads>>>(dG, r, n, dB, count, partV, partI, aTiles,
+                                                                        1.0f);
     rc = check_launch(fn, "belief values");
     if (rc == NOVA_SUCCESS) {
         value_merge_kernel<<<ceil_div(count, 256), 256>>>(count, aTiles, partV, partI, dPi, dV, dA);
