@@ -1241,8 +1241,15 @@ struct PbviCpuWorkspace : Workspace {
     unsigned *pi = nullptr;
     float *hostGamma = nullptr, *hostGammaPrime = nullptr;
     unsigned *hostPi = nullptr;
+    bool hostPinned = false;  // the three host arrays are page-locked (cudaHostRegister)
     ~PbviCpuWorkspace() override {
         cudaDeviceSynchronize();
+        if (hostPinned) {
+            cudaHostUnregister(hostGamma);
+            cudaHostUnregister(hostGammaPrime);
+            cudaHostUnregister(hostPi);
+            cudaGetLastError();
+        }
         cudaFree(S); cudaFree(T); cudaFree(O); cudaFree(R); cudaFree(Z); cudaFree(B);
         cudaFree(Gamma); cudaFree(GammaPrime); cudaFree(pi);
     }
@@ -1707,10 +1714,12 @@ extern "C" int pomdp_pbvi_initialize_cpu(const POMDP *pomdp, POMDPPBVICPU *pbvi)
         auto *old = find_workspace<PbviCpuWorkspace>(pbvi);
         if (old != nullptr) {
             scoring = old->eng.scoring;
-            if (pbvi->Gamma == old->hostGamma) { delete[] pbvi->Gamma; pbvi->Gamma = nullptr; }
-            if (pbvi->GammaPrime == old->hostGammaPrime) { delete[] pbvi->GammaPrime; pbvi->GammaPrime = nullptr; }
-            if (pbvi->pi == old->hostPi) { delete[] pbvi->pi; pbvi->pi = nullptr; }
-            registry().erase(pbvi);
+            const bool ownG = pbvi->Gamma == old->hostGamma, ownGP = pbvi->GammaPrime == old->hostGammaPrime,
+                       ownPi = pbvi->pi == old->hostPi;
+            registry().erase(pbvi);  // unpins the arrays it made
+            if (ownG) { delete[] pbvi->Gamma; pbvi->Gamma = nullptr; }
+            if (ownGP) { delete[] pbvi->GammaPrime; pbvi->GammaPrime = nullptr; }
+            if (ownPi) { delete[] pbvi->pi; pbvi->pi = nullptr; }
         }
     }
     const size_t rn = (size_t)pomdp->r * pomdp->n;
@@ -1724,6 +1733,22 @@ extern "C" int pomdp_pbvi_initialize_cpu(const POMDP *pomdp, POMDPPBVICPU *pbvi)
     std::unique_ptr<PbviCpuWorkspace> ws(new PbviCpuWorkspace());
     ws->eng.scoring = scoring;
     ws->hostGamma = pbvi->Gamma; ws->hostGammaPrime = pbvi->GammaPrime; ws->hostPi = pbvi->pi;
+    // Page-locked in place (they stay new[] arrays, as the reference's
+    // callers expect), so each update's host copies run at full link speed;
+    // without it the copies are staged, with the same results.
+    if (cudaHostRegister(pbvi->Gamma, rn * sizeof(float), cudaHostRegisterDefault) == cudaSuccess) {
+        if (cudaHostRegister(pbvi->GammaPrime, rn * sizeof(float), cudaHostRegisterDefault) == cudaSuccess) {
+            if (cudaHostRegister(pbvi->pi, pomdp->r * sizeof(unsigned), cudaHostRegisterDefault) == cudaSuccess) {
+                ws->hostPinned = true;
+            } else {
+                cudaHostUnregister(pbvi->GammaPrime);
+                cudaHostUnregister(pbvi->Gamma);
+            }
+        } else {
+            cudaHostUnregister(pbvi->Gamma);
+        }
+    }
+    cudaGetLastError();
     std::lock_guard<std::mutex> lock(registry_mutex());
     registry()[pbvi] = std::move(ws);
     return NOVA_SUCCESS;
