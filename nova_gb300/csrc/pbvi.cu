@@ -493,7 +493,7 @@ __global__ void __launch_bounds__(256) proj_kernel(DevModel md, const unsigned *
             const bool va = ua < nU, vb = ub < nU;
             // Observation pairs (q, q+1) per instruction, with the exact
             // f32x2 form of fadd(acc, fmul(c, g)) described at
-            // proj_state_major_kernel.
+            // common.h (fma of the product by a run-time 1.0).
             unsigned long long acc0[ZC / 2], acc1[ZC / 2];
 #pragma unroll
             for (int q = 0; q < ZC / 2; q++) { acc0[q] = 0ull; acc1[q] = 0ull; }
@@ -523,88 +523,82 @@ __global__ void __launch_bounds__(256) proj_kernel(DevModel md, const unsigned *
     }
 }
 
-// The same values in the state-contiguous layout [m][z][uRows][sCols]. One
-// block per (a, 8 consecutive states) and column range of the alphas
-// (blockIdx.y): warp w owns state s0 + w and its lanes UPL alphas each of a
-// (32*UPL)-alpha chunk (coalesced reads of the transposed alphas; the state's
-// coefficients broadcast from shared memory). The chunk's results go through
-// shared memory so that each (o, u) column segment of the 8 states is written
-// as one 32-byte sector. The blocks of one column range run together, so its
-// part of the transposed alphas stays in L2.
+// The state-contiguous layout [m][z][uRows][sCols] (see proj_state_lanes_kernel).
 constexpr unsigned kProjTileS = 8;
 constexpr unsigned kStateMajorMinStates = 2048;
 constexpr int kProjUPL = 2;  // alphas per lane of the state-contiguous projection
+
+// State-contiguous table, register form: one block per (a, 8 consecutive
+// states) and column range of the alphas; lane (sl, ul) of every warp owns
+// state s0 + sl and UPL alphas (the block's 8 warps cover 32*UPL alphas per
+// step). Each lane reads its state's coefficients from shared memory
+// (per-state blocks padded by 4 floats, so the 8 states of a warp fall in
+// distinct banks) and keeps 32 observations' sums in registers; for every
+// (o, alpha) the 8 lanes of one alpha write the 8 states' values as one
+// 32-byte sector, straight from registers.
 template <int ZC, int UPL>
-__global__ void __launch_bounds__(256, UPL == 1 ? 3 : 2) proj_state_major_kernel(
+__global__ void __launch_bounds__(256, UPL == 1 ? 3 : 2) proj_state_lanes_kernel(
         DevModel md, const unsigned *__restrict__ succLen, const float *__restrict__ C1,
         const float *__restrict__ Gt, size_t gtCols, unsigned nU, float *__restrict__ Proj, size_t uRows,
         size_t sCols, unsigned uRange, float one) {
-    constexpr unsigned CH = 32 * UPL;  // alphas per chunk
-    const unsigned long long one2 = pack_f32x2(one, one);
     extern __shared__ float smem[];
-    float *Cs = smem;                                                     // [8][ns][ZC]
-    float *Out = Cs + (size_t)kProjTileS * md.ns * ZC;                    // [ZC][CH][9]
-    int *Ss = reinterpret_cast<int *>(Out + (size_t)ZC * CH * (kProjTileS + 1));  // [8][ns]
+    const unsigned cStride = md.ns * ZC + 4;
+    float *Cs = smem;                                                   // [8][cStride]
+    int *Ss = reinterpret_cast<int *>(Cs + (size_t)kProjTileS * cStride);  // [8][ns]
+    __shared__ unsigned Ls[kProjTileS];
+    const unsigned long long one2 = pack_f32x2(one, one);
     const unsigned tilesS = (md.n + kProjTileS - 1) / kProjTileS;
     const unsigned a = blockIdx.x / tilesS, s0 = (blockIdx.x % tilesS) * kProjTileS;
     const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const unsigned s = s0 + warp;
+    const unsigned sl = lane >> 2, ul = lane & 3;
+    const unsigned s = s0 + sl;
     const bool live = s < md.n;
-    const unsigned L = live ? succLen[(size_t)s * md.m + a] : 0u;
     const float gamma = md.gamma;
-    for (unsigned e = lane; e < L; e += 32) Ss[warp * md.ns + e] = md.S[((size_t)s * md.m + a) * md.ns + e];
+    if (threadIdx.x < kProjTileS)
+        Ls[threadIdx.x] = s0 + threadIdx.x < md.n ? succLen[(size_t)(s0 + threadIdx.x) * md.m + a] : 0u;
+    for (unsigned e = threadIdx.x; e < kProjTileS * md.ns; e += blockDim.x) {
+        const unsigned st = e / md.ns, l = e % md.ns;
+        Ss[e] = s0 + st < md.n ? md.S[((size_t)(s0 + st) * md.m + a) * md.ns + l] : 0;
+    }
     for (unsigned o0 = 0; o0 < md.z; o0 += ZC) {
         __syncthreads();
-        if (live) {
-            const float *crow = C1 + (((size_t)a * md.n + s) * md.ns) * md.z + o0;
-            float *cw = Cs + (size_t)warp * md.ns * ZC;
-            for (unsigned e = lane; e < L * ZC; e += 32) {
-                const unsigned l = e / ZC, q = e % ZC;
-                cw[e] = (o0 + q < md.z) ? crow[(size_t)l * md.z + q] : 0.0f;
-            }
+        for (unsigned e = threadIdx.x; e < kProjTileS * md.ns * ZC; e += blockDim.x) {
+            const unsigned st = e / (md.ns * ZC), rem = e % (md.ns * ZC), l = rem / ZC, q = rem % ZC;
+            Cs[st * cStride + rem] = (s0 + st < md.n && l < Ls[st] && o0 + q < md.z)
+                ? C1[(((size_t)a * md.n + s0 + st) * md.ns + l) * md.z + o0 + q] : 0.0f;
         }
         __syncthreads();
         const unsigned zc = min((unsigned)ZC, md.z - o0);
-        const float *cw = Cs + (size_t)warp * md.ns * ZC;
-        const int *sw = Ss + warp * md.ns;
+        const unsigned L = Ls[sl];
+        const float *cw = Cs + (size_t)sl * cStride;
+        const int *sw = Ss + sl * md.ns;
         const unsigned uBegin = blockIdx.y * uRange, uEnd = min(nU, uBegin + uRange);
-        for (unsigned u0 = uBegin; u0 < uEnd; u0 += CH) {
+        for (unsigned u0 = uBegin + warp * 4u * UPL; u0 < uEnd; u0 += 32u * UPL) {
+            unsigned uu[UPL];
             bool v[UPL];
 #pragma unroll
-            for (int j = 0; j < UPL; j++) v[j] = live && u0 + lane + 32u * j < uEnd;
-            // Two observations (q, q+1) per instruction: an f32x2 multiply
-            // (each element rounded as the scalar multiply rounds it), then
-            // the sum as an f32x2 fused multiply-add of the product by 1.0:
-            // p * 1 is exact, so fma(p, 1, acc) is the correctly rounded
-            // acc + p. (A plain f32x2 add that consumes an f32x2 product is
-            // contracted by the compiler into one fused multiply-add, which
-            // would skip the product's rounding; the factor 1.0 arrives as a
-            // kernel argument, so it cannot be folded away.)
+            for (int j = 0; j < UPL; j++) {
+                uu[j] = u0 + ul + 4u * j;
+                v[j] = live && uu[j] < uEnd;
+            }
             unsigned long long acc[UPL][ZC / 2];
 #pragma unroll
             for (int j = 0; j < UPL; j++)
 #pragma unroll
                 for (int q = 0; q < ZC / 2; q++) acc[j][q] = 0ull;
-            // The next successor's alpha values are loaded before this one's
-            // products (the last iteration reloads its own), so the gathers
-            // overlap the arithmetic.
             float gn[UPL];
             if (L > 0) {
-                const float *grow = Gt + (size_t)sw[0] * gtCols + u0 + lane;
+                const float *grow = Gt + (size_t)sw[0] * gtCols;
 #pragma unroll
-                for (int j = 0; j < UPL; j++) gn[j] = v[j] ? grow[32 * j] : 0.0f;
+                for (int j = 0; j < UPL; j++) gn[j] = v[j] ? grow[uu[j]] : 0.0f;
             }
             for (unsigned l = 0; l < L; l++) {
-                float g[UPL];
-#pragma unroll
-                for (int j = 0; j < UPL; j++) g[j] = gn[j];
-                const unsigned ln = l + 1 < L ? l + 1 : l;
-                const float *grow = Gt + (size_t)sw[ln] * gtCols + u0 + lane;
-#pragma unroll
-                for (int j = 0; j < UPL; j++) gn[j] = v[j] ? grow[32 * j] : 0.0f;
                 unsigned long long gg[UPL];
 #pragma unroll
-                for (int j = 0; j < UPL; j++) gg[j] = pack_f32x2(g[j], g[j]);
+                for (int j = 0; j < UPL; j++) gg[j] = pack_f32x2(gn[j], gn[j]);
+                const float *grow = Gt + (size_t)sw[l + 1 < L ? l + 1 : l] * gtCols;
+#pragma unroll
+                for (int j = 0; j < UPL; j++) gn[j] = v[j] ? grow[uu[j]] : 0.0f;
                 const ulonglong2 *c2 = reinterpret_cast<const ulonglong2 *>(cw + l * ZC);
 #pragma unroll
                 for (int q4 = 0; q4 < ZC / 4; q4++) {
@@ -616,23 +610,15 @@ __global__ void __launch_bounds__(256, UPL == 1 ? 3 : 2) proj_state_major_kernel
                     }
                 }
             }
-            __syncthreads();  // the previous chunk's columns have been written out
 #pragma unroll
-            for (int q = 0; q < ZC; q++)
+            for (int q = 0; q < ZC; q++) {
+                if ((unsigned)q < zc) {
 #pragma unroll
-                for (int j = 0; j < UPL; j++)
-                    Out[((size_t)q * CH + lane + 32 * j) * (kProjTileS + 1) + warp] =
-                        fmul(f32x2_part(acc[j][q / 2], q & 1), gamma);
-            __syncthreads();
-            // 8 threads per (o, u) column segment: s0 .. s0+7.
-            const unsigned ds = threadIdx.x % kProjTileS;
-            const unsigned sOut = s0 + ds;
-            for (unsigned c = threadIdx.x / kProjTileS; c < zc * CH; c += blockDim.x / kProjTileS) {
-                const unsigned q = c / CH, du = c % CH;
-                const unsigned u = u0 + du;
-                if (u < uEnd && sOut < md.n)
-                    Proj[(((size_t)a * md.z + o0 + q) * uRows + u) * sCols + sOut] =
-                        Out[((size_t)q * CH + du) * (kProjTileS + 1) + ds];
+                    for (int j = 0; j < UPL; j++)
+                        if (v[j])
+                            Proj[(((size_t)a * md.z + o0 + q) * uRows + uu[j]) * sCols + s] =
+                                fmul(f32x2_part(acc[j][q / 2], q & 1), gamma);
+                }
             }
         }
     }
@@ -966,33 +952,32 @@ bool BackupEngine::ensure_proj(unsigned nU) {
 int BackupEngine::project(unsigned nU, const char *fn) {
     if (projStateMajor) {
         const unsigned zc = md.z >= 16 ? 32u : 8u;
-        const size_t smem = ((size_t)kProjTileS * md.ns * zc + (size_t)zc * 32 * kProjUPL * (kProjTileS + 1)) *
-                                sizeof(float) + (size_t)kProjTileS * md.ns * sizeof(int);
-        // Column ranges of about 32 MB of the transposed alphas (multiples of 64).
-        const unsigned uRange = (unsigned)std::max<size_t>(
-            32 * kProjUPL, ((32ull << 20) / ((size_t)md.n * sizeof(float))) / (32 * kProjUPL) * (32 * kProjUPL));
-        const dim3 blocks(md.m * ceil_div(md.n, kProjTileS), ceil_div(std::max(nU, 1u), uRange));
+        const size_t smem = (size_t)kProjTileS * (md.ns * zc + 4) * sizeof(float) +
+                            (size_t)kProjTileS * md.ns * sizeof(int);
         if (!projAttrDone) {
-            cudaFuncSetAttribute(proj_state_major_kernel<32, kProjUPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-            cudaFuncSetAttribute(proj_state_major_kernel<8, kProjUPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(proj_state_lanes_kernel<32, kProjUPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            cudaFuncSetAttribute(proj_state_lanes_kernel<8, kProjUPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
             cudaFuncSetAttribute(proj_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
             cudaFuncSetAttribute(proj_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
             projAttrDone = true;
         }
-        if (zc == 32) {
-            proj_state_major_kernel<32, kProjUPL><<<blocks, 256, smem, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj,
-                                                                       projCols, projSCols, uRange, 1.0f);
-        } else {
-            proj_state_major_kernel<8, kProjUPL><<<blocks, 256, smem, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj,
-                                                                      projCols, projSCols, uRange, 1.0f);
-        }
+        // Column ranges of about 32 MB of the transposed alphas (multiples of 32*UPL).
+        const unsigned uRange = (unsigned)std::max<size_t>(
+            32 * kProjUPL, ((32ull << 20) / ((size_t)md.n * sizeof(float))) / (32 * kProjUPL) * (32 * kProjUPL));
+        const dim3 blocks(md.m * ceil_div(md.n, kProjTileS), ceil_div(std::max(nU, 1u), uRange));
+        if (zc == 32)
+            proj_state_lanes_kernel<32, kProjUPL><<<blocks, 256, smem, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj,
+                                                                             projCols, projSCols, uRange, 1.0f);
+        else
+            proj_state_lanes_kernel<8, kProjUPL><<<blocks, 256, smem, stream>>>(md, succLen, C1, Gt, gtCols, nU, Proj,
+                                                                            projCols, projSCols, uRange, 1.0f);
         return check_launch(fn, "projection table");
     }
     const size_t smem32 = (size_t)md.ns * 32 * sizeof(float) + md.ns * sizeof(int);
     const unsigned blocks = md.m * md.n;
     if (!projAttrDone) {
-        cudaFuncSetAttribute(proj_state_major_kernel<32, kProjUPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(proj_state_major_kernel<8, kProjUPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(proj_state_lanes_kernel<32, kProjUPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(proj_state_lanes_kernel<8, kProjUPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cudaFuncSetAttribute(proj_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cudaFuncSetAttribute(proj_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         projAttrDone = true;
@@ -1099,8 +1084,8 @@ int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsi
     // rows to the scan (BF16's wider margin does).
     {
         const unsigned zc = md.z >= 16 ? 32u : 8u;
-        const size_t smemSM = ((size_t)kProjTileS * md.ns * zc + (size_t)zc * 32 * kProjUPL * (kProjTileS + 1)) *
-                                  sizeof(float) + (size_t)kProjTileS * md.ns * sizeof(int);
+        const size_t smemSM = (size_t)kProjTileS * (md.ns * zc + 4) * sizeof(float) +
+                              (size_t)kProjTileS * md.ns * sizeof(int);
         projStateMajor = wantTc && state_major_wanted(smemSM);
     }
     if (useProjNow && (rc = project(nU, fn)) != NOVA_SUCCESS) return rc;
@@ -1172,8 +1157,8 @@ int BackupEngine::backup_fixed(const float *src, float *dst, unsigned *pi, const
     if (!useProjNow) return NOVA_ERROR_KERNEL_EXECUTION;
     {
         const unsigned zc = md.z >= 16 ? 32u : 8u;
-        const size_t smemSM = ((size_t)kProjTileS * md.ns * zc + (size_t)zc * 32 * kProjUPL * (kProjTileS + 1)) *
-                                  sizeof(float) + (size_t)kProjTileS * md.ns * sizeof(int);
+        const size_t smemSM = (size_t)kProjTileS * (md.ns * zc + 4) * sizeof(float) +
+                              (size_t)kProjTileS * md.ns * sizeof(int);
         projStateMajor = state_major_wanted(smemSM);
     }
     if ((rc = project(nU, fn)) != NOVA_SUCCESS) return rc;
