@@ -25,6 +25,7 @@ POMDP_CONFIGS = {
     "pbvi_n4096_r256": dict(n=4096, m=16, z=32, ns=32, r=256, rz=64, gamma=0.95, horizon=4),
     "expand_n512": dict(n=512, m=8, z=16, ns=16, r=1024, rz=32, gamma=0.95, horizon=50),
     "pbvi_n4096_prof": dict(n=4096, m=2, z=32, ns=32, r=2048, rz=64, gamma=0.95, horizon=10),
+    "pbvi_n4096_m4z8": dict(n=4096, m=4, z=8, ns=32, r=8192, rz=64, gamma=0.95, horizon=10),
     "grad_n1024": dict(n=1024, m=8, z=16, ns=16, r=2048, rz=32, gamma=0.95, horizon=50),
 }
 MDP_CONFIGS = {
