@@ -1615,6 +1615,15 @@ extern "C" int pomdp_pbvi_set_scoring_gpu(POMDPPBVIGPU *pbvi, unsigned int mode)
         NOVA_ERR("pomdp_pbvi_set_scoring_gpu", "The solver is not initialized.");
         return NOVA_ERROR_INVALID_DATA;
     }
+    if (ws->eng.scoring != mode) {
+        // Captured updates belong to the old mode (updates are synchronous,
+        // so no replay is in flight).
+        for (int d = 0; d < 2; d++) {
+            if (ws->eng.graph[d]) cudaGraphExecDestroy(ws->eng.graph[d]);
+            ws->eng.graph[d] = nullptr;
+            ws->eng.graphSrc[d] = nullptr;
+        }
+    }
     ws->eng.scoring = mode;
     return NOVA_SUCCESS;
 }

@@ -154,7 +154,7 @@ int tc_build(BackupEngine &eng, const char *fn);
 // count stay on the device (eng.tc rowList, eng.itemCount); `timed` records
 // the GEMM events.
 int tc_score_launch(BackupEngine &eng, const float *src, unsigned nU, bool timed, const char *fn);
-bool tc_schedule_fixed(const BackupEngine &eng);
+bool tc_schedule_fixed(const BackupEngine &eng);  // and built for eng.scoring
 const unsigned *tc_row_list(const BackupEngine &eng);
 int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, const unsigned **rowList,
              const char *fn);

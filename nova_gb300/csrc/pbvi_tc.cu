@@ -1097,7 +1097,11 @@ int tc_score_launch(BackupEngine &eng, const float *src, unsigned nU, bool timed
     return NOVA_SUCCESS;
 }
 
-bool tc_schedule_fixed(const BackupEngine &eng) { return eng.tc != nullptr && eng.tc->schedFixed >= 0; }
+bool tc_schedule_fixed(const BackupEngine &eng) {
+    // Fixed, and the operand is built for the solver's current mode (a
+    // rebuild must not end up inside a captured update).
+    return eng.tc != nullptr && eng.tc->schedFixed >= 0 && eng.tc->mode == eng.scoring;
+}
 
 const unsigned *tc_row_list(const BackupEngine &eng) { return eng.tc ? eng.tc->rowList : nullptr; }
 

@@ -104,3 +104,24 @@ def test_large_state_layouts_equal_reference(mode):
     G, pi = orc.pbvi_solve(md)
     np.testing.assert_array_equal(bits(pol.gamma_array()), bits(G))
     np.testing.assert_array_equal(pol.pi_array(), pi)
+
+
+def test_graph_mode_survives_scoring_change():
+    """Changing the scoring mode drops the captured updates; the next ones
+    are captured (or run) in the new mode, with nova's results."""
+    from nova_gb300.pomdp_pbvi import POMDPPBVIGPU
+    md = synth.random_pomdp(n=150, m=2, z=4, ns=8, r=256, rz=16, gamma=0.95, horizon=12, seed=29)
+    p = POMDP.from_arrays(md)
+    p.initialize_gpu()
+    s = POMDPPBVIGPU(p)
+    s.set_scoring(npp.SCORING_FP16)
+    s.set_graph(True)
+    for _ in range(8):
+        s.update()
+    s.set_scoring(npp.SCORING_BF16)
+    for _ in range(md["horizon"] - 8):
+        s.update()
+    pol = s.get_policy()
+    G, pi = orc.pbvi_solve(md)
+    np.testing.assert_array_equal(bits(pol.gamma_array()), bits(G))
+    np.testing.assert_array_equal(pol.pi_array(), pi)
