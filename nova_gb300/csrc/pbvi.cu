@@ -535,7 +535,10 @@ constexpr int kProjUPL = 2;  // alphas per lane of the state-contiguous projecti
 // (per-state blocks padded by 4 floats, so the 8 states of a warp fall in
 // distinct banks) and keeps 32 observations' sums in registers; for every
 // (o, alpha) the 8 lanes of one alpha write the 8 states' values as one
-// 32-byte sector, straight from registers.
+// 32-byte sector, straight from registers. Successor lists are staged
+// successor-major ([l][8 states]), so the 8 states' l-th successors sit in
+// 8 banks, and each lane's transposed-alpha gathers run two successors
+// ahead of the arithmetic.
 template <int ZC, int UPL>
 __global__ void __launch_bounds__(256, UPL == 1 ? 3 : 2) proj_state_lanes_kernel(
         DevModel md, const unsigned *__restrict__ succLen, const float *__restrict__ C1,
@@ -544,7 +547,7 @@ __global__ void __launch_bounds__(256, UPL == 1 ? 3 : 2) proj_state_lanes_kernel
     extern __shared__ float smem[];
     const unsigned cStride = md.ns * ZC + 4;
     float *Cs = smem;                                                   // [8][cStride]
-    int *Ss = reinterpret_cast<int *>(Cs + (size_t)kProjTileS * cStride);  // [8][ns]
+    int *Ss = reinterpret_cast<int *>(Cs + (size_t)kProjTileS * cStride);  // [ns][8]
     __shared__ unsigned Ls[kProjTileS];
     const unsigned long long one2 = pack_f32x2(one, one);
     const unsigned tilesS = (md.n + kProjTileS - 1) / kProjTileS;
@@ -558,7 +561,7 @@ __global__ void __launch_bounds__(256, UPL == 1 ? 3 : 2) proj_state_lanes_kernel
         Ls[threadIdx.x] = s0 + threadIdx.x < md.n ? succLen[(size_t)(s0 + threadIdx.x) * md.m + a] : 0u;
     for (unsigned e = threadIdx.x; e < kProjTileS * md.ns; e += blockDim.x) {
         const unsigned st = e / md.ns, l = e % md.ns;
-        Ss[e] = s0 + st < md.n ? md.S[((size_t)(s0 + st) * md.m + a) * md.ns + l] : 0;
+        Ss[l * kProjTileS + st] = s0 + st < md.n ? md.S[((size_t)(s0 + st) * md.m + a) * md.ns + l] : 0;
     }
     for (unsigned o0 = 0; o0 < md.z; o0 += ZC) {
         __syncthreads();
@@ -571,7 +574,7 @@ __global__ void __launch_bounds__(256, UPL == 1 ? 3 : 2) proj_state_lanes_kernel
         const unsigned zc = min((unsigned)ZC, md.z - o0);
         const unsigned L = Ls[sl];
         const float *cw = Cs + (size_t)sl * cStride;
-        const int *sw = Ss + sl * md.ns;
+        const int *sw = Ss + sl;
         const unsigned uBegin = blockIdx.y * uRange, uEnd = min(nU, uBegin + uRange);
         for (unsigned u0 = uBegin + warp * 4u * UPL; u0 < uEnd; u0 += 32u * UPL) {
             unsigned uu[UPL];
@@ -586,19 +589,26 @@ __global__ void __launch_bounds__(256, UPL == 1 ? 3 : 2) proj_state_lanes_kernel
             for (int j = 0; j < UPL; j++)
 #pragma unroll
                 for (int q = 0; q < ZC / 2; q++) acc[j][q] = 0ull;
-            float gn[UPL];
+            float gn[UPL], gn2[UPL];
             if (L > 0) {
                 const float *grow = Gt + (size_t)sw[0] * gtCols;
+                const float *grow2 = Gt + (size_t)sw[(L > 1 ? 1 : 0) * kProjTileS] * gtCols;
 #pragma unroll
-                for (int j = 0; j < UPL; j++) gn[j] = v[j] ? grow[uu[j]] : 0.0f;
+                for (int j = 0; j < UPL; j++) {
+                    gn[j] = v[j] ? grow[uu[j]] : 0.0f;
+                    gn2[j] = v[j] ? grow2[uu[j]] : 0.0f;
+                }
             }
             for (unsigned l = 0; l < L; l++) {
                 unsigned long long gg[UPL];
 #pragma unroll
                 for (int j = 0; j < UPL; j++) gg[j] = pack_f32x2(gn[j], gn[j]);
-                const float *grow = Gt + (size_t)sw[l + 1 < L ? l + 1 : l] * gtCols;
+                const float *grow = Gt + (size_t)sw[(l + 2 < L ? l + 2 : L - 1) * kProjTileS] * gtCols;
 #pragma unroll
-                for (int j = 0; j < UPL; j++) gn[j] = v[j] ? grow[uu[j]] : 0.0f;
+                for (int j = 0; j < UPL; j++) {
+                    gn[j] = gn2[j];
+                    gn2[j] = v[j] ? grow[uu[j]] : 0.0f;
+                }
                 const ulonglong2 *c2 = reinterpret_cast<const ulonglong2 *>(cw + l * ZC);
 #pragma unroll
                 for (int q4 = 0; q4 < ZC / 4; q4++) {
@@ -1067,7 +1077,6 @@ int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsi
     stats.uniqueAlphas = nU;
     cudaEventRecord(ev[1], stream);
     const unsigned allItems = md.r * md.m;
-    bool done = false;
     // With room for the projection table every exact score is a 64-term
     // dot product over it: the plain form scans every row over it, and the
     // tensor-core form re-scores its near-ties and scans its unresolved rows
