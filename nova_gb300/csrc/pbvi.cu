@@ -525,7 +525,7 @@ __global__ void __launch_bounds__(256) proj_kernel(DevModel md, const unsigned *
 
 // The state-contiguous layout [m][z][uRows][sCols] (see proj_state_lanes_kernel).
 constexpr unsigned kProjTileS = 8;
-constexpr unsigned kStateMajorMinStates = 2048;
+constexpr unsigned kStateMajorMinStates = 1024;
 constexpr int kProjUPL = 2;  // alphas per lane of the state-contiguous projection
 
 // State-contiguous table, register form: one block per (a, 8 consecutive

@@ -87,13 +87,14 @@ def test_graph_updates_equal_reference(n):
     np.testing.assert_array_equal(pol.pi_array(), pi)
 
 
+@pytest.mark.parametrize("n", [1100, 2100])
 @pytest.mark.parametrize("mode", [npp.SCORING_FP16, npp.SCORING_BF16])
-def test_large_state_layouts_equal_reference(mode):
-    """n > 2048: FP16 updates use the state-contiguous projection table (while
+def test_large_state_layouts_equal_reference(mode, n):
+    """n > 1024: FP16 updates use the state-contiguous projection table (while
     the exact scan stays small), BF16 the alpha-contiguous one; both give
     nova's results."""
     from nova_gb300.pomdp_pbvi import POMDPPBVIGPU
-    md = synth.random_pomdp(n=2100, m=3, z=5, ns=8, r=300, rz=16, gamma=0.95, horizon=6, seed=23)
+    md = synth.random_pomdp(n=n, m=3, z=5, ns=8, r=300, rz=16, gamma=0.95, horizon=6, seed=23)
     p = POMDP.from_arrays(md)
     p.initialize_gpu()
     s = POMDPPBVIGPU(p)
