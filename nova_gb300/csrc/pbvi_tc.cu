@@ -318,6 +318,13 @@ __device__ __forceinline__ unsigned chunk_mask(const float (&v)[32], float lim) 
         for (int k = 0; k < w; k++) t[k] = t[2 * k] | t[2 * k + 1];
     return t[0];
 }
+// The smallest float above a finite or -inf f (+0 and -0 step to the
+// smallest subnormal): x > f is x >= next_up(f) for every non-NaN x.
+__device__ __forceinline__ float next_up(float f) {
+    const unsigned b = __float_as_uint(f);
+    if ((b & 0x7fffffffu) == 0u) return __uint_as_float(1u);
+    return __uint_as_float((b & 0x80000000u) ? b - 1u : b + 1u);
+}
 // v[c] for a run-time c without indexing the register array.
 __device__ __forceinline__ float chunk_select(const float (&v)[32], unsigned c) {
     float t[16];
@@ -473,7 +480,15 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
                         // listed (the list's first entry is that best).
                         best = fmaxf(best, mx);
                         lim = best - thr;
-                        unsigned mask = chunk_mask(v, lim);
+                        // Scores at or below the list's last entry f would
+                        // only raise the dropped maximum (push's first
+                        // branch). If any score of the chunk is above f, its
+                        // insertion drops f itself, which bounds them all;
+                        // otherwise the chunk's maximum is the largest of
+                        // them. Either way the list and the dropped maximum
+                        // end as if every score >= lim had been pushed.
+                        unsigned mask = chunk_mask(v, fmaxf(lim, next_up(top.v[K - 1])));
+                        if (mask == 0u) top.excl = fmaxf(top.excl, mx);
                         while (mask) {
                             const unsigned c = __ffs(mask) - 1;
                             mask &= mask - 1;
