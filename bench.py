@@ -727,13 +727,19 @@ def main():
         host.update()  # uploads the model and builds the tables; not timed
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        marks = []
         for _ in range(args.e2e_steps):
             host.update()
+            marks.append(time.perf_counter())
         wall = time.perf_counter() - t0
+        step_ms = [round((b - a) * 1e3, 1) for a, b in zip([t0] + marks[:-1], marks)]
         rn4 = cfg["r"] * cfg["n"] * 4
-        e2e = {"value": r * args.e2e_steps / wall, "unit": UNIT, "h2d_bytes_per_step": 2 * rn4 + 4 * cfg["r"],
+        # Each call uploads the input set and pi and reads back the output set
+        # and pi; the host output set is uploaded too only when some belief
+        # keeps its row (no action above the -1e10 sentinel), never here.
+        e2e = {"value": r * args.e2e_steps / wall, "unit": UNIT, "h2d_bytes_per_step": rn4 + 4 * cfg["r"],
                "d2h_bytes_per_step": rn4 + 4 * cfg["r"],
-               "api": "pomdp_pbvi_update_cpu (host Gamma/GammaPrime/pi; wall clock)"}
+               "step_ms": step_ms, "api": "pomdp_pbvi_update_cpu (host Gamma/GammaPrime/pi; wall clock)"}
         del host
 
     # ---- CPU baseline (oracle port of nova's loop) on a bounded sample ------

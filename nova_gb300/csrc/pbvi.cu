@@ -818,6 +818,7 @@ BackupEngine::~BackupEngine() {
     cudaFree(succLen); cudaFree(suppLen); cudaFree(C1); cudaFree(C3);
     cudaFree(hash); cudaFree(rep); cudaFree(uniqJ); cudaFree(nUniqueDev); cudaFree(Gt);
     cudaFree(jstar); cudaFree(actVal); cudaFree(partV); cudaFree(partU); cudaFree(items); cudaFree(itemCount);
+    cudaFree(keptCount);
     cudaFree(dotScratch); cudaFree(bDense); cudaFree(resultA); cudaFree(resultV); cudaFree(rowScratch);
     cudaFree(vnb); cudaFree(vnp1b); cudaFree(btilde);
     cudaFree(Proj); cudaFree(ustar); cudaFree(scanV); cudaFree(scanU);
@@ -848,6 +849,7 @@ int BackupEngine::build(const DevModel &model, const char *fn) {
     if ((rc = dev_alloc(&actVal, (size_t)md.r * md.m, fn, "the action values")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&items, (size_t)md.r * md.m, fn, "the work list")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&itemCount, 1, fn, "the work list count")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&keptCount, 1, fn, "the kept-belief count")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&dotScratch, md.r, fn, "the FP64 values")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&bDense, md.n, fn, "the belief")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&resultA, 1, fn, "the action")) != NOVA_SUCCESS) return rc;
@@ -1064,6 +1066,34 @@ int BackupEngine::assemble(const float *src, float *dst, unsigned *pi, int onlyB
                                                                              firstBelief, dst, pi, dstRowOverride,
                                                                              actionOut);
     return check_launch(fn, "alpha assembly");
+}
+
+// Beliefs whose every action value fails to beat the sentinel: the assembly
+// leaves their row and action untouched (pomdp_pbvi_cpu.cpp:128-145).
+__global__ void count_kept_kernel(const float *__restrict__ actVal, unsigned r, unsigned m, unsigned *count) {
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= r) return;
+    for (unsigned a = 0; a < m; a++)
+        if (actVal[(size_t)i * m + a] > NOVA_FLT_MIN) return;
+    atomicAdd(count, 1u);
+}
+
+int BackupEngine::count_kept(unsigned *out, const char *fn) {
+    if (cudaMemsetAsync(keptCount, 0, sizeof(unsigned), stream) != cudaSuccess) {
+        cudaGetLastError();
+        NOVA_ERR(fn, "Failed to clear the kept-belief count.");
+        return NOVA_ERROR_KERNEL_EXECUTION;
+    }
+    count_kept_kernel<<<ceil_div(md.r, 256), 256, 0, stream>>>(actVal, md.r, md.m, keptCount);
+    int rc = check_launch(fn, "kept beliefs");
+    if (rc != NOVA_SUCCESS) return rc;
+    if (cudaMemcpyAsync(out, keptCount, sizeof(unsigned), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+            cudaStreamSynchronize(stream) != cudaSuccess) {
+        cudaGetLastError();
+        NOVA_ERR(fn, "Failed to read the kept-belief count.");
+        return NOVA_ERROR_MEMCPY_TO_HOST;
+    }
+    return NOVA_SUCCESS;
 }
 
 int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsigned *pi, const char *fn) {
@@ -1778,9 +1808,9 @@ static int pbvi_cpu_prepare(PbviCpuWorkspace *ws, const POMDP *pomdp, const char
     return NOVA_SUCCESS;
 }
 
-// One backup with host arrays as the source of truth: upload the input set,
-// the output set (rows a belief does not improve keep their contents) and
-// pi; back up on the device; download the output set and pi.
+// One backup with host arrays as the source of truth: upload the input set
+// and pi, back up on the device, download the output set and pi (with the
+// host's output set uploaded first when a belief keeps its row).
 static int pbvi_cpu_step(PbviCpuWorkspace *ws, const POMDP *pomdp, POMDPPBVICPU *pbvi, const char *fn) {
     const size_t rn = (size_t)pomdp->r * pomdp->n;
     const bool even = (pbvi->currentHorizon % 2u) == 0u;
@@ -1788,9 +1818,19 @@ static int pbvi_cpu_step(PbviCpuWorkspace *ws, const POMDP *pomdp, POMDPPBVICPU 
     float *hdst = even ? pbvi->GammaPrime : pbvi->Gamma;
     int rc;
     if ((rc = h2d(ws->Gamma, hsrc, rn * sizeof(float), fn, "Gamma")) != NOVA_SUCCESS) return rc;
-    if ((rc = h2d(ws->GammaPrime, hdst, rn * sizeof(float), fn, "Gamma (prime)")) != NOVA_SUCCESS) return rc;
     if ((rc = h2d(ws->pi, pbvi->pi, pomdp->r * sizeof(unsigned), fn, "pi")) != NOVA_SUCCESS) return rc;
     if ((rc = ws->eng.backup_all(ws->Gamma, pomdp->r, ws->GammaPrime, ws->pi, fn)) != NOVA_SUCCESS) return rc;
+    // The update writes every row of the output set except those of beliefs
+    // no action of which beats the sentinel, so the host's output set is
+    // uploaded only when such a belief exists; the update is then repeated
+    // over it (the input set on the device is unchanged).
+    unsigned kept = 0;
+    if ((rc = ws->eng.count_kept(&kept, fn)) != NOVA_SUCCESS) return rc;
+    if (kept != 0) {
+        if ((rc = h2d(ws->GammaPrime, hdst, rn * sizeof(float), fn, "Gamma (prime)")) != NOVA_SUCCESS) return rc;
+        if ((rc = h2d(ws->pi, pbvi->pi, pomdp->r * sizeof(unsigned), fn, "pi")) != NOVA_SUCCESS) return rc;
+        if ((rc = ws->eng.backup_all(ws->Gamma, pomdp->r, ws->GammaPrime, ws->pi, fn)) != NOVA_SUCCESS) return rc;
+    }
     if ((rc = d2h(hdst, ws->GammaPrime, rn * sizeof(float), fn, "Gamma (prime)")) != NOVA_SUCCESS) return rc;
     if ((rc = d2h(pbvi->pi, ws->pi, pomdp->r * sizeof(unsigned), fn, "pi")) != NOVA_SUCCESS) return rc;
     pbvi->currentHorizon++;

@@ -74,6 +74,7 @@ struct BackupEngine {
     size_t partCap = 0;
     unsigned *items = nullptr;           // [r*m] work list (belief*m + action)
     unsigned *itemCount = nullptr;       // device scalar
+    unsigned *keptCount = nullptr;       // device scalar (count_kept)
     double *dotScratch = nullptr;        // [r] FP64 V(b) row values
     float *bDense = nullptr;             // [n]
     unsigned *resultA = nullptr;         // [1]
@@ -135,6 +136,10 @@ struct BackupEngine {
     // Action values and best-action assembly for all beliefs (or one).
     int assemble(const float *src, float *dst, unsigned *pi, int onlyBelief, float *dstRowOverride,
                  unsigned *actionOut, const char *fn);
+    // After backup_all: the number of beliefs whose every action value
+    // failed to beat the -1e10 sentinel (their row and action were left as
+    // they were in dst and pi).
+    int count_kept(unsigned *out, const char *fn);
 };
 
 // Held exclusively while an update graph is captured, shared by everything

@@ -68,6 +68,45 @@ def test_stepwise_update_cpu_api_host_arrays():
         assert alg.currentHorizon == h + 1
 
 
+def kept_belief_model(seed=3):
+    """Beliefs 0..39 live on states 0..29, whose rewards are -3e10, so no action
+    of theirs beats the -1e10 sentinel and the update leaves their rows and
+    actions as they were; states 30..59 lead only to themselves, so beliefs
+    40..79 are backed up normally."""
+    md = synth.random_pomdp(n=60, m=3, z=4, ns=6, r=80, rz=8, gamma=0.9, horizon=4, seed=seed)
+    rng = np.random.default_rng(seed)
+    for s in range(30, 60):
+        for a in range(3):
+            md["S"][s, a] = np.sort(rng.choice(np.arange(30, 60), 6, replace=False))
+    md["R"][:30, :] = -3e10
+    for i in range(80):
+        pool = np.arange(0, 30) if i < 40 else np.arange(30, 60)
+        md["Z"][i] = np.sort(rng.choice(pool, 8, replace=False))
+    md["GammaInitial"] = rng.normal(size=(80, 60)).astype(np.float32)
+    return md
+
+
+def test_stepwise_update_cpu_api_keeps_rows_below_sentinel():
+    """update_cpu uploads the host output set only when some belief keeps its
+    row; both kinds of belief match nova's in-place update step by step."""
+    md = kept_belief_model()
+    p = POMDP.from_arrays(md)
+    alg = POMDPPBVICPU(p, GammaInitial=md["GammaInitial"])
+    G = md["GammaInitial"].copy()
+    Gp = G.copy()
+    pi = np.zeros(md["r"], np.uint32)
+    r, n = md["r"], md["n"]
+    for h in range(4):
+        alg.update()
+        src, dst = (G, Gp) if h % 2 == 0 else (Gp, G)
+        orc.pbvi_update(md, src, dst, pi)
+        host = np.ctypeslib.as_array(alg.GammaPrime if h % 2 == 0 else alg.Gamma, shape=(r * n,)).reshape(r, n)
+        np.testing.assert_array_equal(bits(host), bits(dst))
+        np.testing.assert_array_equal(np.ctypeslib.as_array(alg.pi, shape=(r,)), pi)
+    assert np.array_equal(bits(Gp[:40]), bits(md["GammaInitial"][:40]))  # kept rows did survive
+    assert not np.array_equal(bits(Gp[40:]), bits(md["GammaInitial"][40:]))
+
+
 @pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("seed", [7, 8])
 def test_random_models_stepwise_against_oracle(seed, mode):
