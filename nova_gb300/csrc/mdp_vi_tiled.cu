@@ -46,7 +46,7 @@ constexpr unsigned kThreads = 1024;
 constexpr unsigned kWarps = kThreads / 32;     // row ranges (and level slices) per block
 constexpr int kPairGroups = 4;             // groups of 64 records (32 pairs) prefetched per warp
 constexpr unsigned kMaxRows = 65535u;       // rows of one block (16-bit row field)
-constexpr unsigned kDefaultTileStates = 12288u;
+constexpr unsigned kDefaultTileStates = 10240u;
 constexpr unsigned long long kAutoMinEntries = 1ull << 22;
 
 std::atomic<unsigned> g_mode{NOVA_VI_TILING_AUTO};
