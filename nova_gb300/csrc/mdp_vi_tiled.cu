@@ -11,7 +11,8 @@
 //     stages V one tile at a time (cp.async, double-buffered) and adds the
 //     products of the successors that fall in that tile.
 //   * The plan regroups the successor entries once per solver: one 8-byte
-//     record {row << 16 | offset in tile, T} per entry. Within a block the
+//     record {row << 16 | offset in tile, fl(gamma * T)} per entry (the
+//     reference's first rounding, done once). Within a block the
 //     m*Sb rows are split into equal ranges, one per warp, so a row is
 //     only ever touched by one warp. A row's successors that fall in one tile
 //     form a run (they are consecutive in the row's list); the q-th record of
@@ -96,9 +97,9 @@ __device__ __forceinline__ void apply_pairs(uint4 r, unsigned g0, unsigned b0, u
     const unsigned row0 = r.x >> 16, off0 = r.x & 0xFFFFu;
     const unsigned row1 = r.z >> 16, off1 = r.z & 0xFFFFu;
     if (p0 >= b0 && p0 < b1 && row0 < rows && off0 < tileLen)
-        part[row0] = fadd(part[row0], fmul(fmul(gamma, __uint_as_float(r.y)), vtile[off0]));
+        part[row0] = fadd(part[row0], fmul(__uint_as_float(r.y), vtile[off0]));
     if (p1 >= b0 && p1 < b1 && row1 < rows && off1 < tileLen)
-        part[row1] = fadd(part[row1], fmul(fmul(gamma, __uint_as_float(r.w)), vtile[off1]));
+        part[row1] = fadd(part[row1], fmul(__uint_as_float(r.w), vtile[off1]));
     __syncwarp();
 }
 
@@ -209,6 +210,7 @@ __global__ void vi_plan_scan_rows_kernel(unsigned n, unsigned m, unsigned ns, co
 
 struct PlanGeometry {
     unsigned n, m, ns, Vt, T, Sb, rowsPerWarp, L;
+    float gamma;
     __device__ __forceinline__ size_t sub(unsigned blk, unsigned t, unsigned rowLocal) const {
         return (((size_t)blk * T + t) * kWarps + rowLocal / rowsPerWarp) * L;
     }
@@ -259,7 +261,7 @@ __global__ void vi_plan_fill_kernel(PlanGeometry g, unsigned blocks, const int *
             const size_t sb = g.sub(blk, t, rowLocal) + q;
             const unsigned c = cursor[sb];
             cursor[sb] = c + 1;
-            rec[start[sb] + c] = make_uint2((rowLocal << 16) | ((unsigned)sp - t * g.Vt), __float_as_uint(Tr[l]));
+            rec[start[sb] + c] = make_uint2((rowLocal << 16) | ((unsigned)sp - t * g.Vt), __float_as_uint(fmul(g.gamma, Tr[l])));
         }
     }
 }
@@ -528,7 +530,7 @@ int vi_plan_build(ViTilePlan *plan, const MDP *mdp, const int *S, const float *T
         release(plan);
         return NOVA_SUCCESS;
     }
-    PlanGeometry g{n, m, ns, Vt, tiles, Sb, ceil_div((unsigned long long)Sb * m, kWarps), L};
+    PlanGeometry g{n, m, ns, Vt, tiles, Sb, ceil_div((unsigned long long)Sb * m, kWarps), L, mdp->gamma};
     const unsigned long long nSub = (unsigned long long)blocks * tiles * kWarps * L;
     if (nSub >= (1ull << 32) - 1) { release(plan); return NOVA_SUCCESS; }
 

@@ -63,7 +63,7 @@ struct ViTilePlan {
     unsigned levels = 0;        // longest run of one row's successors inside one tile
     unsigned grid = 0;          // resident CTAs
     size_t smemBytes = 0;
-    uint2 *rec = nullptr;          // [entries] {row << 16 | offset in tile, T bits}
+    uint2 *rec = nullptr;          // [entries] {row << 16 | offset in tile, bits of fl(gamma * T)}
     unsigned *levelStart = nullptr;  // build scratch: first record of each (slice, level) sub-bin
     unsigned *sliceStart = nullptr;  // [blocks*tiles*warps + 1] first record of each (block, tile, warp) slice
     unsigned *counts = nullptr;    // build scratch
