@@ -185,7 +185,7 @@ NOVA_API int mdp_vi_residual_gpu(const MDP *mdp, const MDPVIGPU *vi, double *res
  * own order (mdp_vi_cpu.cpp:45-52), so results stay bit-identical; other
  * models use the per-row gather sweep. A solver builds its tile plan (8 bytes
  * per successor entry) at its first sweep after initialize, from the model's
- * S and T as they are then.
+ * S, T and gamma as they are then.
  *  mode: NOVA_VI_TILING_AUTO (default: tiled for models with at least 2^22
  *        successor entries), NOVA_VI_TILING_ALWAYS (whenever the model
  *        qualifies), NOVA_VI_TILING_NEVER.
