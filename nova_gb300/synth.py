@@ -27,6 +27,7 @@ POMDP_CONFIGS = {
     "pbvi_n4096_prof": dict(n=4096, m=2, z=32, ns=32, r=2048, rz=64, gamma=0.95, horizon=10),
     "pbvi_n4096_m4z8": dict(n=4096, m=4, z=8, ns=32, r=8192, rz=64, gamma=0.95, horizon=10),
     "grad_n1024": dict(n=1024, m=8, z=16, ns=16, r=2048, rz=32, gamma=0.95, horizon=50),
+    "pbvi_n59_r3725": dict(n=59, m=7, z=29, ns=16, r=3725, rz=32, gamma=0.95, horizon=10),
 }
 MDP_CONFIGS = {
     "vi_n1m": dict(n=1 << 20, m=8, ns=16, gamma=0.99, horizon=2000),
