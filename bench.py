@@ -19,7 +19,7 @@ CPU algorithm on this host's cores (the oracle port; nova's own CPU sources
 are not present on the GPU host) on the same workload.
 
 Multi-GPU: every rank runs an independent replica of the workload (PBVI
-beliefs of one POMDP need the full alpha set each step, and this build has
+beliefs of one POMDP need the full alpha set each step, and the library has
 no collective); value is the sum over ranks of beliefs backed up divided by
 the maximum time over ranks.
 """
