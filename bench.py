@@ -558,6 +558,20 @@ def run_mdp(args, dist_rank):
             "note": "FP32 values near 78 have a 7.6e-6 ulp; the FP64 residual of the FP32 iteration stalls above 1e-6"}
 
 
+def replica_throughput(dist, world, units_per_rank, ms_local, device):
+    """Whole-job throughput of `world` independent replicas that each process
+    units_per_rank units: the job takes as long as its slowest rank (an
+    all-reduce MAX of the per-rank milliseconds), and the units of all ranks
+    count. Returns (units per second, job milliseconds)."""
+    ms = float(ms_local)
+    if dist is not None:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return world * units_per_rank / (ms * 1e-3), ms
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -636,13 +650,8 @@ def main():
         if dist:
             dist.barrier()
     launches = lib.nova_gb300_kernel_launches() - launches0
-    ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
     r = cfg["r"]
-    value = world * r * args.steps / (ms * 1e-3)
+    value, ms = replica_throughput(dist, world, r * args.steps, e0.elapsed_time(e1), "cuda")
 
     # ---- roofline of the scoring kernel --------------------------------------
     hbm, tc_peak, peak_kind = measured_peaks()

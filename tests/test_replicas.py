@@ -1,0 +1,68 @@
+"""The multi-rank path of bench.py on CPU: N independent replicas, the job
+time is the slowest rank's and the units of every rank count (two gloo ranks
+on 127.0.0.1)."""
+import os
+import socket
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, out):
+    import torch.distributed as dist
+    sys.path.insert(0, ROOT)
+    import bench
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        # rank 0 takes 100 ms, rank 1 takes 250 ms for 1000 units each
+        value, ms = bench.replica_throughput(dist, world, 1000, 100.0 if rank == 0 else 250.0, "cpu")
+        out[rank] = (value, ms)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_replica_throughput_two_gloo_ranks():
+    mp = pytest.importorskip("torch.multiprocessing")
+    ctx = mp.get_context("spawn")
+    with ctx.Manager() as mgr:
+        out = mgr.dict()
+        port = _free_port()
+        procs = [ctx.Process(target=_rank, args=(r, 2, port, out)) for r in range(2)]
+        for p in procs:
+            p.start()
+        for p in procs:
+            p.join(120)
+            assert p.exitcode == 0
+        res = dict(out)
+    for r in range(2):
+        value, ms = res[r]
+        assert ms == 250.0
+        assert value == pytest.approx(2 * 1000 / 0.25)
+
+
+def test_replica_throughput_single_rank():
+    sys.path.insert(0, ROOT)
+    import bench
+    value, ms = bench.replica_throughput(None, 1, 500, 50.0, "cpu")
+    assert ms == 50.0 and value == pytest.approx(10000.0)
+
+
+def test_reference_arm_nonzero_rank_exits_without_work():
+    """Under torchrun only rank 0 times the reference arm; the others exit 0
+    and print nothing."""
+    import subprocess
+    env = dict(os.environ, RANK="1", LOCAL_RANK="1", WORLD_SIZE="2", MASTER_ADDR="127.0.0.1")
+    res = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2",
+                          "--steps", "1", "--warmup", "0"], env=env, capture_output=True, text=True, timeout=120)
+    assert res.returncode == 0, res.stderr
+    assert res.stdout.strip() == ""
