@@ -68,6 +68,24 @@ def test_stepwise_update_cpu_api_host_arrays():
         assert alg.currentHorizon == h + 1
 
 
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("shape", [(1, 1, 1, 1, 40, 1), (2, 1, 3, 2, 50, 2), (33, 4, 1, 33, 64, 33),
+                                   (7, 9, 2, 3, 1, 7), (64, 1, 64, 4, 130, 5), (129, 2, 2, 5, 257, 129),
+                                   (50, 2, 1, 7, 300, 50)])
+def test_degenerate_shapes_against_oracle(shape, mode):
+    """One state, one action, one observation, one belief, full belief
+    support (rz = n) and dense successor lists (ns = n), from a random
+    initial set whose rows are all distinct (so the tensor-core modes score
+    the first updates on the tensor cores whenever r >= 32)."""
+    n, m, z, ns, r, rz = shape
+    md = synth.random_pomdp(n=n, m=m, z=z, ns=ns, r=r, rz=rz, gamma=0.9, horizon=5, seed=n + r)
+    md["GammaInitial"] = np.random.default_rng(n * r).normal(-3.0, 1.0, size=(r, n)).astype(np.float32)
+    G, pi = solve_gpu(md, mode)
+    Go, po = orc.pbvi_solve(md)
+    np.testing.assert_array_equal(bits(G), bits(Go))
+    np.testing.assert_array_equal(pi, po)
+
+
 def kept_belief_model(seed=3):
     """Beliefs 0..39 live on states 0..29, whose rewards are -3e10, so no action
     of theirs beats the -1e10 sentinel and the update leaves their rows and
