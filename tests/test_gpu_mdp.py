@@ -154,6 +154,24 @@ def test_tiled_sweeps_match_oracle(tiling, n, m_actions, ns, tile):
     np.testing.assert_array_equal(pol.pi_array(), pi)
 
 
+@pytest.mark.parametrize("mode", [nmvi.TILING_NEVER, nmvi.TILING_ALWAYS])
+@pytest.mark.parametrize("n,m_actions,ns", [(1, 1, 1), (2, 3, 2), (5, 1, 5), (70, 2, 70)])
+def test_degenerate_shapes_both_sweeps(tiling, mode, n, m_actions, ns):
+    """One state, one action, one successor, and dense successor lists
+    (ns = n), with the per-row and the column-tiled sweep (64-state tiles;
+    a row with more than 31 successors inside one tile keeps the per-row
+    sweep)."""
+    tiling.set_tiling(mode, 64)
+    md = synth.random_mdp(n=n, m=m_actions, ns=ns, gamma=0.9, horizon=7, seed=n)
+    m = MDP.from_arrays(md)
+    m.initialize_gpu()
+    pol = MDPValueIterationGPU(m, Vinitial=np.zeros(md["n"], np.float32)).solve()
+    assert tiling.tiling_status() == (2 if mode == nmvi.TILING_NEVER or ns > 31 else 1)
+    V, pi = orc.mdp_vi_solve(md, horizon=7, VInitial=np.zeros(md["n"], np.float32))
+    np.testing.assert_array_equal(bits(pol.V_array()), bits(V))
+    np.testing.assert_array_equal(pol.pi_array(), pi)
+
+
 def test_tiled_execute_until_converged_and_cpu_api(tiling):
     tiling.set_tiling(nmvi.TILING_ALWAYS, 512)
     md = ragged_sorted_mdp(2500, 4, 6, seed=9, gamma=0.9, horizon=40)
