@@ -91,7 +91,7 @@ __device__ __forceinline__ void load_pairs(uint4 (&buf)[kPairGroups], const uint
 // least 64 positions apart, so the rows of a pair-group are distinct; groups
 // run in slice order, which is each row's successor order.
 __device__ __forceinline__ void apply_pairs(uint4 r, unsigned g0, unsigned b0, unsigned b1, unsigned lane,
-                                            float gamma, const float *vtile, unsigned tileLen, float *part,
+                                            const float *vtile, unsigned tileLen, float *part,
                                             unsigned rows) {
     const unsigned p0 = g0 + 2u * lane, p1 = p0 + 1u;
     const unsigned row0 = r.x >> 16, off0 = r.x & 0xFFFFu;
@@ -104,7 +104,7 @@ __device__ __forceinline__ void apply_pairs(uint4 r, unsigned g0, unsigned b0, u
 }
 
 __global__ void __launch_bounds__(kThreads, 1) bellman_tiled_kernel(
-        unsigned n, unsigned m, float gamma, unsigned Vt, unsigned T, unsigned Sb, unsigned blocks,
+        unsigned n, unsigned m, unsigned Vt, unsigned T, unsigned Sb, unsigned blocks,
         const uint2 *__restrict__ rec, const unsigned *__restrict__ sliceStart, const float *__restrict__ R,
         const float *__restrict__ V, float *__restrict__ Vp, unsigned *__restrict__ pi, ViDeviceState *st,
         double tol, int early_exit) {
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(kThreads, 1) bellman_tiled_kernel(
 #pragma unroll
                 for (int k = 0; k < kPairGroups; k++) {
                     const unsigned g0 = c0 + 64u * k;
-                    if (g0 < b1) apply_pairs(cur[k], g0, b0, b1, lane, gamma, vcur, tileLen, part, rows);
+                    if (g0 < b1) apply_pairs(cur[k], g0, b0, b1, lane, vcur, tileLen, part, rows);
                 }
             }
             cp_async_wait_all();
@@ -261,7 +261,8 @@ __global__ void vi_plan_fill_kernel(PlanGeometry g, unsigned blocks, const int *
             const size_t sb = g.sub(blk, t, rowLocal) + q;
             const unsigned c = cursor[sb];
             cursor[sb] = c + 1;
-            rec[start[sb] + c] = make_uint2((rowLocal << 16) | ((unsigned)sp - t * g.Vt), __float_as_uint(fmul(g.gamma, Tr[l])));
+            rec[start[sb] + c] =
+                make_uint2((rowLocal << 16) | ((unsigned)sp - t * g.Vt), __float_as_uint(fmul(g.gamma, Tr[l])));
         }
     }
 }
@@ -642,7 +643,7 @@ int vi_plan_build(ViTilePlan *plan, const MDP *mdp, const int *S, const float *T
 int vi_tiled_sweep(const ViTilePlan *plan, const MDP *mdp, const float *R, const float *V, float *Vp, unsigned *pi,
                    ViDeviceState *st, double tol, int early_exit, cudaStream_t stream, const char *fn) {
     bellman_tiled_kernel<<<plan->grid, kThreads, plan->smemBytes, stream>>>(
-        mdp->n, mdp->m, mdp->gamma, plan->tileStates, plan->tiles, plan->blockStates, plan->blocks, plan->rec,
+        mdp->n, mdp->m, plan->tileStates, plan->tiles, plan->blockStates, plan->blocks, plan->rec,
         plan->sliceStart, R, V, Vp, pi, st, tol, early_exit);
     return check_launch(fn, "Bellman update (tiled)");
 }
