@@ -679,6 +679,42 @@ def main():
                     "traffic": None, "kernel": "tensor-core scoring did not run (exact scoring only)",
                     "peak_source": peak_kind}
 
+    # ---- e2e through the host-buffer entry point ----------------------------
+    # Measured right after the device-resident steps, under the same clocks;
+    # the BF16 and plain legs below run afterwards on a new device solver.
+    pol = alg.get_policy()
+    Gnow = pol.gamma_array()
+    del pol
+    del alg  # frees the device solver (its operands and projection table)
+    torch.cuda.synchronize()
+    e2e = None
+    if args.e2e_steps > 0:
+        host = POMDPPBVICPU(p, GammaInitial=Gnow)
+        host.update()  # uploads the model and builds the tables; not timed
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        marks = []
+        for _ in range(args.e2e_steps):
+            host.update()
+            marks.append(time.perf_counter())
+        wall = time.perf_counter() - t0
+        step_ms = [round((b - a) * 1e3, 1) for a, b in zip([t0] + marks[:-1], marks)]
+        rn4 = cfg["r"] * cfg["n"] * 4
+        # Each call uploads the input set and pi and reads back the output set
+        # and pi; the host output set is uploaded too only when some belief
+        # keeps its row (no action above the -1e10 sentinel), never here.
+        e2e = {"value": r * args.e2e_steps / wall, "unit": UNIT, "h2d_bytes_per_step": rn4 + 4 * cfg["r"],
+               "d2h_bytes_per_step": rn4 + 4 * cfg["r"],
+               "step_ms": step_ms, "api": "pomdp_pbvi_update_cpu (host Gamma/GammaPrime/pi; wall clock)"}
+        del host
+
+    # ---- a device solver for the BF16 and plain legs, from the same state ----
+    if args.bf16_steps > 0 or args.plain_steps > 0:
+        alg = POMDPPBVIGPU(p, GammaInitial=Gnow)
+        alg.set_scoring(npp.SCORING_FP16)
+        alg.update()  # builds the operands and tables; not timed
+        torch.cuda.synchronize()
+
     # ---- BF16 tensor-core scoring on the same state ----------------------------
     bf16 = None
     if args.bf16_steps > 0:
@@ -723,33 +759,9 @@ def main():
                  "ms_per_step": pms / args.plain_steps,
                  "form": "FP32 SIMT scoring of every unique alpha in nova's operation order"}
         alg.set_scoring(npp.SCORING_FP16)
-
-    # ---- e2e through the host-buffer entry point ----------------------------
-    pol = alg.get_policy()
-    Gnow = pol.gamma_array()
-    del pol
-    del alg  # frees the device solver (its operands and projection table)
-    torch.cuda.synchronize()
-    e2e = None
-    if args.e2e_steps > 0:
-        host = POMDPPBVICPU(p, GammaInitial=Gnow)
-        host.update()  # uploads the model and builds the tables; not timed
+    if args.bf16_steps > 0 or args.plain_steps > 0:
+        del alg  # frees the second device solver before the remaining legs
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        marks = []
-        for _ in range(args.e2e_steps):
-            host.update()
-            marks.append(time.perf_counter())
-        wall = time.perf_counter() - t0
-        step_ms = [round((b - a) * 1e3, 1) for a, b in zip([t0] + marks[:-1], marks)]
-        rn4 = cfg["r"] * cfg["n"] * 4
-        # Each call uploads the input set and pi and reads back the output set
-        # and pi; the host output set is uploaded too only when some belief
-        # keeps its row (no action above the -1e10 sentinel), never here.
-        e2e = {"value": r * args.e2e_steps / wall, "unit": UNIT, "h2d_bytes_per_step": rn4 + 4 * cfg["r"],
-               "d2h_bytes_per_step": rn4 + 4 * cfg["r"],
-               "step_ms": step_ms, "api": "pomdp_pbvi_update_cpu (host Gamma/GammaPrime/pi; wall clock)"}
-        del host
 
     # ---- CPU baseline (oracle port of nova's loop) on a bounded sample ------
     cpu = None
