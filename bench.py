@@ -49,12 +49,14 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="pbvi_n4096")
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-mdp", action="store_true")
     ap.add_argument("--bf16-steps", type=int, default=2)
     ap.add_argument("--precision-steps", type=int, default=3)
+    ap.add_argument("--precision-horizon", type=int, default=12)
+    ap.add_argument("--parity-beliefs", type=int, default=16)
     ap.add_argument("--batch-horizon", type=int, default=20)
     ap.add_argument("--batch-threads", type=int, default=16)
     return ap.parse_args()
@@ -181,6 +183,47 @@ def measured_peaks():
         return 6800.0, 1700.0, "fallback (sustained)"
 
 
+def gemm_traffic(units, split):
+    """DRAM bytes per launch of the scoring GEMM: an ncu capture of a smaller
+    launch of the same kernel (profiles/tc_score_gemm_traffic.json: its DRAM
+    read and write bytes and its work units, one unit being one (a,o) pair x
+    128-row tile x alpha group) scaled to `units` units, since each unit
+    streams one A tile and writes one candidate set. None when no capture of
+    this operand form is recorded."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "tc_score_gemm_traffic.json")) as f:
+            d = json.load(f)["bf16_split" if split else "fp16"]
+        per_unit = (float(d["dram_bytes_read"]) + float(d["dram_bytes_write"])) / float(d["units"])
+        return per_unit * units, ("DRAM bytes per launch: ncu capture of a %d-unit launch (%s) scaled to %d units"
+                                  % (d["units"], d["workload"], units))
+    except Exception:
+        return None, "no ncu capture recorded for this operand form"
+
+
+def sampled_parity(alg, model, k, seed):
+    """One more (untimed) update on `alg`, then its rows and actions for k
+    sampled beliefs (those with rows sent to the exact scan, those with the
+    most alphas re-scored, random ones) against nova's loop-form backup (the
+    oracle, as the checker) over all actions and the full alpha set."""
+    from oracle import oracle as orc
+    pol = alg.get_policy()
+    G = pol.gamma_array()
+    del pol
+    alg.update()
+    st = alg.stats()
+    cand, exact = alg.row_detail()
+    pol = alg.get_policy()
+    Gp, pi = pol.gamma_array(), pol.pi_array()
+    del pol
+    beliefs = orc.choose_parity_beliefs(cand, exact, k=k, seed=seed)
+    t0 = time.perf_counter()
+    bad = orc.sampled_backup_parity(model, G, Gp, pi, beliefs, threads=host_cores())
+    return {"matched": "%d of %d" % (len(beliefs) - len(bad), len(beliefs)), "beliefs": beliefs,
+            "mismatched": bad, "horizon": st["horizon"], "scoring": st["scoring"],
+            "rows_exact_scan": st["rowsOverflow"], "candidates_rescored": st["candidates"],
+            "max_candidates_one_belief": int(cand.max()), "oracle_seconds": time.perf_counter() - t0}
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -243,6 +286,98 @@ def run_precision(args):
     out["note"] = ("tensor-core alphas are bit-identical to the plain FP32 path's; dV_b0 is their FP32 rounding "
                    "against FP64 on the same selections, dV_b0_free_fp64_run the gap to an FP64 solve that made "
                    "different argmax choices at near-ties")
+    return out
+
+
+def run_precision_headline(args, model, pomdp):
+    """|V(b0) - V_FP64(b0)| on the full pbvi_n4096 workload (r=8192): H
+    backups from GammaInitial with the library's default (FP16 tensor-core)
+    scoring, their selections recorded, then the same H backups recomputed
+    in FP64 on the GPU with those selections held fixed
+    (pomdp_pbvi_value_replay_f64_gpu); b0 = belief 0. The difference is the
+    arithmetic error of the FP32 backups (the tensor-core alphas equal the
+    plain FP32 path's bit for bit)."""
+    from nova_gb300 import synth
+    from nova_gb300.pomdp_adjoint import pbvi_value_vs_fp64
+    H = args.precision_horizon
+    b0 = synth.dense_belief(model, 0)
+    t0 = time.perf_counter()
+    V, V64, istar, _, _ = pbvi_value_vs_fp64(model, b0, H, pomdp=pomdp)
+    return {"horizon": H, "r": model["r"], "n": model["n"], "V_b0": V, "V_b0_fp64_same_selections": V64,
+            "dV_b0": abs(V - V64), "alpha": istar, "seconds": time.perf_counter() - t0,
+            "fp64": "GPU FP64 replay of the recorded selections (checked against the oracle's FP64 forward on "
+                    "small models in the tests)"}
+
+
+def run_margins(args):
+    """Candidates within proven margins at n=4096 (pbvi_n4096, seed 0): after
+    --warmup FP16 backups, for 2048 random (belief, action, observation) rows,
+    the exact scores (FP64, from a dense A row and the distinct alphas) of all
+    alphas, and how many lie within 2E of the best for the error bound E of
+    each operand form: E = a1 (U gmax + gN Gmax) with U the sum of both
+    operands' unit roundoffs (FP16 2^-11, BF16 2^-8, E4M3 2^-4), the FP32
+    build of A and the accumulation; the split forms carry one operand as a
+    hi + lo pair (2^-16). Worst-case operand rounding is used for both
+    operands here (the library bounds A's rounding by its measured value,
+    which is tighter). This is the design input for the operand precision
+    of the scoring GEMM."""
+    import torch
+    from nova_gb300 import synth
+    from nova_gb300 import nova_pomdp_pbvi as npp
+    from nova_gb300.pomdp import POMDP
+    from nova_gb300.pomdp_pbvi import POMDPPBVIGPU
+    cfg = dict(synth.POMDP_CONFIGS["pbvi_n4096"])
+    model = synth.random_pomdp(**cfg, seed=args.seed)
+    n, m, z, ns, r, rz = (cfg[k] for k in ("n", "m", "z", "ns", "r", "rz"))
+    p = POMDP.from_arrays(model)
+    p.initialize_gpu()
+    alg = POMDPPBVIGPU(p, GammaInitial=model["GammaInitial"])
+    alg.set_scoring(npp.SCORING_FP16)
+    for _ in range(args.warmup):
+        alg.update()
+    pol = alg.get_policy()
+    G = pol.gamma_array()
+    del pol
+    del alg
+    dev = "cuda"
+    S = torch.tensor(model["S"].astype(np.int64), device=dev)
+    T = torch.tensor(model["T"].astype(np.float64), device=dev)
+    O = torch.tensor(model["O"].astype(np.float64), device=dev)
+    rng = np.random.default_rng(args.seed + 1)
+    NS = 2048
+    ri, ra, ro = rng.integers(0, r, NS), rng.integers(0, m, NS), rng.integers(0, z, NS)
+    A = torch.zeros((NS, n), dtype=torch.float64, device=dev)
+    for t in range(NS):
+        i, a, o = int(ri[t]), int(ra[t]), int(ro[t])
+        sk = torch.tensor(model["Z"][i].astype(np.int64), device=dev)
+        w = torch.tensor(model["B"][i].astype(np.float64), device=dev)[:, None] * T[sk, a, :]
+        W = torch.zeros(n, dtype=torch.float64, device=dev)
+        W.index_add_(0, S[sk, a, :].reshape(-1), w.reshape(-1))
+        A[t] = float(np.float32(cfg["gamma"])) * W * O[a, :, o]
+    Gu = torch.tensor(np.unique(G, axis=0).astype(np.float64), device=dev)
+    h = 0.5 * (Gu.max(0).values - Gu.min(0).values)
+    gmax, Gmax = float(h.max()), float(Gu.abs().max())
+    sc = A @ Gu.T
+    best = sc.max(1).values
+    a1 = A.abs().sum(1)
+    u24 = 2.0 ** -24
+    epsA = (rz * ns + 4) * u24
+    gN = (ns + rz + 3) * u24 * 1.01
+
+    def bound(uA, uG, ksplit=1):
+        acc = (ksplit * n / 16 + 2) / 4194304.0
+        return a1 * ((epsA + (1 + uA) * (uG + 2 * u24) + uA + acc) * gmax + gN * Gmax)
+    forms = {"fp16": bound(2 ** -11, 2 ** -11), "bf16": bound(2 ** -8, 2 ** -8),
+             "bf16_alphas_split": bound(2 ** -8, 2 ** -16, 2), "bf16_both_split": bound(2 ** -16, 2 ** -16, 3),
+             "e4m3": bound(2 ** -4, 2 ** -4), "reference_rounding_only": a1 * gN * Gmax}
+    out = {"workload": "pbvi_n4096 (seed %d) after %d FP16 backups; %d sampled rows" % (args.seed, args.warmup, NS),
+           "distinct_alphas": int(Gu.shape[0]), "gmax": gmax, "Gmax": Gmax}
+    for name, E in forms.items():
+        cnt = (sc >= (best - 2 * E)[:, None]).sum(1).cpu().numpy()
+        out[name] = {"mean": float(cnt.mean()), "p50": float(np.percentile(cnt, 50)),
+                     "p90": float(np.percentile(cnt, 90)), "p99": float(np.percentile(cnt, 99)),
+                     "max": int(cnt.max()), "rows_over_128": float((cnt > 128).mean()),
+                     "E_over_a1_gmax_median": float(torch.median(E / (a1 * gmax)))}
     return out
 
 
@@ -598,6 +733,12 @@ def main():
         if rank == 0:
             print(json.dumps({"batch": run_batch(args)}))
         return
+    if args.config == "margins_n4096":
+        import torch
+        torch.cuda.set_device(local_rank)
+        if rank == 0:
+            print(json.dumps({"margins": run_margins(args)}))
+        return
     if args.config == "grad_n1024":
         import torch
         torch.cuda.set_device(local_rank)
@@ -660,18 +801,11 @@ def main():
     if gemm:
         flops = [2.0 * r * u * n_pad * cfg["m"] * cfg["z"] for u, _ in gemm]
         achieved = sum(flops) / (sum(t for _, t in gemm) * 1e-3) / 1e12
-        # DRAM traffic per launch: the ncu capture of the n=4096 small case
-        # (profiles/tc_score_gemm_n4096_small.md: 593.8 MB read + 33.1 MB
-        # written over 1024 work units) scaled by this launch's work units
-        # (m*z pairs x 128-row tiles x alpha groups); traffic grows with the
-        # units, since each unit streams one A tile and writes one candidate set.
         groups = [s["tcGroups"] for s in stats if s["msGemm"] > 0][-1]
         units = cfg["m"] * cfg["z"] * ((r + 127) // 128) * max(1, groups)
-        traffic = (593.8e6 + 33.1e6) / 1024.0 * units
+        traffic, traffic_note = gemm_traffic(units, split=False)
         roofline = {"bound": "tensor", "achieved": achieved, "peak": tc_peak, "unit": "TFLOP/s",
-                    "frac": achieved / tc_peak, "traffic": traffic,
-                    "traffic_note": "bytes per launch, scaled from an ncu capture of a 1024-unit launch to %d units"
-                                    % units,
+                    "frac": achieved / tc_peak, "traffic": traffic, "traffic_note": traffic_note,
                     "kernel": "tcgen05 FP16 scoring GEMM (kind::f16, FP32 accumulate in TMEM) with fused candidate-list epilogue",
                     "flops_per_launch": flops[-1], "peak_source": peak_kind}
     else:
@@ -708,12 +842,16 @@ def main():
                "step_ms": step_ms, "api": "pomdp_pbvi_update_cpu (host Gamma/GammaPrime/pi; wall clock)"}
         del host
 
-    # ---- a device solver for the BF16 and plain legs, from the same state ----
-    if args.bf16_steps > 0 or args.plain_steps > 0:
+    # ---- a device solver for the parity check and the BF16 and plain legs ---
+    parity = {}
+    second = args.bf16_steps > 0 or args.plain_steps > 0 or args.parity_beliefs > 0
+    if second:
         alg = POMDPPBVIGPU(p, GammaInitial=Gnow)
         alg.set_scoring(npp.SCORING_FP16)
         alg.update()  # builds the operands and tables; not timed
         torch.cuda.synchronize()
+        if rank == 0 and args.parity_beliefs > 0:
+            parity["fp16"] = sampled_parity(alg, model, args.parity_beliefs, seed=1)
 
     # ---- BF16 tensor-core scoring on the same state ----------------------------
     bf16 = None
@@ -735,12 +873,16 @@ def main():
         fach = (sum(2.0 * r * u * n_pad * cfg["m"] * cfg["z"] for u, _ in fgemm) /
                 (sum(t for _, t in fgemm) * 1e-3) / 1e12) if fgemm else None
         bf16 = {"value": r * args.bf16_steps / (fms * 1e-3), "unit": UNIT, "steps": args.bf16_steps,
-                "ms_per_step": fms / args.bf16_steps, "gemm_tflops": fach,
+                "ms_per_step": fms / args.bf16_steps, "gemm_tflops_fp16_equivalent": fach,
+                "gemm_tflops": 2.0 * fach if fach else None,
                 "rows_rescored": fl["rowsMultiCand"], "rows_exact_scan": fl["rowsOverflow"],
-                "note": "same tcgen05 kernel with BF16 operands; its wider proven margin sends most rows to the "
-                        "exact scan at this size",
+                "candidates_rescored": fl["candidates"],
+                "note": "same tcgen05 kernel with BF16 operands: beliefs in one BF16 term, alphas as a hi + lo pair "
+                        "of BF16 terms (twice the FP16 form's MMA work); proven-margin exact re-score",
                 "step_breakdown_ms": {k: fl[k] for k in ("msDedup", "msProject", "msScore", "msGemm", "msRescore",
                                                          "msActions", "msAssemble", "msTotal")}}
+        if rank == 0 and args.parity_beliefs > 0:
+            parity["bf16"] = sampled_parity(alg, model, args.parity_beliefs, seed=2)
         alg.set_scoring(npp.SCORING_FP16)
 
     # ---- plain FP32 form on the same state -----------------------------------
@@ -759,7 +901,7 @@ def main():
                  "ms_per_step": pms / args.plain_steps,
                  "form": "FP32 SIMT scoring of every unique alpha in nova's operation order"}
         alg.set_scoring(npp.SCORING_FP16)
-    if args.bf16_steps > 0 or args.plain_steps > 0:
+    if second:
         del alg  # frees the second device solver before the remaining legs
         torch.cuda.synchronize()
 
@@ -774,6 +916,10 @@ def main():
 
     mdp = None if args.no_mdp else run_mdp(args, rank)
     precision = run_precision(args) if (rank == 0 and args.precision_steps > 0) else None
+    if rank == 0 and args.precision_horizon > 0:
+        precision = precision or {}
+        precision["pbvi_n4096"] = run_precision_headline(args, model, p)
+        precision["max_dV_b0"] = max(v["dV_b0"] for k, v in precision.items() if isinstance(v, dict))
 
     last = stats[-1]
     out = {
@@ -798,6 +944,9 @@ def main():
         "rows_rescored": last["rowsMultiCand"], "pairs_full_exact": last["rowsOverflow"],
         "mdp_vi": mdp,
         "precision_vs_fp64": precision,
+        "parity_sampled": parity or None,
+        "tc_vs_plain_fp32": {"fp16": value / plain["value"] if plain else None,
+                             "bf16": bf16["value"] / plain["value"] if (plain and bf16) else None},
     }
     if rank == 0:
         print(json.dumps(out))

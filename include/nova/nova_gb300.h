@@ -21,20 +21,21 @@ NOVA_NS_BEGIN
 /* Belief-scoring modes of the PBVI / Perseus backup.
  *  NOVA_SCORING_EXACT: every candidate alpha is scored in FP32 in the
  *      reference's operation order (bit-identical to pomdp_pbvi_cpu.cpp:37-103).
- *  NOVA_SCORING_BF16: tcgen05 tensor cores score all alphas in BF16 (FP32
- *      accumulate); every alpha within a proven error bound of the best is
- *      re-scored in the exact FP32 order, so the argmax equals EXACT's.
- *  NOVA_SCORING_FP16: as BF16 with FP16 operands (per-belief power-of-two
- *      scaling keeps them in range); the tighter rounding leaves fewer
- *      alphas to re-score. */
+ *  NOVA_SCORING_BF16: tcgen05 tensor cores score all alphas with BF16
+ *      operands and FP32 accumulation: the belief operand in one BF16 term,
+ *      the alphas as a pair of BF16 terms (hi + lo, 16 significant bits), so
+ *      the scoring GEMM does twice FP16's work; every alpha within a proven
+ *      error bound of the best is re-scored in the exact FP32 order, so the
+ *      argmax equals EXACT's.
+ *  NOVA_SCORING_FP16: one FP16 term per operand (per-belief power-of-two
+ *      scaling keeps them in range), half BF16's GEMM work; the default. */
 #define NOVA_SCORING_EXACT 0u
 #define NOVA_SCORING_BF16  1u
 #define NOVA_SCORING_FP16  2u
 
 /* Select the scoring mode used by later pomdp_pbvi_update_gpu calls on this
- * solver struct. The default is NOVA_SCORING_FP16: at n=4096 with 8192
- * alphas its proven margin leaves ~2% of rows to the exact scan, BF16's
- * ~93%. Tensor-core scoring engages once 32 distinct alphas exist and the
+ * solver struct. The default is NOVA_SCORING_FP16 (the fastest). Tensor-core
+ * scoring engages once 32 distinct alphas exist and the
  * projection table fits in device memory; otherwise rows are scored exactly.
  * All modes give bit-identical results. */
 NOVA_API int pomdp_pbvi_set_scoring_gpu(POMDPPBVIGPU *pbvi, unsigned int mode);
@@ -65,6 +66,18 @@ typedef struct NovaPBVIStats {
 } NovaPBVIStats;
 
 NOVA_API int pomdp_pbvi_get_stats_gpu(const POMDPPBVIGPU *pbvi, NovaPBVIStats *stats);
+
+/* Per-belief detail of the last pomdp_pbvi_update_gpu on this solver, when
+ * it scored on the tensor cores (NovaPBVIStats.tcGroups != 0): for belief i,
+ * candidates[i] = alphas re-scored exactly in the FP32 order because their
+ * tensor-core score lay within the proven margin of the best, summed over
+ * the belief's (action, observation) rows, and exactRows[i] = its rows that
+ * were scanned exactly over every alpha. Host arrays of r entries. A test
+ * and measurement aid for the scoring path of pomdp_pbvi_cpu.cpp:37-103; no
+ * reference counterpart. NOVA_ERROR_INVALID_DATA if the last update did not
+ * use the tensor cores (or ran as a graph replay). */
+NOVA_API int pomdp_pbvi_row_detail_gpu(const POMDPPBVIGPU *pbvi, unsigned int *candidates,
+        unsigned int *exactRows);
 
 /* V(b) = max_i Gamma_i . b over the solver's current device Gamma (the one
  * get_policy would return), reduced in FP64 on the device. b is a dense host
@@ -103,6 +116,22 @@ NOVA_API int pomdp_pbvi_adjoint_gpu(const POMDP *pomdp, unsigned int horizon,
         unsigned int checkpointEvery, const float *d_checkpoints, const unsigned int *d_actions,
         const unsigned int *d_selects, const float *d_b, double *d_dR, double *d_dT, double *d_dO,
         double *d_dGamma0, double *Vb, unsigned int *bestAlpha);
+
+/* V(b) of the alpha set that horizon recorded backups make from d_Gamma0
+ * ([r][n], FP32, device), recomputed in FP64 with the recorded selections
+ * held fixed (d_actions [horizon][r], d_selects [horizon][r][z] as
+ * pomdp_pbvi_execute_recorded_gpu writes them): every backup
+ * Gamma_t[i](s) = R(s,a) + gamma sum_l T(s,a,l) sum_o O(a,S,o) Gamma_{t-1}[j_o](S)
+ * (pomdp_pbvi_cpu.cpp:37-162 with its argmax results fixed) runs in FP64
+ * from the model's device arrays. *Vb = d_b . Gamma_H[alpha] for alpha < r
+ * (the FP32 run's own maximising alpha, so that only the arithmetic
+ * differs), else the FP64 maximum from -1e10 with the lowest index on ties
+ * (pomdp_alpha_vectors.cpp:52-79); *bestAlpha (may be NULL) receives the
+ * row used. The FP64 reference of a solve's V(b0); no reference
+ * counterpart. */
+NOVA_API int pomdp_pbvi_value_replay_f64_gpu(const POMDP *pomdp, unsigned int horizon, const float *d_Gamma0,
+        const unsigned int *d_actions, const unsigned int *d_selects, const float *d_b, unsigned int alpha,
+        double *Vb, unsigned int *bestAlpha);
 
 /* Solve count independent POMDPs, each as pomdp_pbvi_execute_gpu would
  * (initialize, `horizon` updates with the given NOVA_SCORING_* mode,
@@ -220,9 +249,13 @@ NOVA_API int nova_gb300_device_status(unsigned int *deviceError);
  * keeps until exit; r beyond that limit is rejected with
  * NOVA_ERROR_INVALID_DATA. Calls share the scratch, so calls that overlap on
  * the GPU race and must be serialised by the caller. The first call on a
- * device resolves the scratch's device address for it; make that first call
- * before any stream capture. Kernels run on the default stream and the call
- * returns after the result is copied back. */
+ * device resolves the scratch's device address for it (again after the
+ * device's context is created anew, e.g. after cudaDeviceReset); make that
+ * first call before any stream capture. Kernels run on the calling thread's
+ * per-thread default stream, which is not ordered against the caller's
+ * non-blocking streams or other host threads: work that writes d_Gamma, d_pi
+ * or d_b there must be complete before the call. The call returns after the
+ * result is copied back. */
 #define NOVA_VALUE_NOALLOC_MAX_ROWS 65536u
 NOVA_API int pomdp_alpha_vectors_value_noalloc_gpu(const float *d_Gamma, const unsigned int *d_pi,
         unsigned int r, unsigned int n, const float *d_b, double *Vb, unsigned int *a);

@@ -10,18 +10,28 @@
 //     R(s,a)). Successor states are cut into tiles of Vt states; the CTA
 //     stages V one tile at a time (cp.async, double-buffered) and adds the
 //     products of the successors that fall in that tile.
-//   * The plan regroups the successor entries once per solver: one 8-byte
-//     record {row << 16 | offset in tile, fl(gamma * T)} per entry (the
-//     reference's first rounding, done once). Within a block the
-//     m*Sb rows are split into equal ranges, one per warp, so a row is
-//     only ever touched by one warp. A row's successors that fall in one tile
-//     form a run (they are consecutive in the row's list); the q-th record of
-//     every run goes to level q. The records of (block, tile, warp) are
-//     stored level after level, so within a level every row appears at most
-//     once and lanes add to their rows' partial sums without conflicts, and
-//     level q is applied before level q+1, which keeps each row's products in
-//     list order. Records stream from HBM exactly once per sweep (the same 8
-//     bytes per entry as S and T).
+//   * A row's successors inside one tile form a run (consecutive in the
+//     row's list). The plan, built once per solver, stores for every chunk
+//     (block, tile) the 8-byte records {row << 16 | offset in tile,
+//     fl(gamma * T)} (the reference's first rounding, done once) of all its
+//     runs, level after level: level q holds the q-th record of every run
+//     with more than q records, runs ordered by length (longest first), so
+//     run j has its level-q record at position j of level q. Thread k of the
+//     CTA applies runs k, k + 1024, ... of the chunk, each run's records in
+//     list order into its row's partial sum; the rows of one chunk's runs are
+//     distinct, so no two threads touch one partial sum, and the chunks of a
+//     block run in tile order with one CTA barrier between tiles. Records
+//     stream from HBM exactly once per sweep (the same 8 bytes per entry as S
+//     and T): each thread loads its next chunk's records into registers while
+//     it applies the current chunk's, and the chunk after that is prefetched
+//     into L2 with one bulk prefetch.
+//   * Within a chunk the single-record runs are ordered so that a warp's 32
+//     runs fall in distinct shared-memory banks: runs are bucketed by the
+//     bank of their partial sum (row mod 32), sorted inside each bucket by
+//     the distance (tile offset - row) mod 32, and dealt out round-robin over
+//     the buckets. A full round is 32 distinct partial-sum banks, and since
+//     the k-th runs of the buckets have about the same distance, their V
+//     offsets fall in distinct banks too.
 //
 // Order of operations: the reference computes Q = R(s,a), then for each
 // successor in list order Q += (gamma * T) * V[s'] (mdp_vi_cpu.cpp:45-52).
@@ -44,9 +54,9 @@ namespace nova_gb300 {
 namespace {
 
 constexpr unsigned kThreads = 1024;
-constexpr unsigned kWarps = kThreads / 32;     // row ranges (and level slices) per block
-constexpr int kPairGroups = 4;             // groups of 64 records (32 pairs) prefetched per warp
+constexpr int kRunsPerThread = 5;           // level-0 records held in registers per thread and chunk
 constexpr unsigned kMaxRows = 65535u;       // rows of one block (16-bit row field)
+constexpr unsigned kMaxLevels = 31u;        // longest run of one row inside one tile
 constexpr unsigned kDefaultTileStates = 10240u;
 constexpr unsigned long long kAutoMinEntries = 1ull << 22;
 
@@ -73,93 +83,116 @@ __device__ __forceinline__ void stage_tile(float *dst, const float *__restrict__
     cp_async_commit();
 }
 
-// Records of one warp slice are read as 16-byte pairs: pair j of the slice
-// holds records 2j and 2j+1 counted from a0, the slice start rounded down
-// to an even record (the record array has one spare record at its end).
-__device__ __forceinline__ void load_pairs(uint4 (&buf)[kPairGroups], const uint4 *__restrict__ rec2, unsigned a0,
-                                           unsigned b1, unsigned lane) {
-#pragma unroll
-    for (int k = 0; k < kPairGroups; k++) {
-        const unsigned j = (a0 >> 1) + 32u * k + lane;
-        buf[k] = 2u * j < b1 ? __ldg(rec2 + j) : make_uint4(0xFFFFFFFFu, 0u, 0xFFFFFFFFu, 0u);
-    }
+// Bulk prefetch of a record range into L2 (16-byte aligned; the record
+// array has two spare records at its end).
+__device__ __forceinline__ void prefetch_l2(const uint2 *rec, unsigned b, unsigned e) {
+    if (e <= b) return;
+    const uintptr_t lo = reinterpret_cast<uintptr_t>(rec + b) & ~(uintptr_t)15;
+    const uintptr_t hi = (reinterpret_cast<uintptr_t>(rec + e) + 15) & ~(uintptr_t)15;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((unsigned)(hi - lo)) : "memory");
 }
 
-// Apply one pair-group: records [g0, g0 + 64) of this warp's slice, lane l
-// holding records g0 + 2l and g0 + 2l + 1; records outside [b0, b1) and
-// padding records are skipped. The plan keeps two records of one row at
-// least 64 positions apart, so the rows of a pair-group are distinct; groups
-// run in slice order, which is each row's successor order.
-__device__ __forceinline__ void apply_pairs(uint4 r, unsigned g0, unsigned b0, unsigned b1, unsigned lane,
-                                            const float *vtile, unsigned tileLen, float *part,
-                                            unsigned rows) {
-    const unsigned p0 = g0 + 2u * lane, p1 = p0 + 1u;
-    const unsigned row0 = r.x >> 16, off0 = r.x & 0xFFFFu;
-    const unsigned row1 = r.z >> 16, off1 = r.z & 0xFFFFu;
-    if (p0 >= b0 && p0 < b1 && row0 < rows && off0 < tileLen)
-        part[row0] = fadd(part[row0], fmul(__uint_as_float(r.y), vtile[off0]));
-    if (p1 >= b0 && p1 < b1 && row1 < rows && off1 < tileLen)
-        part[row1] = fadd(part[row1], fmul(__uint_as_float(r.w), vtile[off1]));
-    __syncwarp();
+// The records a thread needs for one chunk: level-0 records of its runs
+// tid + kThreads * i (i < kRunsPerThread), and the level-1 record of run tid.
+struct ChunkRegs {
+    uint2 r0[kRunsPerThread];
+    uint2 r1;
+    unsigned start, n0, n1;
+};
+
+__device__ __forceinline__ void load_chunk(ChunkRegs &c, const uint2 *__restrict__ rec,
+                                           const unsigned *__restrict__ chunkStart,
+                                           const unsigned *__restrict__ levelCnt, unsigned L, size_t chunk,
+                                           unsigned tid) {
+    c.start = __ldg(chunkStart + chunk);
+    c.n0 = __ldg(levelCnt + chunk * L);
+    c.n1 = L > 1 ? __ldg(levelCnt + chunk * L + 1) : 0u;
+#pragma unroll
+    for (int i = 0; i < kRunsPerThread; i++) {
+        const unsigned j = tid + kThreads * i;
+        c.r0[i] = j < c.n0 ? __ldg(rec + c.start + j) : make_uint2(0xFFFFFFFFu, 0u);
+    }
+    c.r1 = tid < c.n1 ? __ldg(rec + c.start + c.n0 + tid) : make_uint2(0xFFFFFFFFu, 0u);
+}
+
+// One record into the running partial sum q: q + fl(gamma*T) * V[s'].
+__device__ __forceinline__ float apply_record(float q, uint2 r, const float *vtile, unsigned tileLen) {
+    const unsigned off = r.x & 0xFFFFu;
+    return off < tileLen ? fadd(q, fmul(__uint_as_float(r.y), vtile[off])) : q;
+}
+
+// Run j of a chunk: its level-0 record r0, then (j < n1) the further
+// levels in list order; first1 is the level-1 record when already loaded.
+__device__ __forceinline__ void apply_run(uint2 r0, bool have1, uint2 first1, unsigned j, const ChunkRegs &c,
+                                          const uint2 *__restrict__ rec, const unsigned *__restrict__ levelCnt,
+                                          unsigned L, size_t chunk, const float *vtile, unsigned tileLen,
+                                          float *part, unsigned rows) {
+    const unsigned row = r0.x >> 16;
+    if (row >= rows) return;
+    float q = apply_record(part[row], r0, vtile, tileLen);
+    if (j < c.n1) {
+        q = apply_record(q, have1 ? first1 : __ldg(rec + c.start + c.n0 + j), vtile, tileLen);
+        unsigned base = c.n0 + c.n1;
+        for (unsigned lv = 2; lv < L; lv++) {
+            const unsigned nq = __ldg(levelCnt + chunk * L + lv);
+            if (j >= nq) break;
+            q = apply_record(q, __ldg(rec + c.start + base + j), vtile, tileLen);
+            base += nq;
+        }
+    }
+    part[row] = q;
 }
 
 __global__ void __launch_bounds__(kThreads, 1) bellman_tiled_kernel(
-        unsigned n, unsigned m, unsigned Vt, unsigned T, unsigned Sb, unsigned blocks,
-        const uint2 *__restrict__ rec, const unsigned *__restrict__ sliceStart, const float *__restrict__ R,
-        const float *__restrict__ V, float *__restrict__ Vp, unsigned *__restrict__ pi, ViDeviceState *st,
-        double tol, int early_exit) {
+        unsigned n, unsigned m, unsigned Vt, unsigned T, unsigned Sb, unsigned blocks, unsigned L,
+        const uint2 *__restrict__ rec, const unsigned *__restrict__ chunkStart,
+        const unsigned *__restrict__ levelCnt, const float *__restrict__ R, const float *__restrict__ V,
+        float *__restrict__ Vp, unsigned *__restrict__ pi, ViDeviceState *st, double tol, int early_exit) {
     if (early_exit && *(volatile unsigned *)&st->converged) return;  // uniform across the grid
     extern __shared__ __align__(16) unsigned char smem[];
     float *vt = reinterpret_cast<float *>(smem);            // [2][Vt]
     float *part = vt + 2 * (size_t)Vt;                      // [Sb*m]
-    const uint4 *rec2 = reinterpret_cast<const uint4 *>(rec);
-    const unsigned tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const unsigned tid = threadIdx.x;
     double local = 0.0;
     for (unsigned blk = blockIdx.x; blk < blocks; blk += gridDim.x) {
         const unsigned s0 = blk * Sb;
         const unsigned nsb = min(Sb, n - s0);
         const unsigned rows = nsb * m;
         for (unsigned i = tid; i < rows; i += blockDim.x) part[i] = __ldg(R + (size_t)s0 * m + i);
-        // Slice (block, tile, warp) is sliceStart[(blk*T + t)*kWarps + warp] ..
-        // sliceStart[... + 1]; lanes 0 and 1 hold the two bounds.
-        const size_t sub0 = (size_t)blk * T * kWarps + warp;
-        unsigned bdCur = lane < 2 ? __ldg(sliceStart + sub0 + lane) : 0u;
-        unsigned bdNext = (T > 1 && lane < 2) ? __ldg(sliceStart + sub0 + kWarps + lane) : 0u;
+        const size_t c0 = (size_t)blk * T;
         stage_tile(vt, V, n, 0, Vt);
-        uint4 cur[kPairGroups], nxt[kPairGroups];
-#pragma unroll
-        for (int k = 0; k < kPairGroups; k++) nxt[k] = make_uint4(0xFFFFFFFFu, 0u, 0xFFFFFFFFu, 0u);
-        load_pairs(cur, rec2, __shfl_sync(0xffffffffu, bdCur, 0) & ~1u, __shfl_sync(0xffffffffu, bdCur, 1), lane);
+        if (tid == 0) {
+            prefetch_l2(rec, __ldg(chunkStart + c0), __ldg(chunkStart + c0 + min(T, 2u)));
+        }
+        ChunkRegs cur, nxt;
+        load_chunk(cur, rec, chunkStart, levelCnt, L, c0, tid);
         cp_async_wait_all();
         __syncthreads();
         for (unsigned t = 0; t < T; t++) {
             const float *vcur = vt + (size_t)(t & 1) * Vt;
-            unsigned bdNext2 = 0u;
+            const size_t chunk = c0 + t;
             if (t + 1 < T) {
-                // The other buffer held tile t-1; every warp passed the
+                // The other buffer held tile t-1; every thread passed the
                 // barrier that ended tile t-1, so it is free.
                 stage_tile(vt + (size_t)((t + 1) & 1) * Vt, V, n, t + 1, Vt);
-                load_pairs(nxt, rec2, __shfl_sync(0xffffffffu, bdNext, 0) & ~1u,
-                           __shfl_sync(0xffffffffu, bdNext, 1), lane);
-                if (t + 2 < T && lane < 2) bdNext2 = __ldg(sliceStart + sub0 + (size_t)(t + 2) * kWarps + lane);
+                if (tid == 0 && t + 2 < T)
+                    prefetch_l2(rec, __ldg(chunkStart + chunk + 2), __ldg(chunkStart + chunk + 3));
+                load_chunk(nxt, rec, chunkStart, levelCnt, L, chunk + 1, tid);
             }
-            const unsigned b0 = __shfl_sync(0xffffffffu, bdCur, 0), b1 = __shfl_sync(0xffffffffu, bdCur, 1);
-            const unsigned a0 = b0 & ~1u;
             const unsigned tileLen = min(Vt, n - t * Vt);
-            for (unsigned c0 = a0; c0 < b1; c0 += 64u * kPairGroups) {
-                if (c0 != a0) load_pairs(cur, rec2, c0, b1, lane);
 #pragma unroll
-                for (int k = 0; k < kPairGroups; k++) {
-                    const unsigned g0 = c0 + 64u * k;
-                    if (g0 < b1) apply_pairs(cur[k], g0, b0, b1, lane, vcur, tileLen, part, rows);
-                }
+            for (int i = 0; i < kRunsPerThread; i++) {
+                const unsigned j = tid + kThreads * i;
+                if (j < cur.n0)
+                    apply_run(cur.r0[i], i == 0, cur.r1, j, cur, rec, levelCnt, L, chunk, vcur, tileLen, part,
+                              rows);
             }
+            for (unsigned j = tid + kThreads * kRunsPerThread; j < cur.n0; j += kThreads)
+                apply_run(__ldg(rec + cur.start + j), false, cur.r1, j, cur, rec, levelCnt, L, chunk, vcur, tileLen,
+                          part, rows);
             cp_async_wait_all();
             __syncthreads();
-#pragma unroll
-            for (int k = 0; k < kPairGroups; k++) cur[k] = nxt[k];
-            bdCur = bdNext;
-            bdNext = bdNext2;
+            cur = nxt;
         }
         // Action scan of mdp_vi_cpu.cpp:55-58 (lowest action on ties).
         for (unsigned i = tid; i < nsb; i += blockDim.x) {
@@ -209,131 +242,116 @@ __global__ void vi_plan_scan_rows_kernel(unsigned n, unsigned m, unsigned ns, co
 }
 
 struct PlanGeometry {
-    unsigned n, m, ns, Vt, T, Sb, rowsPerWarp, L;
+    unsigned n, m, ns, Vt, T, Sb, L;
     float gamma;
-    __device__ __forceinline__ size_t sub(unsigned blk, unsigned t, unsigned rowLocal) const {
-        return (((size_t)blk * T + t) * kWarps + rowLocal / rowsPerWarp) * L;
-    }
 };
 
-// Records per (block, tile, warp, level) sub-bin.
-__global__ void vi_plan_count_kernel(PlanGeometry g, const int *__restrict__ S, unsigned *counts) {
+// Calls f(tile, first list index, run length) for every run of the row.
+template <typename F>
+__device__ __forceinline__ void for_each_run(const int *Sr, unsigned ns, unsigned Vt, F f) {
+    unsigned l = 0;
+    while (l < ns) {
+        const int sp = Sr[l];
+        if (sp < 0) break;
+        const unsigned t = (unsigned)sp / Vt;
+        unsigned e = l + 1;
+        while (e < ns && Sr[e] >= 0 && (unsigned)Sr[e] / Vt == t) e++;
+        f(t, l, e - l);
+        l = e;
+    }
+}
+
+__device__ __forceinline__ unsigned run_cell(unsigned rowLocal, unsigned off) {
+    const unsigned qb = rowLocal & 31u, vb = off & 31u;
+    return qb * 32u + ((vb - qb) & 31u);
+}
+
+// Per chunk c = block * T + tile: levelCnt[c*L + q] = runs with more than q
+// records; cell[c*1024 + qb*32 + d] = single-record runs whose partial sum
+// is in bank qb at distance d; longCnt[c*(L+1) + len] = runs of len >= 2.
+__global__ void vi_plan_count_kernel(PlanGeometry g, const int *__restrict__ S, unsigned *__restrict__ levelCnt,
+                                     unsigned *__restrict__ cell, unsigned *__restrict__ longCnt) {
     const unsigned long long row = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= (unsigned long long)g.n * g.m) return;
     const unsigned blk = (unsigned)(row / g.m) / g.Sb;
     const unsigned rowLocal = (unsigned)(row - (unsigned long long)blk * g.Sb * g.m);
     const int *Sr = S + row * g.ns;
-    unsigned runTile = 0xFFFFFFFFu, q = 0;
-    for (unsigned l = 0; l < g.ns; l++) {
-        const int sp = Sr[l];
-        if (sp < 0) break;
-        const unsigned t = (unsigned)sp / g.Vt;
-        q = t == runTile ? q + 1 : 0;
-        runTile = t;
-        atomicAdd(counts + g.sub(blk, t, rowLocal) + q, 1u);
-    }
+    for_each_run(Sr, g.ns, g.Vt, [&](unsigned t, unsigned l0, unsigned len) {
+        const size_t c = (size_t)blk * g.T + t;
+        for (unsigned q = 0; q < len; q++) atomicAdd(levelCnt + c * g.L + q, 1u);
+        if (len == 1) atomicAdd(cell + c * 1024 + run_cell(rowLocal, (unsigned)Sr[l0] - t * g.Vt), 1u);
+        else atomicAdd(longCnt + c * (g.L + 1) + len, 1u);
+    });
 }
 
-// Write every record to its sub-bin. One thread per (block, warp) owns all
-// sub-bins of that warp's row range and walks its rows in order, so each
-// sub-bin lists its rows in ascending order (fewer shared-memory bank
-// conflicts on the partial sums) and the plan does not depend on timing.
-__global__ void vi_plan_fill_kernel(PlanGeometry g, unsigned blocks, const int *__restrict__ S,
-                                    const float *__restrict__ Tm, const unsigned *__restrict__ start,
-                                    unsigned *cursor, uint2 *rec) {
-    const unsigned idx = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned blk = idx / kWarps, w = idx % kWarps;
-    if (blk >= blocks) return;
-    const unsigned nsb = min(g.Sb, g.n - blk * g.Sb);
-    const unsigned rowsBlk = nsb * g.m;
-    const unsigned r0 = w * g.rowsPerWarp, r1 = min(rowsBlk, r0 + g.rowsPerWarp);
-    for (unsigned rowLocal = r0; rowLocal < r1; rowLocal++) {
-        const unsigned long long row = (unsigned long long)blk * g.Sb * g.m + rowLocal;
-        const int *Sr = S + row * g.ns;
-        const float *Tr = Tm + row * g.ns;
-        unsigned runTile = 0xFFFFFFFFu, q = 0;
-        for (unsigned l = 0; l < g.ns; l++) {
-            const int sp = Sr[l];
-            if (sp < 0) break;
-            const unsigned t = (unsigned)sp / g.Vt;
-            q = t == runTile ? q + 1 : 0;
-            runTile = t;
-            const size_t sb = g.sub(blk, t, rowLocal) + q;
-            const unsigned c = cursor[sb];
-            cursor[sb] = c + 1;
-            rec[start[sb] + c] =
-                make_uint2((rowLocal << 16) | ((unsigned)sp - t * g.Vt), __float_as_uint(fmul(g.gamma, Tr[l])));
+// Per chunk: its record count; each partial-sum bank's bucket size (bsize)
+// and, in place, the bucket's exclusive prefix over distances (cell); the
+// long runs' exclusive prefix by length, longest first (longCnt).
+__global__ void vi_plan_chunk_kernel(unsigned nChunks, unsigned L, const unsigned *__restrict__ levelCnt,
+                                     unsigned *__restrict__ cell, unsigned *__restrict__ bsize,
+                                     unsigned *__restrict__ longCnt, unsigned *__restrict__ chunkSize) {
+    const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nChunks) return;
+    unsigned total = 0;
+    for (unsigned q = 0; q < L; q++) total += levelCnt[c * L + q];
+    chunkSize[c] = total;
+    for (unsigned qb = 0; qb < 32; qb++) {
+        unsigned *b = cell + c * 1024 + qb * 32;
+        unsigned run = 0;
+        for (unsigned d = 0; d < 32; d++) {
+            const unsigned v = b[d];
+            b[d] = run;
+            run += v;
         }
+        bsize[c * 32 + qb] = run;
+    }
+    unsigned run = 0;
+    for (unsigned len = L; len >= 2; len--) {
+        unsigned *p = longCnt + c * (L + 1) + len;
+        const unsigned v = *p;
+        *p = run;
+        run += v;
     }
 }
 
-// Final layout. Slice sl = (block, tile, warp) holds levels 0..L-1, each
-// sorted by row. The run length of a row (the number of levels it appears
-// in) is found from the deepest level up; the final slice lists, level after
-// level, the rows of that level ordered by (run length descending, row), so
-// level q+1 is a prefix-aligned continuation of level q, and each level
-// after the first starts at least 64 records after the previous one (padding
-// records in between). Two records of one row are then always at least 64
-// positions apart: any 64 consecutive records have distinct rows.
-__global__ void vi_plan_len_kernel(unsigned nSlices, unsigned L, const unsigned *__restrict__ ls,
-                                   const uint2 *__restrict__ recL, unsigned char *__restrict__ len) {
-    const unsigned sl = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sl >= nSlices) return;
-    const size_t base = (size_t)sl * L;
-    for (int q = (int)L - 1; q >= 0; q--) {
-        const unsigned e0 = ls[base + q], e1 = ls[base + q + 1];
-        if (q == (int)L - 1) {
-            for (unsigned e = e0; e < e1; e++) len[e] = (unsigned char)L;
-            continue;
+// Write every record at its place. The position j of a run in its chunk's
+// levels: long runs first, by length (ties in the order threads arrive,
+// which changes nothing: the rows of one chunk are distinct), then the
+// single-record runs dealt round-robin over the 32 partial-sum banks, the
+// k-th run of a bank's bucket (sorted by distance) in round k.
+__global__ void vi_plan_fill_kernel(PlanGeometry g, const int *__restrict__ S, const float *__restrict__ Tm,
+                                    const unsigned *__restrict__ chunkStart, const unsigned *__restrict__ levelCnt,
+                                    unsigned *__restrict__ cell, const unsigned *__restrict__ bsize,
+                                    unsigned *__restrict__ longCnt, uint2 *__restrict__ rec) {
+    const unsigned long long row = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= (unsigned long long)g.n * g.m) return;
+    const unsigned blk = (unsigned)(row / g.m) / g.Sb;
+    const unsigned rowLocal = (unsigned)(row - (unsigned long long)blk * g.Sb * g.m);
+    const int *Sr = S + row * g.ns;
+    const float *Tr = Tm + row * g.ns;
+    for_each_run(Sr, g.ns, g.Vt, [&](unsigned t, unsigned l0, unsigned len) {
+        const size_t c = (size_t)blk * g.T + t;
+        unsigned j;
+        if (len >= 2) {
+            j = atomicAdd(longCnt + c * (g.L + 1) + len, 1u);
+        } else {
+            const unsigned ce = run_cell(rowLocal, (unsigned)Sr[l0] - t * g.Vt);
+            const unsigned qb = ce >> 5;
+            const unsigned rank = atomicAdd(cell + c * 1024 + ce, 1u);
+            j = g.L > 1 ? levelCnt[c * g.L + 1] : 0u;   // the long runs come first
+            const unsigned *bs = bsize + c * 32;
+            for (unsigned b = 0; b < 32; b++) {
+                const unsigned sz = bs[b];
+                j += min(sz, rank) + ((b < qb && sz > rank) ? 1u : 0u);
+            }
         }
-        unsigned p = e1;  // level q+1 starts where level q ends
-        const unsigned p1 = ls[base + q + 2];
-        for (unsigned e = e0; e < e1; e++) {
-            const unsigned row = recL[e].x >> 16;
-            while (p < p1 && (recL[p].x >> 16) < row) p++;
-            len[e] = (p < p1 && (recL[p].x >> 16) == row) ? len[p] : (unsigned char)(q + 1);
+        unsigned base = chunkStart[c];
+        for (unsigned q = 0; q < len; q++) {
+            const unsigned sp = (unsigned)Sr[l0 + q];
+            rec[base + j] = make_uint2((rowLocal << 16) | (sp - t * g.Vt), __float_as_uint(fmul(g.gamma, Tr[l0 + q])));
+            base += levelCnt[c * g.L + q];
         }
-    }
-}
-
-__device__ __forceinline__ unsigned slice_levels(const unsigned *ls, size_t base, unsigned L) {
-    unsigned q = 0;
-    while (q < L && ls[base + q + 1] > ls[base + q]) q++;
-    return q;
-}
-
-__global__ void vi_plan_size_kernel(unsigned nSlices, unsigned L, const unsigned *__restrict__ ls,
-                                    unsigned *__restrict__ size) {
-    const unsigned sl = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sl >= nSlices) return;
-    const size_t base = (size_t)sl * L;
-    const unsigned Ls = slice_levels(ls, base, L);
-    unsigned pos = 0;
-    for (unsigned q = 0; q < Ls; q++) {
-        const unsigned start = pos;
-        pos += ls[base + q + 1] - ls[base + q];
-        if (q + 1 < Ls) pos = max(pos, start + 64u);
-    }
-    size[sl] = pos;
-}
-
-__global__ void vi_plan_order_kernel(unsigned nSlices, unsigned L, const unsigned *__restrict__ ls,
-                                     const uint2 *__restrict__ recL, const unsigned char *__restrict__ len,
-                                     const unsigned *__restrict__ sliceStart, uint2 *__restrict__ rec) {
-    const unsigned sl = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sl >= nSlices) return;
-    const size_t base = (size_t)sl * L;
-    const unsigned Ls = slice_levels(ls, base, L);
-    uint2 *out = rec + sliceStart[sl];
-    unsigned pos = 0;
-    for (unsigned q = 0; q < Ls; q++) {
-        const unsigned start = pos;
-        const unsigned e0 = ls[base + q], e1 = ls[base + q + 1];
-        for (unsigned l = Ls; l > q; l--)
-            for (unsigned e = e0; e < e1; e++)
-                if (len[e] == l) out[pos++] = recL[e];
-        if (q + 1 < Ls) pos = max(pos, start + 64u);  // padding slots keep the sentinel
-    }
+    });
 }
 
 // Exclusive scan of in[0..N) into out[0..N] (out[N] = total) in three
@@ -427,12 +445,11 @@ bool try_alloc(T **p, size_t count) {
 
 void release(ViTilePlan *plan) {
     cudaFree(plan->rec);
-    cudaFree(plan->levelStart);
-    cudaFree(plan->sliceStart);
-    cudaFree(plan->counts);
+    cudaFree(plan->chunkStart);
+    cudaFree(plan->levelCnt);
     cudaFree(plan->flags);
     plan->rec = nullptr;
-    plan->levelStart = plan->sliceStart = plan->counts = plan->flags = nullptr;
+    plan->chunkStart = plan->levelCnt = plan->flags = nullptr;
 }
 
 int scan_counts(const unsigned *counts, unsigned long long N, unsigned *out, cudaStream_t stream, const char *fn) {
@@ -527,107 +544,67 @@ int vi_plan_build(ViTilePlan *plan, const MDP *mdp, const int *S, const float *T
         return rc;
     }
     const unsigned L = std::max(hflags[2], 1u);
-    if (hflags[0] != 0 || hflags[1] != 0 || L > 31) {
+    if (hflags[0] != 0 || hflags[1] != 0 || L > kMaxLevels) {
         release(plan);
         return NOVA_SUCCESS;
     }
-    PlanGeometry g{n, m, ns, Vt, tiles, Sb, ceil_div((unsigned long long)Sb * m, kWarps), L, mdp->gamma};
-    const unsigned long long nSub = (unsigned long long)blocks * tiles * kWarps * L;
-    if (nSub >= (1ull << 32) - 1) { release(plan); return NOVA_SUCCESS; }
+    const PlanGeometry g{n, m, ns, Vt, tiles, Sb, L, mdp->gamma};
+    const unsigned long long nChunks = (unsigned long long)blocks * tiles;
+    if (nChunks * 1024ull >= (1ull << 32) || nChunks * (L + 1) >= (1ull << 32)) { release(plan); return NOVA_SUCCESS; }
 
-    // Pass 2: sub-bin sizes and their exclusive scan.
-    if (!try_alloc(&plan->counts, nSub) || !try_alloc(&plan->levelStart, nSub + 1)) {
+    // Pass 2: per-chunk counts (levels, bank cells, long runs).
+    unsigned *cell = nullptr, *bsize = nullptr, *longCnt = nullptr, *chunkSize = nullptr;
+    auto freeScratch = [&]() {
+        cudaFree(cell); cudaFree(bsize); cudaFree(longCnt); cudaFree(chunkSize);
+        cell = bsize = longCnt = chunkSize = nullptr;
+    };
+    if (!try_alloc(&plan->levelCnt, nChunks * L) || !try_alloc(&cell, nChunks * 1024) ||
+            !try_alloc(&bsize, nChunks * 32) || !try_alloc(&longCnt, nChunks * (L + 1)) ||
+            !try_alloc(&chunkSize, nChunks) || !try_alloc(&plan->chunkStart, nChunks + 1)) {
+        freeScratch();
         release(plan);
         return NOVA_SUCCESS;
     }
-    if (cudaMemsetAsync(plan->counts, 0, nSub * sizeof(unsigned), stream) != cudaSuccess) {
+    if (cudaMemsetAsync(plan->levelCnt, 0, nChunks * L * sizeof(unsigned), stream) != cudaSuccess ||
+            cudaMemsetAsync(cell, 0, nChunks * 1024 * sizeof(unsigned), stream) != cudaSuccess ||
+            cudaMemsetAsync(longCnt, 0, nChunks * (L + 1) * sizeof(unsigned), stream) != cudaSuccess) {
         cudaGetLastError();
+        freeScratch();
         release(plan);
         NOVA_ERR(fn, "Failed to clear the sweep plan counters.");
         return NOVA_ERROR_KERNEL_EXECUTION;
     }
-    vi_plan_count_kernel<<<rowBlocks, 256, 0, stream>>>(g, S, plan->counts);
-    if ((rc = check_launch(fn, "sweep plan (count)")) != NOVA_SUCCESS) { release(plan); return rc; }
-    rc = scan_counts(plan->counts, nSub, plan->levelStart, stream, fn);
-    if (rc == NOVA_ERROR_DEVICE_MALLOC) { release(plan); return NOVA_SUCCESS; }
-    if (rc != NOVA_SUCCESS) { release(plan); return rc; }
-    unsigned total = 0;
-    if ((rc = d2h(&total, plan->levelStart + nSub, sizeof(unsigned), fn, "the sweep plan size")) != NOVA_SUCCESS) {
-        release(plan);
-        return rc;
-    }
-
-    // Pass 3: records (one spare at the end: the sweep reads them in pairs).
-    if (!try_alloc(&plan->rec, (size_t)total + 1)) { release(plan); return NOVA_SUCCESS; }
-    if (cudaMemsetAsync(plan->counts, 0, nSub * sizeof(unsigned), stream) != cudaSuccess) {
-        cudaGetLastError();
-        release(plan);
-        NOVA_ERR(fn, "Failed to clear the sweep plan cursors.");
-        return NOVA_ERROR_KERNEL_EXECUTION;
-    }
-    if (cudaMemsetAsync(plan->rec + total, 0xFF, sizeof(uint2), stream) != cudaSuccess) {
-        cudaGetLastError();
-        release(plan);
-        NOVA_ERR(fn, "Failed to clear the sweep plan records.");
-        return NOVA_ERROR_KERNEL_EXECUTION;
-    }
-    vi_plan_fill_kernel<<<ceil_div((unsigned long long)blocks * kWarps, 128), 128, 0, stream>>>(
-        g, blocks, S, T, plan->levelStart, plan->counts, plan->rec);
-    if ((rc = check_launch(fn, "sweep plan (fill)")) != NOVA_SUCCESS) { release(plan); return rc; }
-    if ((rc = sync_device(fn)) != NOVA_SUCCESS) { release(plan); return rc; }
-    cudaFree(plan->counts);
-    cudaFree(plan->flags);
-    plan->counts = plan->flags = nullptr;
-
-    // Pass 4: the final layout (rows by run length, levels 64 records apart).
-    const unsigned nSlices = (unsigned)((unsigned long long)blocks * tiles * kWarps);
-    unsigned char *len = nullptr;
-    unsigned *sliceSize = nullptr;
-    uint2 *rec2 = nullptr;
-    if (!try_alloc(&len, (size_t)total + 1) || !try_alloc(&sliceSize, nSlices) ||
-            !try_alloc(&plan->sliceStart, (size_t)nSlices + 1)) {
-        cudaFree(len);
-        cudaFree(sliceSize);
-        release(plan);
-        return NOVA_SUCCESS;
-    }
-    const unsigned sliceBlocks = ceil_div(nSlices, 128);
-    vi_plan_len_kernel<<<sliceBlocks, 128, 0, stream>>>(nSlices, L, plan->levelStart, plan->rec, len);
-    rc = check_launch(fn, "sweep plan (run lengths)");
+    vi_plan_count_kernel<<<rowBlocks, 256, 0, stream>>>(g, S, plan->levelCnt, cell, longCnt);
+    rc = check_launch(fn, "sweep plan (count)");
     if (rc == NOVA_SUCCESS) {
-        vi_plan_size_kernel<<<sliceBlocks, 128, 0, stream>>>(nSlices, L, plan->levelStart, sliceSize);
-        rc = check_launch(fn, "sweep plan (slice sizes)");
+        vi_plan_chunk_kernel<<<ceil_div(nChunks, 128), 128, 0, stream>>>((unsigned)nChunks, L, plan->levelCnt, cell,
+                                                                         bsize, longCnt, chunkSize);
+        rc = check_launch(fn, "sweep plan (chunks)");
     }
-    if (rc == NOVA_SUCCESS) rc = scan_counts(sliceSize, nSlices, plan->sliceStart, stream, fn);
-    unsigned total2 = 0;
+    if (rc == NOVA_SUCCESS) rc = scan_counts(chunkSize, nChunks, plan->chunkStart, stream, fn);
+    unsigned total = 0;
     if (rc == NOVA_SUCCESS)
-        rc = d2h(&total2, plan->sliceStart + nSlices, sizeof(unsigned), fn, "the sweep plan size");
-    // Small slices pay a lot of padding; in automatic mode such models keep
-    // the per-row sweep.
-    if (rc == NOVA_SUCCESS && mode == NOVA_VI_TILING_AUTO && (double)total2 > 1.5 * (double)total)
-        rc = NOVA_ERROR_DEVICE_MALLOC;
-    if (rc == NOVA_SUCCESS && !try_alloc(&rec2, (size_t)total2 + 1)) rc = NOVA_ERROR_DEVICE_MALLOC;
-    if (rc == NOVA_SUCCESS && cudaMemsetAsync(rec2, 0xFF, ((size_t)total2 + 1) * sizeof(uint2), stream) != cudaSuccess) {
+        rc = d2h(&total, plan->chunkStart + nChunks, sizeof(unsigned), fn, "the sweep plan size");
+    // Pass 3: the records (two spare ones at the end for the bulk prefetch).
+    if (rc == NOVA_SUCCESS && !try_alloc(&plan->rec, (size_t)total + 2)) rc = NOVA_ERROR_DEVICE_MALLOC;
+    if (rc == NOVA_SUCCESS &&
+            cudaMemsetAsync(plan->rec, 0xFF, ((size_t)total + 2) * sizeof(uint2), stream) != cudaSuccess) {
         cudaGetLastError();
         rc = NOVA_ERROR_KERNEL_EXECUTION;
     }
     if (rc == NOVA_SUCCESS) {
-        vi_plan_order_kernel<<<sliceBlocks, 128, 0, stream>>>(nSlices, L, plan->levelStart, plan->rec, len,
-                                                              plan->sliceStart, rec2);
-        rc = check_launch(fn, "sweep plan (order)");
+        vi_plan_fill_kernel<<<rowBlocks, 256, 0, stream>>>(g, S, T, plan->chunkStart, plan->levelCnt, cell, bsize,
+                                                           longCnt, plan->rec);
+        rc = check_launch(fn, "sweep plan (fill)");
     }
     if (rc == NOVA_SUCCESS) rc = sync_device(fn);
-    cudaFree(len);
-    cudaFree(sliceSize);
+    freeScratch();
     if (rc != NOVA_SUCCESS) {
-        cudaFree(rec2);
         release(plan);
         return rc == NOVA_ERROR_DEVICE_MALLOC ? NOVA_SUCCESS : rc;  // kGather
     }
-    cudaFree(plan->rec);
-    cudaFree(plan->levelStart);
-    plan->levelStart = nullptr;
-    plan->rec = rec2;
+    cudaFree(plan->flags);
+    plan->flags = nullptr;
     plan->tileStates = Vt;
     plan->tiles = tiles;
     plan->blockStates = Sb;
@@ -643,8 +620,8 @@ int vi_plan_build(ViTilePlan *plan, const MDP *mdp, const int *S, const float *T
 int vi_tiled_sweep(const ViTilePlan *plan, const MDP *mdp, const float *R, const float *V, float *Vp, unsigned *pi,
                    ViDeviceState *st, double tol, int early_exit, cudaStream_t stream, const char *fn) {
     bellman_tiled_kernel<<<plan->grid, kThreads, plan->smemBytes, stream>>>(
-        mdp->n, mdp->m, plan->tileStates, plan->tiles, plan->blockStates, plan->blocks, plan->rec,
-        plan->sliceStart, R, V, Vp, pi, st, tol, early_exit);
+        mdp->n, mdp->m, plan->tileStates, plan->tiles, plan->blockStates, plan->blocks, plan->levels, plan->rec,
+        plan->chunkStart, plan->levelCnt, R, V, Vp, pi, st, tol, early_exit);
     return check_launch(fn, "Bellman update (tiled)");
 }
 

@@ -1175,8 +1175,8 @@ int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsi
 }
 
 bool BackupEngine::state_major_wanted(size_t smemSM) const {
-    return md.n > kStateMajorMinStates && smemSM <= 200 * 1024 && scoring == NOVA_SCORING_FP16 &&
-           lastScanFrac <= 0.01f;
+    return md.n > kStateMajorMinStates && smemSM <= 200 * 1024 &&
+           (scoring == NOVA_SCORING_FP16 || scoring == NOVA_SCORING_BF16) && lastScanFrac <= 0.01f;
 }
 
 bool BackupEngine::fixed_ready() const {
@@ -1679,6 +1679,21 @@ extern "C" int pomdp_pbvi_get_stats_gpu(const POMDPPBVIGPU *pbvi, NovaPBVIStats 
     }
     *stats = ws->eng.stats;
     return NOVA_SUCCESS;
+}
+
+extern "C" int pomdp_pbvi_row_detail_gpu(const POMDPPBVIGPU *pbvi, unsigned int *candidates,
+                                         unsigned int *exactRows) {
+    static const char *fn = "pomdp_pbvi_row_detail_gpu";
+    if (pbvi == nullptr || candidates == nullptr || exactRows == nullptr) {
+        NOVA_ERR(fn, "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    PbviGpuWorkspace *ws = pbvi_gpu_ws(pbvi);
+    if (ws == nullptr || ws->eng.tc == nullptr || ws->eng.stats.tcGroups == 0) {
+        NOVA_ERR(fn, "The solver's last update did not score on the tensor cores.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    return tc_row_detail(ws->eng, candidates, exactRows, fn);
 }
 
 extern "C" int pomdp_pbvi_value_gpu(const POMDP *pomdp, const POMDPPBVIGPU *pbvi, const float *b, double *Vb,

@@ -164,6 +164,9 @@ const unsigned *tc_row_list(const BackupEngine &eng);
 int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, const unsigned **rowList,
              const char *fn);
 void tc_release(TcState *tc);
+// Per-belief detail of the last tensor-core update: alphas re-scored exactly
+// and rows sent to the exact scan, summed over the belief's (a, o) rows.
+int tc_row_detail(const BackupEngine &eng, unsigned *candidates, unsigned *exactRows, const char *fn);
 // Feeds one tensor-core update's scoring time (GEMM, merge and the exact
 // scan it left) to the solver's alpha-group tuner.
 void tc_tune_feedback(BackupEngine &eng, float msScoring, unsigned nU);

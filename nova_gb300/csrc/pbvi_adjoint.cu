@@ -28,6 +28,7 @@
 #include "common.h"
 
 #include <algorithm>
+#include <vector>
 
 #include <nova/constants.h>
 #include <nova/pomdp/pomdp.h>
@@ -212,6 +213,56 @@ struct AdjBuffers {
     }
 };
 
+// Gamma_t from Gamma_{t-1} in FP64 with recorded selections:
+// alpha(s) = R(s,a) + gamma * sum_l T(s,a,l) sum_o O(a,S,o) Gamma_{j_o}(S),
+// every operand widened to FP64 (the same map as replay_kernel without the
+// FP32 roundings; the order of the FP64 sums differs from the reference's).
+__global__ void replay_f64_kernel(AdjModel md, const unsigned *__restrict__ len, const double *__restrict__ Gin,
+                                  const unsigned *__restrict__ act, const unsigned *__restrict__ sel,
+                                  double *__restrict__ Gout) {
+    const unsigned i = blockIdx.x;
+    extern __shared__ unsigned jsh[];  // [z]
+    const unsigned a = min(act[i], md.m - 1);
+    for (unsigned o = threadIdx.x; o < md.z; o += blockDim.x) jsh[o] = min(sel[(size_t)i * md.z + o], md.r - 1);
+    __syncthreads();
+    const double gamma = (double)md.gamma;
+    for (unsigned s = threadIdx.x; s < md.n; s += blockDim.x) {
+        const size_t row = (size_t)s * md.m + a;
+        const unsigned L = len[row];
+        double acc = 0.0;
+        for (unsigned l = 0; l < L; l++) {
+            const unsigned sp = (unsigned)md.S[row * md.ns + l];
+            const float *Orow = md.O + ((size_t)a * md.n + sp) * md.z;
+            double w = 0.0;
+            for (unsigned o = 0; o < md.z; o++) w += (double)Orow[o] * Gin[(size_t)jsh[o] * md.n + sp];
+            acc += (double)md.T[row * md.ns + l] * w;
+        }
+        Gout[(size_t)i * md.n + s] = (double)md.R[row] + gamma * acc;
+    }
+}
+
+__global__ void widen_kernel(const float *__restrict__ in, size_t count, double *__restrict__ out) {
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
+        out[e] = (double)in[e];
+}
+
+// vals[i] = b . Gamma[i] with FP64 alphas.
+__global__ void value_rows_f64_kernel(const double *__restrict__ G, unsigned n, const float *__restrict__ b,
+                                      double *__restrict__ vals) {
+    const unsigned i = blockIdx.x;
+    double acc = 0.0;
+    for (unsigned s = threadIdx.x; s < n; s += blockDim.x) acc += G[(size_t)i * n + s] * (double)b[s];
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    __shared__ double red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (unsigned w = 0; w < blockDim.x / 32; w++) t += red[w];
+        vals[i] = t;
+    }
+}
+
 }  // namespace
 }  // namespace nova_gb300
 
@@ -362,5 +413,74 @@ extern "C" int pomdp_pbvi_execute_recorded_gpu(const POMDP *pomdp, POMDPPBVIGPU 
                                               d_selects + (size_t)t * pomdp->r * pomdp->z);
         if (rc != NOVA_SUCCESS) return rc;
     }
+    return NOVA_SUCCESS;
+}
+
+extern "C" int pomdp_pbvi_value_replay_f64_gpu(const POMDP *pomdp, unsigned int horizon, const float *d_Gamma0,
+                                               const unsigned int *d_actions, const unsigned int *d_selects,
+                                               const float *d_b, unsigned int alpha, double *Vb,
+                                               unsigned int *bestAlpha) {
+    static const char *fn = "pomdp_pbvi_value_replay_f64_gpu";
+    if (pomdp == nullptr || pomdp->n == 0 || pomdp->ns == 0 || pomdp->m == 0 || pomdp->z == 0 || pomdp->r == 0 ||
+            pomdp->d_S == nullptr || pomdp->d_T == nullptr || pomdp->d_O == nullptr || pomdp->d_R == nullptr ||
+            d_Gamma0 == nullptr || (horizon > 0 && (d_actions == nullptr || d_selects == nullptr)) ||
+            d_b == nullptr || Vb == nullptr) {
+        NOVA_ERR(fn, "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    AdjModel md{pomdp->n, pomdp->ns, pomdp->m, pomdp->z, pomdp->r, pomdp->gamma,
+                pomdp->d_S, pomdp->d_T, pomdp->d_O, pomdp->d_R};
+    const unsigned n = md.n, r = md.r, z = md.z, m = md.m, ns = md.ns;
+    const size_t rn = (size_t)r * n;
+    unsigned *len = nullptr;
+    double *GA = nullptr, *GB = nullptr, *vals = nullptr;
+    int rc;
+    auto cleanup = [&]() {
+        cudaDeviceSynchronize();
+        cudaFree(len); cudaFree(GA); cudaFree(GB); cudaFree(vals);
+    };
+    if ((rc = dev_alloc(&len, (size_t)n * m, fn, "the successor lengths")) != NOVA_SUCCESS ||
+            (rc = dev_alloc(&GA, rn, fn, "the FP64 alphas")) != NOVA_SUCCESS ||
+            (rc = dev_alloc(&GB, rn, fn, "the FP64 alphas")) != NOVA_SUCCESS ||
+            (rc = dev_alloc(&vals, r, fn, "the values")) != NOVA_SUCCESS) {
+        cleanup();
+        return rc;
+    }
+    adj_len_kernel<<<ceil_div((size_t)n * m, 256), 256>>>(n * m, ns, md.S, len);
+    if ((rc = check_launch(fn, "successor lengths")) == NOVA_SUCCESS) {
+        widen_kernel<<<(unsigned)std::min<size_t>(ceil_div(rn, 256), 65535u * 8u), 256>>>(d_Gamma0, rn, GA);
+        rc = check_launch(fn, "FP64 alphas");
+    }
+    for (unsigned t = 0; t < horizon && rc == NOVA_SUCCESS; t++) {
+        replay_f64_kernel<<<r, 256, z * sizeof(unsigned)>>>(md, len, GA, d_actions + (size_t)t * r,
+                                                             d_selects + (size_t)t * r * z, GB);
+        rc = check_launch(fn, "FP64 replay");
+        std::swap(GA, GB);
+    }
+    if (rc == NOVA_SUCCESS) {
+        value_rows_f64_kernel<<<r, 256>>>(GA, n, d_b, vals);
+        rc = check_launch(fn, "FP64 values");
+    }
+    if (rc == NOVA_SUCCESS) rc = sync_device(fn);
+    std::vector<double> hv;
+    if (rc == NOVA_SUCCESS) {
+        hv.resize(r);
+        rc = d2h(hv.data(), vals, r * sizeof(double), fn, "the values");
+    }
+    cleanup();
+    if (rc != NOVA_SUCCESS) return rc;
+    // The given alpha, or the maximum from the -1e10 start with the lowest
+    // index on ties (pomdp_alpha_vectors.cpp:52-79).
+    unsigned best = alpha;
+    double V = (double)NOVA_FLT_MIN;
+    if (alpha < r) {
+        V = hv[alpha];
+    } else {
+        best = 0;
+        for (unsigned i = 0; i < r; i++)
+            if (hv[i] > V) { V = hv[i]; best = i; }
+    }
+    *Vb = V;
+    if (bestAlpha != nullptr) *bestAlpha = best;
     return NOVA_SUCCESS;
 }

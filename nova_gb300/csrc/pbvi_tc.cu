@@ -5,29 +5,33 @@
 //           = sum_s A_ao[i,s] * Gamma_j[s],
 //     A_ao[i,s] = gamma * O(a,s,o) * sum_{k,l : S(s_k,a,l) = s} B[i,k] T(s_k,a,l),
 // a dense (r x n) . (n x |Gamma|) product per (a,o) pair. A_ao does not
-// depend on Gamma: it is built once in BF16 ([m*z][rPad][nPad], K-major).
-// Each update packs the unique alphas, shifted by a per-state midpoint c[s]
-// (which changes every score of a row by the same amount), into BF16, and
-// the GEMM scores every row against every unique alpha on the tcgen05
-// tensor cores with FP32 accumulation in TMEM. The epilogue keeps, per row,
-// the 8 best (score, alpha) pairs of each list and the best score it
-// dropped; the scores never reach HBM.
+// depend on Gamma: it is built once in FP16 or BF16 ([m*z][rPad][nPad],
+// K-major, each row scaled by a power of two). Each update packs the unique
+// alphas, shifted by a per-state midpoint c[s] (which changes every score of
+// a row by the same amount), into FP16 -- or, for BF16, into a pair of BF16
+// terms hi + lo whose sum carries 16 bits -- and the GEMM scores every row
+// against every unique alpha on the tcgen05 tensor cores with FP32
+// accumulation in TMEM. The epilogue keeps, per row, the best (score, alpha)
+// pairs of each list and the best score it dropped; the scores never reach
+// HBM.
 //
 // Exactness: for every row the kernel's score differs from the reference's
 // FP32 score (pomdp_pbvi_cpu.cpp:50-83) by at most
-//     E = a1 * (U * gmax + g_N * Gmax)
-// (a1 = sum_s |A_ao[i,s]|, gmax = max |Gamma - c|, Gmax = max |Gamma|;
-// U covers the BF16 rounding of both operands, the FP32 build of A and the
-// tensor-core accumulation over nPad terms; g_N = (ns + rz + 3) * 2^-24
-// covers the reference's own rounding). Every alpha within 2E of the best is
-// re-scored in the reference's exact FP32 order and the argmax taken there;
-// if the dropped-score bound says a candidate may be missing, the (belief,
-// action) pair is rescanned exactly over all alphas. The chosen alphas are
-// therefore exactly the reference's.
+//     E = a1 * (U * gmax + g_N * Gmax) + d1 * gmax
+// (a1 = sum_s |A_ao[i,s]|, d1 = sum_s |A_ao[i,s] - half(A_ao[i,s])| the row's
+// measured operand rounding, gmax = max |Gamma - c|, Gmax = max |Gamma|; U
+// covers the rounding of the alphas, the FP32 build of A and the tensor-core
+// accumulation; g_N = (ns + rz + 3) * 2^-24 covers the reference's own
+// rounding). Every alpha within 2E of the best is re-scored in the
+// reference's exact FP32 order and the argmax taken there; if the
+// dropped-score bound says a candidate may be missing, the (belief, action)
+// pair is rescanned exactly over all alphas. The chosen alphas are therefore
+// exactly the reference's.
 //
 // GEMM kernel: persistent, one CTA per SM, 10 warps: warp 0 issues TMA loads
 // (SWIZZLE_128B tiles 128x64 of A and 256x64 of the alphas into a 4-stage
-// ring), warp 1 issues tcgen05.mma (M=128, N=256, K=16, cta_group::1) into
+// ring; with split alphas each A tile is loaded for the hi and then for the
+// lo block), warp 1 issues tcgen05.mma (M=128, N=256, K=16, cta_group::1) into
 // two 256-column TMEM accumulators, warps 2-9 drain TMEM with tcgen05.ld
 // (two warps per lane quarter, alternate 32-column chunks) and run the top-8
 // epilogue, skipping scores that lie below the row's margin under the
@@ -45,6 +49,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <vector>
 #include <cmath>
 
 namespace nova_gb300 {
@@ -70,9 +75,10 @@ constexpr int BM = 128;            // rows (beliefs) per tile
 constexpr int BN = 256;            // alphas per tile
 constexpr int BK = 64;             // K (states) per stage: 128 bytes of BF16
 constexpr int STAGES = 4;
-constexpr int MAX_TOPK = 16;       // entries per candidate list (layout capacity)
+constexpr int MAX_TOPK = 32;       // entries per candidate list (layout capacity)
 constexpr int MAX_LISTS = 8;       // candidate lists per row: two per alpha group
 constexpr int MAX_ENTRIES = MAX_LISTS * MAX_TOPK;
+constexpr int kLaneEntries = MAX_ENTRIES / 32;   // list entries per lane in the merge
 constexpr unsigned kNoneU = 0xffffffffu;
 constexpr int A_STAGE_BYTES = BM * BK * 2;   // 16 KB
 constexpr int B_STAGE_BYTES = BN * BK * 2;   // 32 KB
@@ -88,13 +94,15 @@ struct TcState {
     uint16_t *A = nullptr;          // [MZ][rPad][nPad] BF16 or FP16 bits, each row scaled by a power of 2
     float *a1 = nullptr;            // [MZ][rPad] bound of sum_s |A| in the row's scaled units
     float *a1raw = nullptr;         // [MZ][rPad] the same bound unscaled
-    uint16_t *Gb = nullptr;         // [capN][nPad] BF16 or FP16 bits of (alpha - c) * 2^gexp
+    float *d1 = nullptr;            // [MZ][rPad] sum_s |A - half(A)| (scaled units): A's actual operand rounding
+    uint16_t *Gb = nullptr;         // [capN][nPad] FP16, or [capN][2 nPad] split BF16, bits of (alpha - c) * 2^gexp
     float *shift = nullptr;         // [n]
-    unsigned *scal = nullptr;       // [0] gmax, [1] Gmax, [2] escale, [3..4] counters, [5] max half-range, [6] G scale (float bits)
+    unsigned *scal = nullptr;       // [0] gmax, [1] Gmax, [2] escale, [3..4] counters, [5] max half-range, [6] G scale, [7] dscale (float bits)
     float *candV = nullptr;         // [MZ][r][MAX_LISTS][MAX_TOPK] (the first K entries of each list used)
     unsigned *candU = nullptr;
     float *candX = nullptr;         // [MZ][r][MAX_LISTS]
     unsigned *rowFlag = nullptr;    // [MZ*r] rows needing the exact scan
+    unsigned *rowCand = nullptr;    // [MZ*r] alphas each row re-scored exactly in the merge
     unsigned *rowList = nullptr;    // [MZ*r] their indices, compacted
     unsigned *chunkCount = nullptr; // [ceil(MZ*r / 4096)] flagged rows per chunk, then chunk offsets
     unsigned *badModel = nullptr;   // [1] set when a probability is negative or NaN
@@ -112,22 +120,26 @@ struct TcState {
     unsigned tuneNext = 0;          // next trial
     bool tuneWarm = false;          // the first tensor-core update (lazy set-up) is not timed
     unsigned groupsUsed = 0;        // groups of the last launch
-    float tuneCost[3] = {0, 0, 0};
+    float tuneCost[3] = {0, 0, 0};   // one per tuned schedule
 };
 
 // Schedules: alpha groups per row tile and entries per candidate list.
 struct TcSchedule {
     unsigned groups, topk;
 };
-constexpr TcSchedule kSchedules[3] = {{4u, 16u}, {4u, 8u}, {2u, 8u}};
+constexpr TcSchedule kSchedules[4] = {{4u, 16u}, {4u, 8u}, {2u, 8u}, {4u, 32u}};
+constexpr int kTunedSchedules = 3;  // the first three are timed on small models
+// Deep contractions use the most lists without tuning: FP16 with 16 entries
+// per list; BF16, whose margin admits several times more candidates, 32.
+constexpr int kDeepScheduleFp16 = 0, kDeepScheduleBf16 = 3;
 // Deep contractions keep the epilogue hidden behind the MMAs; they use the
 // most lists (best resolution) without tuning.
 constexpr size_t kTuneMaxNPad = 2048;
 
 void tc_release(TcState *tc) {
     if (!tc) return;
-    cudaFree(tc->A); cudaFree(tc->a1); cudaFree(tc->a1raw); cudaFree(tc->Gb); cudaFree(tc->shift); cudaFree(tc->scal);
-    cudaFree(tc->candV); cudaFree(tc->candU); cudaFree(tc->candX); cudaFree(tc->rowFlag); cudaFree(tc->rowList);
+    cudaFree(tc->A); cudaFree(tc->a1); cudaFree(tc->a1raw); cudaFree(tc->d1); cudaFree(tc->Gb); cudaFree(tc->shift); cudaFree(tc->scal);
+    cudaFree(tc->candV); cudaFree(tc->candU); cudaFree(tc->candX); cudaFree(tc->rowFlag); cudaFree(tc->rowCand); cudaFree(tc->rowList);
     cudaFree(tc->chunkCount);
     cudaFree(tc->badModel);
     if (tc->g0) cudaEventDestroy(tc->g0);
@@ -338,12 +350,21 @@ __device__ __forceinline__ float chunk_select(const float (&v)[32], unsigned c) 
     return t[0];
 }
 
+// Twice the row's proven error bound (scaled units): the score gap within
+// which an alpha may still be the exact argmax. The GEMM's filter and the
+// merge's cut use this same expression.
+__device__ __forceinline__ float row_margin(const float *__restrict__ a1, const float *__restrict__ d1, size_t idx,
+                                            float escale, float dscale) {
+    return 2.0f * (a1[idx] * escale + d1[idx] * dscale);
+}
+
 template <int K>
 __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
         const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, uint32_t idesc,
         unsigned MZ, unsigned rPad, unsigned r, unsigned mTiles, unsigned nTiles, unsigned groups, unsigned nU,
-        unsigned kBlocks, const float *__restrict__ a1, const unsigned *__restrict__ scal,
-        float *__restrict__ candV, unsigned *__restrict__ candU, float *__restrict__ candX) {
+        unsigned kBlocks, unsigned kSplit, const float *__restrict__ a1, const float *__restrict__ d1,
+        const unsigned *__restrict__ scal, float *__restrict__ candV, unsigned *__restrict__ candU,
+        float *__restrict__ candX) {
     extern __shared__ uint8_t smemRaw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~(uintptr_t)1023);
     uint8_t *sA = smem;
@@ -385,11 +406,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
                 decode_unit(unit, groups, mTiles, nTiles, ao, mt, g, nt0, nt1);
                 const int rowA = (int)(ao * rPad + mt * BM);
                 for (unsigned nt = nt0; nt < nt1 && !*abortFlag; nt++) {
-                    for (unsigned kb = 0; kb < kBlocks; kb++) {
+                    // kSplit B blocks per A block: the split alphas carry a hi
+                    // and a lo block for each 64-state block of A.
+                    for (unsigned kb = 0; kb < kBlocks * kSplit; kb++) {
                         if (!mbar_wait(smem_u32(&bar->empty[stage]), phase ^ 1u, abortFlag)) break;
                         const uint32_t fb = smem_u32(&bar->full[stage]);
                         mbar_expect_tx(fb, A_STAGE_BYTES + B_STAGE_BYTES);
-                        tma_load_2d(smem_u32(sA + stage * A_STAGE_BYTES), &tmA, (int)(kb * BK), rowA, fb);
+                        tma_load_2d(smem_u32(sA + stage * A_STAGE_BYTES), &tmA, (int)((kb / kSplit) * BK), rowA, fb);
                         tma_load_2d(smem_u32(sB + stage * B_STAGE_BYTES), &tmB, (int)(kb * BK), (int)(nt * BN), fb);
                         if (++stage == STAGES) { stage = 0; phase ^= 1u; }
                     }
@@ -407,7 +430,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
                     if (!mbar_wait(smem_u32(&bar->accEmpty[acc]), accPhase ^ 1u, abortFlag)) break;
                     tc_fence_after();
                     const uint32_t dtmem = tmem + acc * BN;
-                    for (unsigned kb = 0; kb < kBlocks; kb++) {
+                    for (unsigned kb = 0; kb < kBlocks * kSplit; kb++) {
                         if (!mbar_wait(smem_u32(&bar->full[stage]), phase, abortFlag)) break;
                         tc_fence_after();
                         const uint64_t adesc = smem_desc_sw128(smem_u32(sA + stage * A_STAGE_BYTES));
@@ -444,6 +467,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
         const unsigned half = (warp - 2u) >> 2;
         const unsigned rowInTile = quarter * 32u + lane;
         const float escale = __uint_as_float(scal[2]);
+        const float dscale = __uint_as_float(scal[7]);
         const float qnan = __uint_as_float(0x7fc00000u);
         unsigned acc = 0, accPhase = 0;
         TopList<K> top;
@@ -455,7 +479,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
             // Same expression as the merge's margin. An infinite margin skips
             // nothing; a NaN one skips everything, and the merge sends such
             // rows to the exact scan whatever their lists hold.
-            const float thr = iRow < r ? 2.0f * a1[(size_t)ao * rPad + iRow] * escale : INFINITY;
+            const float thr = iRow < r ? row_margin(a1, d1, (size_t)ao * rPad + iRow, escale, dscale) : INFINITY;
             float best = -INFINITY, lim = -INFINITY;
             bool ok = true;
             for (unsigned nt = nt0; nt < nt1; nt++) {
@@ -531,11 +555,16 @@ __device__ __forceinline__ uint16_t to_half_bits(float v, bool fp16) {
     if (fp16) return __half_as_ushort(__float2half_rn(v));
     return __bfloat16_as_ushort(__float2bfloat16_rn(v));
 }
+__device__ __forceinline__ float from_half_bits(uint16_t b, bool fp16) {
+    if (fp16) return __half2float(__ushort_as_half(b));
+    return __bfloat162float(__ushort_as_bfloat16(b));
+}
 
 __global__ void tc_build_a_kernel(DevModel md, const unsigned *__restrict__ succLen,
                                   const unsigned *__restrict__ suppLen, size_t rPad, size_t nPad, int fp16,
                                   uint16_t *__restrict__ A, float *__restrict__ a1, float *__restrict__ a1raw,
-                                  float a1Slack, unsigned *__restrict__ badModel) {
+                                  float *__restrict__ d1, float a1Slack, float d1Slack,
+                                  unsigned *__restrict__ badModel) {
     extern __shared__ float W[];  // [n]
     const unsigned i = blockIdx.x / md.m, a = blockIdx.x % md.m;
     for (unsigned s = threadIdx.x; s < md.n; s += blockDim.x) W[s] = 0.0f;
@@ -552,7 +581,7 @@ __global__ void tc_build_a_kernel(DevModel md, const unsigned *__restrict__ succ
         }
     }
     __syncthreads();
-    __shared__ float red[32];
+    __shared__ float red[32], redD[32];
     __shared__ float rowScale;
     for (unsigned o = 0; o < md.z; o++) {
         const size_t ao = (size_t)a * md.z + o;
@@ -582,16 +611,26 @@ __global__ void tc_build_a_kernel(DevModel md, const unsigned *__restrict__ succ
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sum;
         __syncthreads();
         const float scale = rowScale;
+        // d1 = sum_s |A - half(A)| in the row's scaled units: the actual
+        // rounding of this row's operand (each term is exact in FP32).
+        float dsum = 0.0f;
         for (unsigned s = threadIdx.x; s < nPad; s += blockDim.x) {
             float v = 0.0f;
             if (s < md.n) v = md.gamma * W[s] * md.O[((size_t)a * md.n + s) * md.z + o];
-            row[s] = to_half_bits(v * scale, fp16 != 0);
+            const float x = v * scale;
+            const uint16_t hb = to_half_bits(x, fp16 != 0);
+            row[s] = hb;
+            dsum += fabsf(x - from_half_bits(hb, fp16 != 0));
         }
+        for (int off = 16; off > 0; off >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, off);
+        if ((threadIdx.x & 31) == 0) redD[threadIdx.x >> 5] = dsum;
+        __syncthreads();
         if (threadIdx.x == 0) {
-            float t = 0.0f;
-            for (unsigned w = 0; w < blockDim.x / 32; w++) t += red[w];
+            float t = 0.0f, d = 0.0f;
+            for (unsigned w = 0; w < blockDim.x / 32; w++) { t += red[w]; d += redD[w]; }
             a1[ao * rPad + i] = t * scale * a1Slack;
             a1raw[ao * rPad + i] = t * a1Slack;
+            d1[ao * rPad + i] = d * d1Slack;
         }
         __syncthreads();
     }
@@ -651,14 +690,20 @@ __global__ void tc_gscale_kernel(unsigned *scal) {
     scal[6] = __float_as_uint(hr < 1e30f ? ldexpf(1.0f, 13 - e) : 1.0f);
 }
 
-// Gb[u][s] = half((alpha_u(s) - c[s]) * gscale); rows >= nU, states >= n are 0.
+// Gb[u] = half((alpha_u(s) - c[s]) * gscale); rows >= nU, states >= n are 0.
+// Single form (FP16): one value per state, row length nPad. Split form
+// (BF16): each value v is carried as hi = bf16(v) and lo = bf16(v - hi)
+// (v - hi is exact in FP32), so |v - hi - lo| <= 2^-16 |v|; the row holds,
+// for every 64-state block kb, the 64 hi values and then the 64 lo values
+// (row length 2 nPad), and the GEMM multiplies one A block by both.
 // Records gmax = max |(alpha - c) * gscale| over the FP32 values.
 __global__ void tc_pack_kernel(const float *__restrict__ G, unsigned n, size_t nPad, const unsigned *__restrict__ uniqJ,
-                               unsigned nU, const float *__restrict__ shift, int fp16, uint16_t *__restrict__ Gb,
-                               unsigned *__restrict__ scal) {
+                               unsigned nU, const float *__restrict__ shift, int fp16, int split,
+                               uint16_t *__restrict__ Gb, unsigned *__restrict__ scal) {
     const unsigned u = blockIdx.x;
     const float gscale = __uint_as_float(scal[6]);
-    uint16_t *out = Gb + (size_t)u * nPad;
+    const size_t rowLen = split ? 2 * nPad : nPad;
+    uint16_t *out = Gb + (size_t)u * rowLen;
     float m = 0.0f;
     int nanSeen = 0;
     if (u < nU) {
@@ -670,10 +715,18 @@ __global__ void tc_pack_kernel(const float *__restrict__ G, unsigned n, size_t n
                 m = fmaxf(m, fabsf(v));
                 nanSeen |= (v != v);
             }
-            out[s] = to_half_bits(v, fp16 != 0);
+            if (split) {
+                const uint16_t hi = to_half_bits(v, false);
+                const uint16_t lo = to_half_bits(v - from_half_bits(hi, false), false);
+                const size_t at = (size_t)(s / BK) * (2 * BK) + (s % BK);
+                out[at] = hi;
+                out[at + BK] = lo;
+            } else {
+                out[s] = to_half_bits(v, fp16 != 0);
+            }
         }
     } else {
-        for (unsigned s = threadIdx.x; s < nPad; s += blockDim.x) out[s] = 0;
+        for (size_t s = threadIdx.x; s < rowLen; s += blockDim.x) out[s] = 0;
     }
     __shared__ float red[32];
     __shared__ int snan;
@@ -689,13 +742,14 @@ __global__ void tc_pack_kernel(const float *__restrict__ G, unsigned n, size_t n
     }
 }
 
-// escale = U * gmax + gN * Gmax * gscale (all in the packed units); the
-// per-row bound is a1 * escale.
+// escale = U * gmax + gN * Gmax * gscale and dscale = gmax (1 + 2^-22), all
+// in the packed units; the per-row bound is a1 * escale + d1 * dscale.
 __global__ void tc_escale_kernel(unsigned *scal, float U, float gN) {
     const float gmax = __uint_as_float(scal[0]);
     const float Gmax = __uint_as_float(scal[1]);
     const float gscale = __uint_as_float(scal[6]);
     scal[2] = __float_as_uint(U * gmax + gN * Gmax * gscale);
+    scal[7] = __float_as_uint(gmax * (1.0f + 2.4e-7f));
 }
 
 // ---------------------------------------------------------------------------
@@ -731,6 +785,7 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
                                               const unsigned *__restrict__ suppLen, const ProjView pv,
                                               const unsigned *__restrict__ uniqJ, unsigned nLists,
                                               unsigned K, size_t rPad, const float *__restrict__ a1,
+                                              const float *__restrict__ d1,
                                               const float *__restrict__ a1raw, const unsigned *__restrict__ scal,
                                               const float *__restrict__ candV, const unsigned *__restrict__ candU,
                                               const float *__restrict__ candX, unsigned *__restrict__ ustar,
@@ -739,12 +794,12 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
     const unsigned ao = (unsigned)(row / md.r), i = (unsigned)(row % md.r);
     const unsigned a = ao / md.z, o = ao % md.z;
     const size_t base = row * MAX_ENTRIES;
-    const unsigned nEnt = nLists * K;     // <= 128: each lane holds entries lane + 32 j, j < 4
-    float v[4];
-    unsigned u[4];
+    const unsigned nEnt = nLists * K;     // <= MAX_ENTRIES: each lane holds entries lane + 32 j, j < kLaneEntries
+    float v[kLaneEntries];
+    unsigned u[kLaneEntries];
     float tmax = -INFINITY;
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
+    for (int j = 0; j < kLaneEntries; j++) {
         const unsigned e = lane + 32u * j;
         v[j] = -INFINITY;
         u[j] = kNoneU;
@@ -760,8 +815,7 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
         tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, off));
         x = fmaxf(x, __shfl_xor_sync(0xffffffffu, x, off));
     }
-    const float bound = a1[(size_t)ao * rPad + i];
-    const float thr = 2.0f * bound * __uint_as_float(scal[2]);
+    const float thr = row_margin(a1, d1, (size_t)ao * rPad + i, __uint_as_float(scal[2]), __uint_as_float(scal[7]));
     // Usable only with a finite margin, non-negative probabilities, and
     // scores far from the reference's -1e10 sentinel.
     const float Gmax = __uint_as_float(scal[1]);
@@ -772,10 +826,10 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
         if (lane == 0) rowFlag[row] = 1u;
         return 0u;
     }
-    bool c[4];
+    bool c[kLaneEntries];
     unsigned count = 0, first = kNoneU;
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
+    for (int j = 0; j < kLaneEntries; j++) {
         c[j] = u[j] != kNoneU && v[j] >= cut;
         const unsigned msk = __ballot_sync(0xffffffffu, c[j]);
         count += __popc(msk);
@@ -786,7 +840,7 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
         const unsigned src = first & 31u, jj = first >> 5;
         unsigned mine = u[0];
 #pragma unroll
-        for (int j = 1; j < 4; j++)
+        for (int j = 1; j < kLaneEntries; j++)
             if (jj == (unsigned)j) mine = u[j];
         const unsigned uu = __shfl_sync(0xffffffffu, mine, src);
         if (lane == 0) { ustar[js] = uu; jstar[js] = uniqJ[uu]; }
@@ -800,7 +854,7 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
     float best = -INFINITY;
     unsigned bu = kNoneU;
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
+    for (int j = 0; j < kLaneEntries; j++) {
         if (c[j]) {
             const float w = proj_row_score(P, pv, u[j], bk, sk, Li);
             if (bu == kNoneU || w > best || (w == best && u[j] < bu)) { best = w; bu = u[j]; }
@@ -826,12 +880,13 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
 // memory, then added to the global counters once per block.
 __global__ void __launch_bounds__(256) tc_merge_kernel(DevModel md, const unsigned *__restrict__ suppLen,
                                 const ProjView pv, const unsigned *__restrict__ uniqJ, unsigned nLists, unsigned K,
-                                size_t rPad, const float *__restrict__ a1, const float *__restrict__ a1raw,
-                                const unsigned *__restrict__ scal,
+                                size_t rPad, const float *__restrict__ a1, const float *__restrict__ d1,
+                                const float *__restrict__ a1raw, const unsigned *__restrict__ scal,
                                 const float *__restrict__ candV, const unsigned *__restrict__ candU,
                                 const float *__restrict__ candX, unsigned *__restrict__ ustar,
                                 unsigned *__restrict__ jstar, unsigned *__restrict__ rowFlag,
-                                unsigned *__restrict__ counters, const unsigned *__restrict__ badModel) {
+                                unsigned *__restrict__ rowCand, unsigned *__restrict__ counters,
+                                const unsigned *__restrict__ badModel) {
     __shared__ unsigned blockCount[2];
     if (threadIdx.x == 0) { blockCount[0] = 0u; blockCount[1] = 0u; }
     __syncthreads();
@@ -840,8 +895,9 @@ __global__ void __launch_bounds__(256) tc_merge_kernel(DevModel md, const unsign
     const size_t rows = (size_t)md.m * md.z * md.r;
     unsigned rescored = 0;
     if (row < rows)
-        rescored = merge_row(row, lane, md, suppLen, pv, uniqJ, nLists, K, rPad, a1, a1raw, scal, candV,
+        rescored = merge_row(row, lane, md, suppLen, pv, uniqJ, nLists, K, rPad, a1, d1, a1raw, scal, candV,
                              candU, candX, ustar, jstar, rowFlag, badModel);
+    if (lane == 0 && row < rows) rowCand[row] = rescored;
     if (lane == 0 && rescored) {
         atomicAdd(&blockCount[0], 1u);
         atomicAdd(&blockCount[1], rescored);
@@ -959,18 +1015,28 @@ static int encode_map(TcState *tc, CUtensorMap *map, const void *base, size_t ro
 // (Re)builds A in the element type of the engine's scoring mode.
 static int tc_build_operand(BackupEngine &eng, TcState *tc, const char *fn) {
     const DevModel &md = eng.md;
+    // A new operand form starts its schedule choice afresh (the margins,
+    // and with them the best list length, differ between forms).
+    if (tc->mode != eng.scoring) {
+        tc->schedFixed = -1;
+        tc->tuneNext = 0;
+        tc->tuneWarm = false;
+    }
     tc->mode = eng.scoring;
     const size_t aElems = (size_t)tc->MZ * tc->rPad * tc->nPad;
     cudaMemsetAsync(tc->A, 0, aElems * sizeof(uint16_t), eng.stream);
     cudaMemsetAsync(tc->a1, 0, (size_t)tc->MZ * tc->rPad * sizeof(float), eng.stream);
     cudaMemsetAsync(tc->a1raw, 0, (size_t)tc->MZ * tc->rPad * sizeof(float), eng.stream);
+    cudaMemsetAsync(tc->d1, 0, (size_t)tc->MZ * tc->rPad * sizeof(float), eng.stream);
     cudaMemsetAsync(tc->badModel, 0, sizeof(unsigned), eng.stream);
     // a1 bounds sum_s |A| with A in exact arithmetic: the FP32 sums of
     // non-negative terms are inflated by their worst-case rounding.
     const float slack = 1.0f + (float)(md.n + md.rz * md.ns + 8) * 1.2e-7f;
+    // d1 is an FP32 sum of nPad exact non-negative terms.
+    const float dslack = 1.0f + (float)(tc->nPad + 8) * 1.2e-7f;
     tc_build_a_kernel<<<md.r * md.m, 256, md.n * sizeof(float), eng.stream>>>(
         md, eng.succLen, eng.suppLen, tc->rPad, tc->nPad, tc->mode == NOVA_SCORING_FP16 ? 1 : 0, tc->A, tc->a1,
-        tc->a1raw, slack, tc->badModel);
+        tc->a1raw, tc->d1, slack, dslack, tc->badModel);
     int rc = check_launch(fn, "scoring operand build");
     if (rc != NOVA_SUCCESS) return rc;
     return encode_map(tc, &tc->tmA, tc->A, (size_t)tc->MZ * tc->rPad, tc->nPad, BM, fn);
@@ -989,7 +1055,7 @@ int tc_build(BackupEngine &eng, const char *fn) {
     size_t freeB = 0, totalB = 0;
     cudaMemGetInfo(&freeB, &totalB);
     const size_t slots = (size_t)tc->MZ * md.r * MAX_LISTS;
-    const size_t need = aElems * 2 + tc->capN * tc->nPad * 2 + slots * (MAX_TOPK * 8 + 4) + (size_t)tc->MZ * md.r * 4;
+    const size_t need = aElems * 2 + tc->capN * tc->nPad * 4 + slots * (MAX_TOPK * 8 + 4) + (size_t)tc->MZ * md.r * 12;
     if (need + (256ull << 20) > freeB) {
         NOVA_ERR(fn, "Not enough device memory for the tensor-core operands; using exact scoring.");
         return NOVA_ERROR_DEVICE_MALLOC;
@@ -1007,13 +1073,16 @@ int tc_build(BackupEngine &eng, const char *fn) {
     if ((rc = dev_alloc(&tc->A, aElems, fn, "the tensor-core scoring operand")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->a1, (size_t)tc->MZ * tc->rPad, fn, "the row bounds")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->a1raw, (size_t)tc->MZ * tc->rPad, fn, "the row bounds")) != NOVA_SUCCESS) return rc;
-    if ((rc = dev_alloc(&tc->Gb, tc->capN * tc->nPad, fn, "the packed alphas")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->d1, (size_t)tc->MZ * tc->rPad, fn, "the row bounds")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->Gb, tc->capN * tc->nPad * 2, fn, "the packed alphas")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->shift, md.n, fn, "the alpha shift")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->scal, 8, fn, "the scoring scalars")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->candV, slots * MAX_TOPK, fn, "the candidate scores")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->candU, slots * MAX_TOPK, fn, "the candidate alphas")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->candX, slots, fn, "the dropped-score bounds")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->rowFlag, (size_t)tc->MZ * md.r, fn, "the exact-scan flags")) != NOVA_SUCCESS) return rc;
+    if ((rc = dev_alloc(&tc->rowCand, (size_t)tc->MZ * md.r, fn, "the per-row re-score counts")) != NOVA_SUCCESS)
+        return rc;
     if ((rc = dev_alloc(&tc->rowList, (size_t)tc->MZ * md.r, fn, "the exact-scan rows")) != NOVA_SUCCESS) return rc;
     if ((rc = dev_alloc(&tc->chunkCount, ceil_div((size_t)tc->MZ * md.r, kCompactChunk), fn,
                         "the exact-scan chunk counts")) != NOVA_SUCCESS)
@@ -1026,6 +1095,8 @@ int tc_build(BackupEngine &eng, const char *fn) {
     cudaEventCreate(&tc->g0);
     cudaEventCreate(&tc->g1);
     if (cudaFuncSetAttribute(tc_score_gemm_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(tc_score_gemm_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM) !=
             cudaSuccess ||
         cudaFuncSetAttribute(tc_score_gemm_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM) !=
             cudaSuccess) {
@@ -1044,6 +1115,8 @@ int tc_score_launch(BackupEngine &eng, const float *src, unsigned nU, bool timed
     if (tc->mode != eng.scoring && (rc = tc_build_operand(eng, tc, fn)) != NOVA_SUCCESS) return rc;
     const DevModel &md = eng.md;
     const bool fp16 = tc->mode == NOVA_SCORING_FP16;
+    // BF16 carries the alphas as two BF16 terms (split); FP16 as one.
+    const unsigned kSplit = fp16 ? 1u : 2u;
     const size_t nPadRows = round_up(nU, BN);
     const unsigned nTiles = (unsigned)(nPadRows / BN);
     // ---- pack the shifted, scaled unique alphas ----
@@ -1053,30 +1126,39 @@ int tc_score_launch(BackupEngine &eng, const float *src, unsigned nU, bool timed
     tc_gscale_kernel<<<1, 1, 0, eng.stream>>>(tc->scal);
     if ((rc = check_launch(fn, "alpha scale")) != NOVA_SUCCESS) return rc;
     tc_pack_kernel<<<(unsigned)nPadRows, 256, 0, eng.stream>>>(src, md.n, tc->nPad, eng.uniqJ, nU, tc->shift,
-                                                              fp16 ? 1 : 0, tc->Gb, tc->scal);
+                                                              fp16 ? 1 : 0, kSplit == 2u ? 1 : 0, tc->Gb, tc->scal);
     if ((rc = check_launch(fn, "alpha packing")) != NOVA_SUCCESS) return rc;
-    // Error factors relative to sum_s |A| |alpha - c| (packed units): the
-    // rounding of both operands to BF16 (2^-9 each) or FP16 (2^-12 each,
-    // plus the absolute error of FP16 subnormals, below 2^-25 per entry),
-    // the FP32 build of A (epsA) and of alpha - c, and the accumulation:
-    // each tcgen05.mma step (K=16) adds at most 2^-22 of the running sum of
-    // magnitudes. The reference's own rounding over ns + rz + 3 operations
-    // is relative to a1 * Gmax.
+    // The row bound is a1 * escale + d1 * dscale (packed units), with
+    // escale = U * gmax + gN * Gmax * gscale and dscale = gmax (1 + 2^-22).
+    // Against the reference's FP32 score, the tensor-core score of a row
+    // (shifted by a row constant) differs by at most
+    //  * sum_s |A - Ahalf| |alpha - c|  <= d1 gmax: A's operand rounding,
+    //    measured per row when A was built;
+    //  * epsA a1 gmax: the FP32 build of A itself;
+    //  * (1 + uA)(uG + 2^-23) a1 gmax: the alphas' rounding to FP16 (uG =
+    //    2^-11, plus the absolute error of FP16 subnormals, below 2^-25 per
+    //    entry) or to the hi + lo BF16 pair (uG = 2^-16), and the FP32
+    //    rounding of alpha - c;
+    //  * the accumulation: each tcgen05.mma step (K=16) adds at most 2^-22 of
+    //    the running sum of magnitudes, over kSplit * nPad / 16 steps;
+    //  * gN a1 Gmax: the reference's own rounding over ns + rz + 3 operations.
+    // uA is A's unit roundoff (2^-11 FP16, 2^-8 BF16).
     const double u24 = 1.0 / 16777216.0;
     const double epsA = (double)(md.rz * md.ns + 4) * u24;
-    const double rnd = fp16 ? 1.0 / 2048.0 : 1.0 / 512.0;
-    const double accum = ((double)tc->nPad / 16.0 + 2.0) / 4194304.0;
-    const float U = (float)(((1.0 + epsA) * (1.0 + rnd) * (1.0 + rnd) * (1.0 + 2.0 * u24) - 1.0) +
-                            accum * (1.0 + 2.0 * rnd) + (fp16 ? (double)tc->nPad / 33554432.0 / 8192.0 : 0.0) +
-                            1.0 / 1048576.0);
+    const double uA = fp16 ? 1.0 / 2048.0 : 1.0 / 256.0;
+    const double uG = fp16 ? 1.0 / 2048.0 : 1.0 / 65536.0;
+    const double steps = (double)kSplit * (double)tc->nPad / 16.0 + 2.0;
+    const float U = (float)(epsA * (1.0 + 2.0 * u24) + (1.0 + uA) * (uG + 2.0 * u24) +
+                            steps / 4194304.0 * (1.0 + uA) * (1.0 + uG) * (1.0 + 2.0 * u24) +
+                            (fp16 ? (double)tc->nPad / 33554432.0 / 8192.0 : 0.0) + 1.0 / 1048576.0);
     const float gN = (float)((double)(md.ns + md.rz + 3) * u24 * 1.01);
     tc_escale_kernel<<<1, 1, 0, eng.stream>>>(tc->scal, U, gN);
     if ((rc = check_launch(fn, "margin")) != NOVA_SUCCESS) return rc;
     // ---- GEMM ----
     CUtensorMap tmB;
-    if ((rc = encode_map(tc, &tmB, tc->Gb, nPadRows, tc->nPad, BN, fn)) != NOVA_SUCCESS) return rc;
+    if ((rc = encode_map(tc, &tmB, tc->Gb, nPadRows, tc->nPad * kSplit, BN, fn)) != NOVA_SUCCESS) return rc;
     // Each alpha group leaves two lists per row (one per epilogue half).
-    if (tc->schedFixed < 0 && tc->nPad > kTuneMaxNPad) tc->schedFixed = 0;
+    if (tc->schedFixed < 0 && tc->nPad > kTuneMaxNPad) tc->schedFixed = fp16 ? kDeepScheduleFp16 : kDeepScheduleBf16;
     const TcSchedule sched = kSchedules[tc->schedFixed >= 0 ? tc->schedFixed : (tc->tuneWarm ? (int)tc->tuneNext : 0)];
     const unsigned groups = std::max(1u, std::min<unsigned>(sched.groups, nTiles));
     const unsigned lists = 2u * groups;
@@ -1084,19 +1166,21 @@ int tc_score_launch(BackupEngine &eng, const float *src, unsigned nU, bool timed
     const unsigned totalUnits = tc->MZ * tc->mTiles * groups;
     const unsigned grid = std::min<unsigned>(totalUnits, (unsigned)tc->numSMs);
     if (timed) cudaEventRecord(tc->g0, eng.stream);
-    auto gemm = sched.topk == 16u ? tc_score_gemm_kernel<16> : tc_score_gemm_kernel<8>;
+    auto gemm = sched.topk == 32u ? tc_score_gemm_kernel<32>
+                : (sched.topk == 16u ? tc_score_gemm_kernel<16> : tc_score_gemm_kernel<8>);
     gemm<<<grid, GEMM_THREADS, GEMM_SMEM, eng.stream>>>(
         tc->tmA, tmB, make_idesc(fp16 ? 0u : 1u), tc->MZ, (unsigned)tc->rPad, md.r, tc->mTiles, nTiles, groups, nU,
-        (unsigned)(tc->nPad / BK), tc->a1, tc->scal, tc->candV, tc->candU, tc->candX);
+        (unsigned)(tc->nPad / BK), kSplit, tc->a1, tc->d1, tc->scal, tc->candV, tc->candU, tc->candX);
     if ((rc = check_launch(fn, "tensor-core scoring")) != NOVA_SUCCESS) return rc;
     if (timed) cudaEventRecord(tc->g1, eng.stream);
     // ---- merge, margin, exact re-score of near ties ----
     const size_t rows = (size_t)tc->MZ * md.r;
     cudaMemsetAsync(tc->rowFlag, 0, rows * sizeof(unsigned), eng.stream);
     tc_merge_kernel<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, eng.stream>>>(
-        md, eng.suppLen, eng.proj_view(), eng.uniqJ, lists, sched.topk, tc->rPad, tc->a1, tc->a1raw, tc->scal, tc->candV,
+        md, eng.suppLen, eng.proj_view(), eng.uniqJ, lists, sched.topk, tc->rPad, tc->a1, tc->d1, tc->a1raw, tc->scal,
+        tc->candV,
         tc->candU,
-        tc->candX, eng.ustar, eng.jstar, tc->rowFlag, tc->scal + 3, tc->badModel);
+        tc->candX, eng.ustar, eng.jstar, tc->rowFlag, tc->rowCand, tc->scal + 3, tc->badModel);
     if ((rc = check_launch(fn, "candidate merge")) != NOVA_SUCCESS) return rc;
     // The list can hold every row: it is sized m*z*r like the flags.
     {
@@ -1148,6 +1232,27 @@ int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, 
     return NOVA_SUCCESS;
 }
 
+int tc_row_detail(const BackupEngine &eng, unsigned *candidates, unsigned *exactRows, const char *fn) {
+    const TcState *tc = eng.tc;
+    const DevModel &md = eng.md;
+    const size_t rows = (size_t)md.m * md.z * md.r;
+    std::vector<unsigned> cand(rows), flag(rows);
+    if (cudaStreamSynchronize(eng.stream) != cudaSuccess ||
+            cudaMemcpy(cand.data(), tc->rowCand, rows * sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(flag.data(), tc->rowFlag, rows * sizeof(unsigned), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        NOVA_ERR(fn, "Failed to read the per-row scoring detail.");
+        return NOVA_ERROR_MEMCPY_TO_HOST;
+    }
+    for (unsigned i = 0; i < md.r; i++) { candidates[i] = 0; exactRows[i] = 0; }
+    for (size_t row = 0; row < rows; row++) {   // row = (a*z + o) * r + i
+        const unsigned i = (unsigned)(row % md.r);
+        candidates[i] += cand[row];
+        exactRows[i] += flag[row] ? 1u : 0u;
+    }
+    return NOVA_SUCCESS;
+}
+
 void tc_tune_feedback(BackupEngine &eng, float msScoring, unsigned nU) {
     TcState *tc = eng.tc;
     if (tc == nullptr || tc->schedFixed >= 0 || nU == 0) return;
@@ -1156,9 +1261,9 @@ void tc_tune_feedback(BackupEngine &eng, float msScoring, unsigned nU) {
         return;
     }
     tc->tuneCost[tc->tuneNext] = msScoring / (float)nU;
-    if (++tc->tuneNext < 3) return;
+    if (++tc->tuneNext < (unsigned)kTunedSchedules) return;
     unsigned best = 0;
-    for (unsigned k = 1; k < 3; k++)
+    for (unsigned k = 1; k < (unsigned)kTunedSchedules; k++)
         if (tc->tuneCost[k] < tc->tuneCost[best]) best = k;
     tc->schedFixed = (int)best;
 }

@@ -14,9 +14,13 @@
 // every GPU that loads this library keeps it until the process exits. All
 // calls share it: two calls whose kernels overlap on the GPU (different
 // host threads, or different streams of the caller) race on it, so callers
-// must serialise them. The first call on a device resolves the array's
-// device address for that device (cudaGetSymbolAddress); make that first
-// call before any stream capture.
+// must serialise them. The first call on a device (and the first call after
+// the device's context was created anew, e.g. after cudaDeviceReset)
+// resolves the array's device address for that device
+// (cudaGetSymbolAddress); make that first call before any stream capture.
+// Kernels run on the calling thread's per-thread default stream (the library
+// is built with per-thread default streams): work that writes d_Gamma, d_pi
+// or d_b on other streams or host threads must be complete before the call.
 
 #include "common.h"
 
@@ -80,9 +84,30 @@ __global__ void noalloc_argmax_kernel(unsigned rows, const unsigned *__restrict_
     }
 }
 
-// Device address of the scratch for each device, resolved once per device.
+// Device address of the scratch, resolved once per device and context. A
+// context created anew on a device (after cudaDeviceReset, or when the
+// primary context was released and retained again) loads this module again
+// at a new address, so the cached address is kept together with the context
+// it belongs to and resolved again when the current context differs.
+typedef int (*CtxGetCurrentFn)(void **);
+
+static CtxGetCurrentFn ctx_get_current() {
+    static CtxGetCurrentFn f = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return reinterpret_cast<CtxGetCurrentFn>(p);
+    }();
+    return f;
+}
+
 static std::mutex g_scratch_mutex;
 static NoAllocScratch *g_scratch_addr[64] = {};
+static void *g_scratch_ctx[64] = {};
 
 static int scratch_for_current_device(NoAllocScratch **out, const char *fn) {
     int dev = -1;
@@ -91,15 +116,22 @@ static int scratch_for_current_device(NoAllocScratch **out, const char *fn) {
         NOVA_ERR(fn, "No usable current CUDA device.");
         return NOVA_ERROR_INVALID_CUDA_PARAM;
     }
+    // cudaGetSymbolAddress makes the device's primary context current when
+    // no context is, so the context is read after it on the first call.
+    void *ctx = nullptr;
+    CtxGetCurrentFn getCtx = ctx_get_current();
+    if (getCtx != nullptr && getCtx(&ctx) != 0) ctx = nullptr;
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (g_scratch_addr[dev] == nullptr) {
+    if (g_scratch_addr[dev] == nullptr || ctx == nullptr || ctx != g_scratch_ctx[dev]) {
         void *p = nullptr;
         if (cudaGetSymbolAddress(&p, g_value_scratch) != cudaSuccess || p == nullptr) {
             cudaGetLastError();
             NOVA_ERR(fn, "Failed to resolve the device address of the evaluation scratch.");
             return NOVA_ERROR_KERNEL_EXECUTION;
         }
+        if (getCtx != nullptr && getCtx(&ctx) != 0) ctx = nullptr;
         g_scratch_addr[dev] = static_cast<NoAllocScratch *>(p);
+        g_scratch_ctx[dev] = ctx;
     }
     *out = g_scratch_addr[dev];
     return NOVA_SUCCESS;

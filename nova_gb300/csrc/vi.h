@@ -50,9 +50,10 @@ __device__ __forceinline__ void residual_commit(double local, ViDeviceState *st,
 #endif
 
 // Tile plan of the column-tiled sweep: the model's successor entries
-// regrouped by (block of source states, tile of successor states, warp,
-// level), where level q holds the q-th successor of each row inside the
-// tile. Built once per solver from the device copies of S and T.
+// regrouped by chunk (block of source states, tile of successor states) and,
+// within a chunk, by level, where level q holds the q-th successor of each
+// row inside the tile. Built once per solver from the device copies of S
+// and T.
 struct ViTilePlan {
     enum Status : unsigned { kNotBuilt = 0, kTiled = 1, kGather = 2 };
     Status status = kNotBuilt;
@@ -63,10 +64,9 @@ struct ViTilePlan {
     unsigned levels = 0;        // longest run of one row's successors inside one tile
     unsigned grid = 0;          // resident CTAs
     size_t smemBytes = 0;
-    uint2 *rec = nullptr;          // [entries] {row << 16 | offset in tile, bits of fl(gamma * T)}
-    unsigned *levelStart = nullptr;  // build scratch: first record of each (slice, level) sub-bin
-    unsigned *sliceStart = nullptr;  // [blocks*tiles*warps + 1] first record of each (block, tile, warp) slice
-    unsigned *counts = nullptr;    // build scratch
+    uint2 *rec = nullptr;          // [entries + 2] {row << 16 | offset in tile, bits of fl(gamma * T)}
+    unsigned *chunkStart = nullptr;  // [blocks*tiles + 1] first record of each (block, tile) chunk
+    unsigned *levelCnt = nullptr;    // [blocks*tiles][levels] runs of each chunk with more than q records
     unsigned *flags = nullptr;     // build scratch: unsorted rows, out-of-range successor, longest run
     ~ViTilePlan();
 };

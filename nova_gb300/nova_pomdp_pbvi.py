@@ -72,6 +72,7 @@ _nova.nova_gb300_kernel_launches.restype = ct.c_ulonglong
 _nova.pomdp_pbvi_set_scoring_gpu.argtypes = (_G, ct.c_uint)
 _nova.pomdp_pbvi_set_graph_gpu.argtypes = (_G, ct.c_uint)
 _nova.pomdp_pbvi_get_stats_gpu.argtypes = (_G, ct.POINTER(NovaPBVIStats))
+_nova.pomdp_pbvi_row_detail_gpu.argtypes = (_G, ct.POINTER(ct.c_uint), ct.POINTER(ct.c_uint))
 _nova.pomdp_pbvi_value_gpu.argtypes = (_P, _G, ct.POINTER(ct.c_float), ct.POINTER(ct.c_double),
                                        ct.POINTER(ct.c_uint))
 _nova.pomdp_pbvi_update_record_gpu.argtypes = (_P, _G, ct.c_void_p, ct.c_void_p)
@@ -80,6 +81,8 @@ _nova.pomdp_pbvi_execute_recorded_gpu.argtypes = (_P, _G, ct.c_uint, ct.c_uint, 
 _nova.pomdp_pbvi_adjoint_gpu.argtypes = (_P, ct.c_uint, ct.c_uint, ct.c_void_p, ct.c_void_p, ct.c_void_p,
                                          ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,
                                          ct.POINTER(ct.c_double), ct.POINTER(ct.c_uint))
+_nova.pomdp_pbvi_value_replay_f64_gpu.argtypes = (_P, ct.c_uint, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                                  ct.c_uint, ct.POINTER(ct.c_double), ct.POINTER(ct.c_uint))
 from . import nova_pomdp_alpha_vectors as _npav  # noqa: E402
 _nova.pomdp_pbvi_execute_batched_gpu.argtypes = (ct.POINTER(_P), ct.POINTER(_G),
                                                  ct.POINTER(ct.POINTER(_npav.NovaPOMDPAlphaVectors)), ct.c_uint,

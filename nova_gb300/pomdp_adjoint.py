@@ -136,3 +136,47 @@ def pbvi_record_and_adjoint(model, b0, horizon, checkpoint_every=10):
            acts.cpu().numpy().astype(np.uint32), sels.cpu().numpy().astype(np.uint32))
     pomdp.uninitialize_gpu()
     return out
+
+
+def pbvi_value_vs_fp64(model, b0, horizon, scoring=None, pomdp=None):
+    """V(b0) after `horizon` backups from GammaInitial, and the same value
+    recomputed in FP64 with the run's selections held fixed
+    (pomdp_pbvi_value_replay_f64_gpu). Returns (V, V_fp64, istar, acts,
+    sels): V is the FP64 reduction of the FP32 alphas at their maximising
+    row istar, V_fp64 that row of the FP64 replay, so |V - V_fp64| is the
+    arithmetic error of the FP32 backups; acts [H][r] and sels [H][r][z] are
+    the recorded selections (numpy)."""
+    n, z, r = model["n"], model["z"], model["r"]
+    H = int(horizon)
+    own = pomdp is None
+    if own:
+        pomdp = POMDP.from_arrays(model)
+        pomdp.initialize_gpu()
+    alg = POMDPPBVIGPU(pomdp, GammaInitial=model["GammaInitial"])
+    if scoring is not None:
+        alg.set_scoring(scoring)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    ck = torch.empty((1, r, n), dtype=torch.float32, device=dev)
+    acts = torch.empty((H, r), dtype=torch.int32, device=dev)
+    sels = torch.empty((H, r, z), dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    _check(npp._nova.pomdp_pbvi_execute_recorded_gpu(alg.pomdpPtr, alg, H, H, ck.data_ptr(), acts.data_ptr(),
+                                                     sels.data_ptr()), "pomdp_pbvi_execute_recorded_gpu")
+    V, _ = alg.value(b0)
+    # the maximising row of the FP32 alphas (FP64 reduction, lowest index on ties)
+    pol = alg.get_policy()
+    vals = pol.gamma_array().astype(np.float64) @ np.asarray(b0, np.float64)
+    del pol
+    del alg
+    istar = int(np.argmax(vals))
+    b = torch.as_tensor(np.asarray(b0, np.float32), device=dev)
+    V64 = ct.c_double(0.0)
+    used = ct.c_uint(0)
+    _check(npp._nova.pomdp_pbvi_value_replay_f64_gpu(ct.byref(pomdp), H, ck.data_ptr(), acts.data_ptr(),
+                                                     sels.data_ptr(), b.data_ptr(), istar, ct.byref(V64),
+                                                     ct.byref(used)), "pomdp_pbvi_value_replay_f64_gpu")
+    torch.cuda.synchronize()
+    out = (V, V64.value, istar, acts.cpu().numpy().astype(np.uint32), sels.cpu().numpy().astype(np.uint32))
+    if own:
+        pomdp.uninitialize_gpu()
+    return out

@@ -128,6 +128,18 @@ class POMDPPBVIGPU(npp.NovaPOMDPPBVIGPU):
             raise RuntimeError("pomdp_pbvi_get_stats_gpu failed with code %d" % result)
         return {name: getattr(s, name) for name, _ in s._fields_}
 
+    def row_detail(self):
+        """ Per-belief (candidates re-scored exactly, rows scanned exactly) of the last
+            tensor-core update (pomdp_pbvi_row_detail_gpu), as two uint32 arrays of r. """
+        r = self.pomdp.r
+        cand = np.zeros(r, np.uint32)
+        exact = np.zeros(r, np.uint32)
+        result = npp._nova.pomdp_pbvi_row_detail_gpu(self, cand.ctypes.data_as(ct.POINTER(ct.c_uint)),
+                                                     exact.ctypes.data_as(ct.POINTER(ct.c_uint)))
+        if result != 0:
+            raise RuntimeError("pomdp_pbvi_row_detail_gpu failed with code %d" % result)
+        return cand, exact
+
     def value(self, b):
         """ FP64 V(b) and action over the current device alpha set (pomdp_pbvi_value_gpu). """
         b = np.ascontiguousarray(np.asarray(b, dtype=np.float32).ravel())

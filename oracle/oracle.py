@@ -23,6 +23,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libnova_ref.so")
+# The one setting for where the reference project lies: NOVA_REFERENCE_DIR,
+# else the place it is mounted read-only in the build container. Where neither
+# holds its sources (the GPU host), everything that needs them is skipped.
 REF_DIR = os.environ.get("NOVA_REFERENCE_DIR", "/root/reference")
 
 _F = ct.POINTER(ct.c_float)
@@ -183,6 +186,99 @@ def pbvi_belief_action_sampler(model, Gamma):
         return L.oracle_pbvi_belief_action(n, ns, m, z, G.shape[0], rz, model["gamma"], *ptrs, i, a,
                                            _p(out, _F))
     return run
+
+
+def pbvi_backup_beliefs(model, Gamma, beliefs, threads=None):
+    """nova's loop-form backup (pomdp_pbvi_cpu.cpp:106-162) of the listed
+    beliefs only, against the full alpha set Gamma: returns (rows [k, n],
+    pi [k], kept [k]) where rows[t] / pi[t] are what the update writes for
+    belief beliefs[t] and kept[t] says no action beat the -1e10 sentinel (the
+    update then leaves that belief's row and action untouched; rows[t] is
+    undefined). The (belief, action) pairs run on `threads` host threads
+    (default: all), as each ctypes call releases the GIL."""
+    import threading
+    L = lib()
+    S, T, O, R, Z, B = _arrays(model)
+    n, ns, m, z, r, rz = _dims(model)
+    G = np.ascontiguousarray(Gamma, dtype=np.float32)
+    beliefs = [int(i) for i in beliefs]
+    k = len(beliefs)
+    alphas = np.empty((k, m, n), np.float32)
+    values = np.empty((k, m), np.float32)
+    ptrs = (_p(S, _I), _p(T, _F), _p(O, _F), _p(R, _F), _p(Z, _I), _p(B, _F), _p(G, _F))
+    jobs = [(t, a) for t in range(k) for a in range(m)]
+    lock = threading.Lock()
+    nxt = [0]
+
+    def worker():
+        while True:
+            with lock:
+                if nxt[0] >= len(jobs):
+                    return
+                t, a = jobs[nxt[0]]
+                nxt[0] += 1
+            out = alphas[t, a]
+            values[t, a] = L.oracle_pbvi_belief_action(n, ns, m, z, G.shape[0], rz, model["gamma"], *ptrs,
+                                                       beliefs[t], a, _p(out, _F))
+    if threads is None:
+        try:
+            threads = len(os.sched_getaffinity(0))
+        except Exception:
+            threads = os.cpu_count() or 1
+    ts = [threading.Thread(target=worker) for _ in range(max(1, min(threads, len(jobs))))]
+    for th in ts:
+        th.start()
+    for th in ts:
+        th.join()
+    rows = np.zeros((k, n), np.float32)
+    pi = np.zeros(k, np.uint32)
+    kept = np.ones(k, bool)
+    for t in range(k):
+        best = np.float32(-1e10)
+        for a in range(m):   # strict '>' from nova's -1e10 start: the lowest action wins ties
+            if values[t, a] > best:
+                best = values[t, a]
+                rows[t] = alphas[t, a]
+                pi[t] = a
+                kept[t] = False
+    return rows, pi, kept
+
+
+def choose_parity_beliefs(candidates, exactRows, k=16, seed=0):
+    """k beliefs for a sampled parity check of one tensor-core update: up to
+    k/4 with rows sent to the exact scan (most such rows first), then those
+    with the most alphas re-scored in the merge up to 3k/4, then random ones."""
+    candidates = np.asarray(candidates).astype(np.int64)
+    exactRows = np.asarray(exactRows).astype(np.int64)
+    r = len(candidates)
+    chosen = [int(i) for i in np.argsort(-exactRows, kind="stable")[:k // 4] if exactRows[i] > 0]
+    for i in np.argsort(-candidates, kind="stable"):
+        if len(chosen) >= (3 * k) // 4:
+            break
+        if int(i) not in chosen:
+            chosen.append(int(i))
+    rng = np.random.default_rng(seed)
+    while len(chosen) < min(k, r):
+        i = int(rng.integers(0, r))
+        if i not in chosen:
+            chosen.append(i)
+    return chosen
+
+
+def sampled_backup_parity(model, Gamma, GammaPrime, pi, beliefs, threads=None):
+    """Bits of GammaPrime rows and pi for the listed beliefs against nova's
+    loop-form backup of Gamma (pbvi_backup_beliefs). Returns the list of
+    beliefs whose row or action differ (beliefs that no action improves must
+    keep their row, which the caller checks)."""
+    rows, p, kept = pbvi_backup_beliefs(model, Gamma, beliefs, threads)
+    bad = []
+    for t, i in enumerate(beliefs):
+        if kept[t]:
+            continue
+        if not (np.array_equal(rows[t].view(np.uint32), np.ascontiguousarray(GammaPrime[i], np.float32)
+                               .view(np.uint32)) and int(p[t]) == int(pi[i])):
+            bad.append(int(i))
+    return bad
 
 
 def alpha_value(Gamma, pi, b):

@@ -8,6 +8,7 @@ import tempfile
 import pytest
 
 from conftest import ROOT
+from oracle import oracle as orc
 from nova_gb300 import build, _lib
 from nova_gb300 import nova_pomdp, nova_pomdp_pbvi, nova_pomdp_perseus, nova_pomdp_alpha_vectors
 from nova_gb300 import nova_mdp, nova_mdp_vi, nova_mdp_value_function
@@ -66,10 +67,10 @@ def test_headers_match_ctypes_mirror_c_and_cxx():
     assert ours_c == ours_cxx == _mirror_layout()
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/include"), reason="reference headers not present")
+@pytest.mark.skipif(not os.path.isdir(os.path.join(orc.REF_DIR, "include")), reason="reference headers not present")
 def test_headers_match_reference_headers():
     ours = _layout_program(os.path.join(ROOT, "include"), cxx=True)
-    ref = _layout_program("/root/reference/include", cxx=True)
+    ref = _layout_program(os.path.join(orc.REF_DIR, "include"), cxx=True)
     assert ours == ref
 
 

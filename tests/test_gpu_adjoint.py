@@ -116,3 +116,18 @@ def test_adjoint_full_size_gradient_workload():
         assert rel_err(a, b) < 1e-5
     coords = random_coords(model, 6, np.random.default_rng(1))
     assert fd_check(model, acts, sels, b0, {"R": dR, "T": dT, "O": dO}, coords, istar) < 1e-3
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(n=70, m=4, z=5, ns=9, r=90, rz=11, horizon=15)])
+def test_fp64_replay_value_matches_oracle(kw):
+    """pomdp_pbvi_value_replay_f64_gpu against the oracle's FP64 forward of the
+    same recorded selections (pomdp_pbvi_cpu.cpp:37-162 with its argmax
+    results fixed), at the FP32 run's maximising row."""
+    from nova_gb300.pomdp_adjoint import pbvi_value_vs_fp64
+    model = small_model(seed=9, **kw)
+    b0 = synth.dense_belief(model, 0)
+    H = model["horizon"]
+    V, V64, istar, acts, sels = pbvi_value_vs_fp64(model, b0, H)
+    Vo, _ = orc.pbvi_fixed_forward_f64(model, model["GammaInitial"], acts, sels, b0, istar=istar)
+    assert abs(V64 - Vo) <= 1e-12 * max(1.0, abs(Vo))
+    assert abs(V - V64) <= 1e-4

@@ -205,8 +205,8 @@ def test_tensor_core_scoring_is_exact_and_runs(mode):
     engaged = [s for s in stats if s["scoring"] == mode]
     assert len(engaged) >= 3, stats
     rows = m["r"] * m["m"] * m["z"]
-    # BF16's proven margin is about 16x wider than FP16's, so it leaves more
-    # rows to the exact scan (still a minority here).
+    # BF16's proven margin (A rounded to 8 significant bits) is several
+    # times wider than FP16's, so it may leave more rows to the exact scan.
     limit = 0.25 if mode == npp.SCORING_BF16 else 0.01
     for s in engaged:
         assert s["msGemm"] > 0
@@ -215,8 +215,9 @@ def test_tensor_core_scoring_is_exact_and_runs(mode):
 
 @pytest.mark.parametrize("mode", [npp.SCORING_BF16, npp.SCORING_FP16])
 def test_tensor_core_scoring_many_unresolved_rows(mode):
-    """n=512, r=1024: BF16 leaves a large share of rows to the exact scan;
-    every step must still equal exact scoring bit for bit."""
+    """n=512, r=1024, many near-tied alphas per row: every step must equal
+    exact scoring bit for bit, whatever share of rows the margin leaves to
+    the exact scan."""
     m = synth.random_pomdp(n=512, m=8, z=16, ns=16, r=1024, rz=32, gamma=0.95, horizon=5, seed=5)
     exact, _ = _run_mode(m, npp.SCORING_EXACT, m["horizon"])
     tc, stats = _run_mode(m, mode, m["horizon"])

@@ -194,14 +194,14 @@ def test_raw_loader_rejects_bad_files(tmp_path):
         POMDP().load(str(tmp_path / "missing.raw"), filetype="raw")
 
 
-@pytest.mark.skipif(not os.path.isfile("/root/reference/tests/tiger/tiger_pomdp.raw"),
+@pytest.mark.skipif(not os.path.isfile(os.path.join(orc.REF_DIR, "tests", "tiger", "tiger_pomdp.raw")),
                     reason="reference fixtures not present")
 def test_raw_loader_on_reference_tiger_file():
     import sys
     from nova_gb300.pomdp import POMDP
-    sys.path.insert(0, "/root/reference/python/nova")
+    sys.path.insert(0, os.path.join(orc.REF_DIR, "python", "nova"))
     import file_loader
-    path = "/root/reference/tests/tiger/tiger_pomdp.raw"
+    path = os.path.join(orc.REF_DIR, "tests", "tiger", "tiger_pomdp.raw")
     fl = file_loader.FileLoader()
     fl.load_raw_pomdp(path)
     p = POMDP()
@@ -258,7 +258,7 @@ def test_cassandra_loader_rejects_missing_file(tmp_path):
         POMDP().load(str(tmp_path / "missing.pomdp"), filetype="xml")
 
 
-_REF_DOMAINS = "/root/reference/tests/benchmarks/algorithms/domains"
+_REF_DOMAINS = os.path.join(orc.REF_DIR, "tests", "benchmarks", "algorithms", "domains")
 
 
 @pytest.mark.skipif(not os.path.isdir(_REF_DOMAINS), reason="reference domain files not present")
@@ -270,7 +270,8 @@ def test_cassandra_loader_on_reference_domains(name):
     import importlib.util
     if not hasattr(np, "float"):
         np.float = float
-    spec = importlib.util.spec_from_file_location("ref_file_loader", "/root/reference/python/nova/file_loader.py")
+    spec = importlib.util.spec_from_file_location("ref_file_loader",
+                                                  os.path.join(orc.REF_DIR, "python", "nova", "file_loader.py"))
     fl = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(fl)
     path = os.path.join(_REF_DOMAINS, name + ".pomdp")
