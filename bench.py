@@ -200,8 +200,9 @@ def gemm_traffic(units, split):
         return None, "no ncu capture recorded for this operand form"
 
 
-def sampled_parity(alg, model, k, seed):
-    """One more (untimed) update on `alg`, then its rows and actions for k
+def sampled_parity(alg, model, k, seed, backup0):
+    """One more (untimed) update on `alg` (whose alpha set is that after
+    backup0 backups from GammaInitial plus alg's own updates), then its rows and actions for k
     sampled beliefs (those with rows sent to the exact scan, those with the
     most alphas re-scored, random ones) against nova's loop-form backup (the
     oracle, as the checker) over all actions and the full alpha set."""
@@ -219,7 +220,7 @@ def sampled_parity(alg, model, k, seed):
     t0 = time.perf_counter()
     bad = orc.sampled_backup_parity(model, G, Gp, pi, beliefs, threads=host_cores())
     return {"matched": "%d of %d" % (len(beliefs) - len(bad), len(beliefs)), "beliefs": beliefs,
-            "mismatched": bad, "horizon": st["horizon"], "scoring": st["scoring"],
+            "mismatched": bad, "backup": backup0 + st["horizon"], "scoring": st["scoring"],
             "rows_exact_scan": st["rowsOverflow"], "candidates_rescored": st["candidates"],
             "max_candidates_one_belief": int(cand.max()), "oracle_seconds": time.perf_counter() - t0}
 
@@ -851,7 +852,8 @@ def main():
         alg.update()  # builds the operands and tables; not timed
         torch.cuda.synchronize()
         if rank == 0 and args.parity_beliefs > 0:
-            parity["fp16"] = sampled_parity(alg, model, args.parity_beliefs, seed=1)
+            parity["fp16"] = sampled_parity(alg, model, args.parity_beliefs, seed=1,
+                                            backup0=args.warmup + args.steps)
 
     # ---- BF16 tensor-core scoring on the same state ----------------------------
     bf16 = None
@@ -882,7 +884,8 @@ def main():
                 "step_breakdown_ms": {k: fl[k] for k in ("msDedup", "msProject", "msScore", "msGemm", "msRescore",
                                                          "msActions", "msAssemble", "msTotal")}}
         if rank == 0 and args.parity_beliefs > 0:
-            parity["bf16"] = sampled_parity(alg, model, args.parity_beliefs, seed=2)
+            parity["bf16"] = sampled_parity(alg, model, args.parity_beliefs, seed=2,
+                                            backup0=args.warmup + args.steps)
         alg.set_scoring(npp.SCORING_FP16)
 
     # ---- plain FP32 form on the same state -----------------------------------

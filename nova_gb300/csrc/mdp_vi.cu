@@ -350,6 +350,7 @@ static int vi_gpu_sweep(const MDP *mdp, MDPVIGPU *vi, double tol, int early_exit
     if (rc != NOVA_SUCCESS) return rc;
     if (sync) {
         rc = sync_device(fn);
+        if (rc == NOVA_SUCCESS) rc = vi_state_error(st, fn);
         if (rc != NOVA_SUCCESS) return rc;
     }
     vi->currentHorizon++;
@@ -421,6 +422,11 @@ extern "C" int mdp_vi_execute_gpu(const MDP *mdp, MDPVIGPU *vi, MDPValueFunction
         }
     }
     rc = sync_device(fn);
+    if (rc == NOVA_SUCCESS) {
+        std::lock_guard<std::mutex> lock(registry_mutex());
+        auto *ws = find_workspace<ViGpuWorkspace>(vi);
+        if (ws != nullptr) rc = vi_state_error(ws->st, fn);
+    }
     if (rc == NOVA_SUCCESS) rc = mdp_vi_get_policy_gpu(mdp, vi, policy);
     if (rc != NOVA_SUCCESS) {
         mdp_vi_uninitialize_gpu(mdp, vi);
@@ -492,6 +498,7 @@ extern "C" int mdp_vi_execute_until_converged_gpu(const MDP *mdp, MDPVIGPU *vi, 
             launched++;
         }
         rc = d2h(&h, st, sizeof(h), fn, "the convergence state");
+        if (rc == NOVA_SUCCESS) rc = vi_state_error(st, fn);
         if (rc != NOVA_SUCCESS) { mdp_vi_uninitialize_gpu(mdp, vi); return rc; }
         if (h.converged) break;
     }
@@ -599,6 +606,7 @@ extern "C" int mdp_vi_update_cpu(const MDP *mdp, MDPVICPU *vi) {
     rc = launch_sweep(mdp, ws->S, ws->T, ws->R, ws->V, ws->VPrime, ws->pi, ws->st, 0.0, 0, 0, &ws->plan, fn);
     if (rc != NOVA_SUCCESS) return rc;
     rc = d2h(hdst, ws->VPrime, n * sizeof(float), fn, "the value function (prime)");
+    if (rc == NOVA_SUCCESS) rc = vi_state_error(ws->st, fn);
     if (rc != NOVA_SUCCESS) return rc;
     rc = d2h(vi->pi, ws->pi, n * sizeof(unsigned), fn, "the policy (pi)");
     if (rc != NOVA_SUCCESS) return rc;
@@ -647,6 +655,7 @@ extern "C" int mdp_vi_execute_cpu(const MDP *mdp, MDPVICPU *vi, MDPValueFunction
         if (rc == NOVA_SUCCESS) vi->currentHorizon++;
     }
     if (rc == NOVA_SUCCESS) rc = sync_device(fn);
+    if (rc == NOVA_SUCCESS) rc = vi_state_error(ws->st, fn);
     if (rc == NOVA_SUCCESS) rc = d2h(vi->V, ws->V, n * sizeof(float), fn, "the value function");
     if (rc == NOVA_SUCCESS) rc = d2h(vi->VPrime, ws->VPrime, n * sizeof(float), fn, "the value function (prime)");
     if (rc == NOVA_SUCCESS) rc = d2h(vi->pi, ws->pi, n * sizeof(unsigned), fn, "the policy (pi)");

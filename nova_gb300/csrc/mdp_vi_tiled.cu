@@ -7,31 +7,30 @@
 //
 //   * Source states are cut into blocks of Sb states (one CTA at a time per
 //     block; its m*Sb partial sums Q(s,a) live in shared memory, seeded with
-//     R(s,a)). Successor states are cut into tiles of Vt states; the CTA
-//     stages V one tile at a time (cp.async, double-buffered) and adds the
-//     products of the successors that fall in that tile.
+//     R(s,a)). Successor states are cut into tiles of Vt states. One warp of
+//     the CTA stages V tile after tile into a ring of shared-memory buffers
+//     with bulk copies (cp.async.bulk, completion on an mbarrier); the other
+//     31 warps each own a fixed range of the block's rows and add, tile
+//     after tile, the products of their rows' successors that fall in the
+//     tile. A warp releases a buffer (mbarrier arrive) when it is done with
+//     it, so warps run independently of each other, up to the ring's depth.
 //   * A row's successors inside one tile form a run (consecutive in the
-//     row's list). The plan, built once per solver, stores for every chunk
-//     (block, tile) the 8-byte records {row << 16 | offset in tile,
-//     fl(gamma * T)} (the reference's first rounding, done once) of all its
+//     row's list). The plan, built once per solver, stores for every slice
+//     (block, tile, warp) the 8-byte records {row << 16 | offset in tile,
+//     fl(gamma * T)} (the reference's first rounding, done once) of its
 //     runs, level after level: level q holds the q-th record of every run
 //     with more than q records, runs ordered by length (longest first), so
-//     run j has its level-q record at position j of level q. Thread k of the
-//     CTA applies runs k, k + 1024, ... of the chunk, each run's records in
-//     list order into its row's partial sum; the rows of one chunk's runs are
-//     distinct, so no two threads touch one partial sum, and the chunks of a
-//     block run in tile order with one CTA barrier between tiles. Records
-//     stream from HBM exactly once per sweep (the same 8 bytes per entry as S
-//     and T): each thread loads its next chunk's records into registers while
-//     it applies the current chunk's, and the chunk after that is prefetched
-//     into L2 with one bulk prefetch.
-//   * Within a chunk the single-record runs are ordered so that a warp's 32
-//     runs fall in distinct shared-memory banks: runs are bucketed by the
-//     bank of their partial sum (row mod 32), sorted inside each bucket by
-//     the distance (tile offset - row) mod 32, and dealt out round-robin over
-//     the buckets. A full round is 32 distinct partial-sum banks, and since
-//     the k-th runs of the buckets have about the same distance, their V
-//     offsets fall in distinct banks too.
+//     run j has its level-q record at position j of level q. Lane l of the
+//     warp applies runs l, l + 32, ... of the slice, each run's records in
+//     list order; the runs of a slice have distinct rows, and a warp's
+//     slices run in tile order, so every row receives its products in list
+//     order. Records stream from HBM exactly once per sweep (the same 8
+//     bytes per entry as S and T): each warp loads its next slice's records
+//     while it applies the current one, and the staging warp prefetches the
+//     records of the tile after that into L2 with one bulk prefetch.
+//   * The single-record runs of a slice are dealt round-robin over the 32
+//     shared-memory banks of their partial sums (row mod 32), so a warp's 32
+//     runs of one step update distinct banks.
 //
 // Order of operations: the reference computes Q = R(s,a), then for each
 // successor in list order Q += (gamma * T) * V[s'] (mdp_vi_cpu.cpp:45-52).
@@ -39,6 +38,11 @@
 // order is list order, so this sweep performs the same roundings in the same
 // order and its results are bit-identical. The plan builder checks that;
 // models with unsorted rows keep the per-row sweep.
+//
+// Every mbarrier wait is bounded (about 2 s); a wait that runs out raises
+// the CTA's abort flag and the state's error word, the warps stop, the
+// staging warp waits (bounded) for its copies in flight, and the host
+// reports NOVA_ERROR_KERNEL_EXECUTION.
 
 #include "vi.h"
 
@@ -54,37 +58,67 @@ namespace nova_gb300 {
 namespace {
 
 constexpr unsigned kThreads = 1024;
-constexpr int kRunsPerThread = 5;           // level-0 records held in registers per thread and chunk
-constexpr unsigned kMaxRows = 65535u;       // rows of one block (16-bit row field)
-constexpr unsigned kMaxLevels = 31u;        // longest run of one row inside one tile
-constexpr unsigned kDefaultTileStates = 10240u;
+constexpr unsigned kWarps = kThreads / 32;
+constexpr unsigned kRowWarps = kWarps - 1;        // warps that apply records; the last one stages V
+constexpr int kSteps = 4;                         // groups of 32 records a warp holds per slice in registers
+constexpr unsigned kStages = 3;                   // V tiles in flight
+constexpr unsigned kMaxRows = 65535u;             // rows of one block (16-bit row field)
+constexpr unsigned kMaxLevels = 31u;              // longest run of one row inside one tile
+constexpr unsigned kDefaultTileStates = 8192u;
 constexpr unsigned long long kAutoMinEntries = 1ull << 22;
+constexpr long long kWaitCycles = 4000000000ll;   // ~2 s at 2 GHz
+constexpr size_t kBarrierBytes = 64;              // full[kStages], empty[kStages], abort flag
 
 std::atomic<unsigned> g_mode{NOVA_VI_TILING_AUTO};
 std::atomic<unsigned> g_tile_states{0};
 std::atomic<unsigned> g_last_status{0};
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// Stage V[t*Vt, min(n, (t+1)*Vt)) into dst: 16-byte cp.async for the
-// aligned body, plain loads for the tail of the last tile.
-__device__ __forceinline__ void stage_tile(float *dst, const float *__restrict__ V, unsigned n, unsigned t,
-                                           unsigned Vt) {
-    const unsigned base = t * Vt;
-    const unsigned cnt = min(Vt, n - base);
-    const unsigned c4 = cnt >> 2;
-    for (unsigned i = threadIdx.x; i < c4; i += blockDim.x) cp_async16(dst + 4 * i, V + base + 4 * i);
-    for (unsigned i = (c4 << 2) + threadIdx.x; i < cnt; i += blockDim.x) dst[i] = V[base + i];
-    cp_async_commit();
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
 }
-
-// Bulk prefetch of a record range into L2 (16-byte aligned; the record
-// array has two spare records at its end).
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: false (after raising the abort flag and the error word) if
+// the phase does not complete in ~2 s, or if the CTA already aborted.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abortFlag,
+                                          ViDeviceState *st) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (true) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (*abortFlag) return false;
+        if (clock64() - t0 > kWaitCycles) {
+            *abortFlag = 1;
+            atomicExch(&st->err, 1u);
+            return false;
+        }
+    }
+}
+// Bulk copy global -> shared (16-byte aligned, size a multiple of 16)
+// completing on an mbarrier.
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
+}
+// Bulk prefetch of a record range into L2 (the record array has two spare
+// records at its end for the rounding up to 16 bytes).
 __device__ __forceinline__ void prefetch_l2(const uint2 *rec, unsigned b, unsigned e) {
     if (e <= b) return;
     const uintptr_t lo = reinterpret_cast<uintptr_t>(rec + b) & ~(uintptr_t)15;
@@ -92,51 +126,59 @@ __device__ __forceinline__ void prefetch_l2(const uint2 *rec, unsigned b, unsign
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((unsigned)(hi - lo)) : "memory");
 }
 
-// The records a thread needs for one chunk: level-0 records of its runs
-// tid + kThreads * i (i < kRunsPerThread), and the level-1 record of run tid.
-struct ChunkRegs {
-    uint2 r0[kRunsPerThread];
-    uint2 r1;
+constexpr uint2 kNoRecord = {0xFFFFFFFFu, 0u};
+
+// First record and run counts of one slice: n0 runs, n1 of them longer than
+// one record.
+struct SliceHdr {
     unsigned start, n0, n1;
 };
-
-__device__ __forceinline__ void load_chunk(ChunkRegs &c, const uint2 *__restrict__ rec,
-                                           const unsigned *__restrict__ chunkStart,
-                                           const unsigned *__restrict__ levelCnt, unsigned L, size_t chunk,
-                                           unsigned tid) {
-    c.start = __ldg(chunkStart + chunk);
-    c.n0 = __ldg(levelCnt + chunk * L);
-    c.n1 = L > 1 ? __ldg(levelCnt + chunk * L + 1) : 0u;
+__device__ __forceinline__ SliceHdr load_hdr(const unsigned *__restrict__ sliceStart,
+                                             const unsigned *__restrict__ levelCnt, unsigned L, size_t slice) {
+    SliceHdr h;
+    h.start = __ldg(sliceStart + slice);
+    h.n0 = __ldg(levelCnt + slice * L);
+    h.n1 = L > 1 ? __ldg(levelCnt + slice * L + 1) : 0u;
+    return h;
+}
+// The records a lane holds for one slice: the level-0 records of its runs
+// lane + 32 i (i < kSteps) and the level-1 record of run `lane`.
+struct SliceRegs {
+    uint2 r0[kSteps];
+    uint2 r1;
+};
+__device__ __forceinline__ void load_regs(SliceRegs &g, const uint2 *__restrict__ rec, const SliceHdr &h,
+                                          unsigned lane) {
 #pragma unroll
-    for (int i = 0; i < kRunsPerThread; i++) {
-        const unsigned j = tid + kThreads * i;
-        c.r0[i] = j < c.n0 ? __ldg(rec + c.start + j) : make_uint2(0xFFFFFFFFu, 0u);
+    for (int i = 0; i < kSteps; i++) {
+        const unsigned j = lane + 32u * i;
+        g.r0[i] = j < h.n0 ? __ldg(rec + h.start + j) : kNoRecord;
     }
-    c.r1 = tid < c.n1 ? __ldg(rec + c.start + c.n0 + tid) : make_uint2(0xFFFFFFFFu, 0u);
+    g.r1 = lane < h.n1 ? __ldg(rec + h.start + h.n0 + lane) : kNoRecord;
 }
 
-// One record into the running partial sum q: q + fl(gamma*T) * V[s'].
+// q + fl(gamma*T) * V[s'] for one record.
 __device__ __forceinline__ float apply_record(float q, uint2 r, const float *vtile, unsigned tileLen) {
     const unsigned off = r.x & 0xFFFFu;
     return off < tileLen ? fadd(q, fmul(__uint_as_float(r.y), vtile[off])) : q;
 }
 
-// Run j of a chunk: its level-0 record r0, then (j < n1) the further
-// levels in list order; first1 is the level-1 record when already loaded.
-__device__ __forceinline__ void apply_run(uint2 r0, bool have1, uint2 first1, unsigned j, const ChunkRegs &c,
+// Run j of a slice: its level-0 record r0, then (j < n1) the further levels
+// in list order; r1 is the level-1 record when already loaded.
+__device__ __forceinline__ void apply_run(uint2 r0, bool have1, uint2 r1, unsigned j, const SliceHdr &h,
                                           const uint2 *__restrict__ rec, const unsigned *__restrict__ levelCnt,
-                                          unsigned L, size_t chunk, const float *vtile, unsigned tileLen,
+                                          unsigned L, size_t slice, const float *vtile, unsigned tileLen,
                                           float *part, unsigned rows) {
     const unsigned row = r0.x >> 16;
     if (row >= rows) return;
     float q = apply_record(part[row], r0, vtile, tileLen);
-    if (j < c.n1) {
-        q = apply_record(q, have1 ? first1 : __ldg(rec + c.start + c.n0 + j), vtile, tileLen);
-        unsigned base = c.n0 + c.n1;
+    if (j < h.n1) {
+        q = apply_record(q, have1 ? r1 : __ldg(rec + h.start + h.n0 + j), vtile, tileLen);
+        unsigned base = h.n0 + h.n1;
         for (unsigned lv = 2; lv < L; lv++) {
-            const unsigned nq = __ldg(levelCnt + chunk * L + lv);
+            const unsigned nq = __ldg(levelCnt + slice * L + lv);
             if (j >= nq) break;
-            q = apply_record(q, __ldg(rec + c.start + base + j), vtile, tileLen);
+            q = apply_record(q, __ldg(rec + h.start + base + j), vtile, tileLen);
             base += nq;
         }
     }
@@ -145,55 +187,103 @@ __device__ __forceinline__ void apply_run(uint2 r0, bool have1, uint2 first1, un
 
 __global__ void __launch_bounds__(kThreads, 1) bellman_tiled_kernel(
         unsigned n, unsigned m, unsigned Vt, unsigned T, unsigned Sb, unsigned blocks, unsigned L,
-        const uint2 *__restrict__ rec, const unsigned *__restrict__ chunkStart,
+        const uint2 *__restrict__ rec, const unsigned *__restrict__ sliceStart,
         const unsigned *__restrict__ levelCnt, const float *__restrict__ R, const float *__restrict__ V,
         float *__restrict__ Vp, unsigned *__restrict__ pi, ViDeviceState *st, double tol, int early_exit) {
     if (early_exit && *(volatile unsigned *)&st->converged) return;  // uniform across the grid
-    extern __shared__ __align__(16) unsigned char smem[];
-    float *vt = reinterpret_cast<float *>(smem);            // [2][Vt]
-    float *part = vt + 2 * (size_t)Vt;                      // [Sb*m]
-    const unsigned tid = threadIdx.x;
+    extern __shared__ __align__(128) unsigned char smem[];
+    float *vt = reinterpret_cast<float *>(smem);                              // [kStages][Vt]
+    float *part = vt + (size_t)kStages * Vt;                                  // [Sb*m]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + (((size_t)kStages * Vt + (size_t)Sb * m) * 4 + 15) /
+                                                             16 * 16);
+    volatile int *abortFlag = reinterpret_cast<volatile int *>(bars + 2 * kStages);
+    const unsigned tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        for (unsigned s = 0; s < kStages; s++) {
+            mbar_init(smem_addr(&bars[s]), 1);                 // full: the staging lane's arrival + bytes
+            mbar_init(smem_addr(&bars[kStages + s]), kRowWarps);  // empty: one arrival per row warp
+        }
+        *abortFlag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    unsigned stage = 0, phase = 0;   // ring position, advanced identically by every warp
+    unsigned lastPar[kStages];       // staging lane: parity of the last copy issued per stage (2: none)
+#pragma unroll
+    for (unsigned s = 0; s < kStages; s++) lastPar[s] = 2u;
     double local = 0.0;
-    for (unsigned blk = blockIdx.x; blk < blocks; blk += gridDim.x) {
+    for (unsigned blk = blockIdx.x; blk < blocks && !*abortFlag; blk += gridDim.x) {
         const unsigned s0 = blk * Sb;
         const unsigned nsb = min(Sb, n - s0);
         const unsigned rows = nsb * m;
         for (unsigned i = tid; i < rows; i += blockDim.x) part[i] = __ldg(R + (size_t)s0 * m + i);
-        const size_t c0 = (size_t)blk * T;
-        stage_tile(vt, V, n, 0, Vt);
-        if (tid == 0) {
-            prefetch_l2(rec, __ldg(chunkStart + c0), __ldg(chunkStart + c0 + min(T, 2u)));
-        }
-        ChunkRegs cur, nxt;
-        load_chunk(cur, rec, chunkStart, levelCnt, L, c0, tid);
-        cp_async_wait_all();
         __syncthreads();
-        for (unsigned t = 0; t < T; t++) {
-            const float *vcur = vt + (size_t)(t & 1) * Vt;
-            const size_t chunk = c0 + t;
-            if (t + 1 < T) {
-                // The other buffer held tile t-1; every thread passed the
-                // barrier that ended tile t-1, so it is free.
-                stage_tile(vt + (size_t)((t + 1) & 1) * Vt, V, n, t + 1, Vt);
-                if (tid == 0 && t + 2 < T)
-                    prefetch_l2(rec, __ldg(chunkStart + chunk + 2), __ldg(chunkStart + chunk + 3));
-                load_chunk(nxt, rec, chunkStart, levelCnt, L, chunk + 1, tid);
+        const size_t c0 = (size_t)blk * T;
+        if (warp == kRowWarps) {
+            // ---- staging warp: V tiles into the ring, records into L2 ----
+            if (lane == 0) {
+                prefetch_l2(rec, __ldg(sliceStart + c0 * kRowWarps), __ldg(sliceStart + (c0 + min(T, 2u)) * kRowWarps));
+                unsigned sg = stage, ph = phase;
+                for (unsigned t = 0; t < T; t++) {
+                    if (!mbar_wait(smem_addr(&bars[kStages + sg]), ph ^ 1u, abortFlag, st)) break;
+                    const unsigned base = t * Vt, cnt = min(Vt, n - base);
+                    const unsigned body = cnt & ~3u;
+                    float *dst = vt + (size_t)sg * Vt;
+                    for (unsigned k = body; k < cnt; k++) dst[k] = __ldg(V + base + k);  // tail of the last tile
+                    const uint32_t fb = smem_addr(&bars[sg]);
+                    mbar_expect_tx(fb, body * 4u);
+                    if (body) bulk_copy(smem_addr(dst), V + base, body * 4u, fb);
+                    lastPar[sg] = ph;
+                    if (t + 2 < T)
+                        prefetch_l2(rec, __ldg(sliceStart + (c0 + t + 2) * kRowWarps),
+                                    __ldg(sliceStart + (c0 + t + 3) * kRowWarps));
+                    if (++sg == kStages) { sg = 0; ph ^= 1u; }
+                }
             }
-            const unsigned tileLen = min(Vt, n - t * Vt);
+        } else {
+            // ---- row warps ----
+            const size_t sl0 = c0 * kRowWarps + warp;   // slice of (blk, t) is sl0 + t * kRowWarps
+            SliceHdr hA = load_hdr(sliceStart, levelCnt, L, sl0);
+            SliceHdr hB = T > 1 ? load_hdr(sliceStart, levelCnt, L, sl0 + kRowWarps) : SliceHdr{0, 0, 0};
+            SliceRegs cur, nxt;
+            load_regs(cur, rec, hA, lane);
+            unsigned sg = stage, ph = phase;
+            for (unsigned t = 0; t < T; t++) {
+                const size_t slice = sl0 + (size_t)t * kRowWarps;
+                SliceHdr hC{0, 0, 0};
+                if (t + 1 < T) {
+                    load_regs(nxt, rec, hB, lane);
+                    if (t + 2 < T) hC = load_hdr(sliceStart, levelCnt, L, slice + 2 * kRowWarps);
+                }
+                if (!mbar_wait(smem_addr(&bars[sg]), ph, abortFlag, st)) break;
+                const float *vcur = vt + (size_t)sg * Vt;
+                const unsigned tileLen = min(Vt, n - t * Vt);
 #pragma unroll
-            for (int i = 0; i < kRunsPerThread; i++) {
-                const unsigned j = tid + kThreads * i;
-                if (j < cur.n0)
-                    apply_run(cur.r0[i], i == 0, cur.r1, j, cur, rec, levelCnt, L, chunk, vcur, tileLen, part,
-                              rows);
+                for (int i = 0; i < kSteps; i++) {
+                    const unsigned j = lane + 32u * i;
+                    if (j < hA.n0)
+                        apply_run(cur.r0[i], i == 0, cur.r1, j, hA, rec, levelCnt, L, slice, vcur, tileLen, part,
+                                  rows);
+                }
+                for (unsigned j = lane + 32u * kSteps; j < hA.n0; j += 32u)
+                    apply_run(__ldg(rec + hA.start + j), false, kNoRecord, j, hA, rec, levelCnt, L, slice, vcur,
+                              tileLen, part, rows);
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_addr(&bars[kStages + sg]));
+                if (++sg == kStages) { sg = 0; ph ^= 1u; }
+                cur = nxt;
+                hA = hB;
+                hB = hC;
             }
-            for (unsigned j = tid + kThreads * kRunsPerThread; j < cur.n0; j += kThreads)
-                apply_run(__ldg(rec + cur.start + j), false, cur.r1, j, cur, rec, levelCnt, L, chunk, vcur, tileLen,
-                          part, rows);
-            cp_async_wait_all();
-            __syncthreads();
-            cur = nxt;
         }
+        // Every warp advances the ring by the block's T tiles.
+        {
+            const unsigned adv = stage + T;
+            phase ^= (adv / kStages) & 1u;
+            stage = adv % kStages;
+        }
+        __syncthreads();
+        if (*abortFlag) break;
         // Action scan of mdp_vi_cpu.cpp:55-58 (lowest action on ties).
         for (unsigned i = tid; i < nsb; i += blockDim.x) {
             const float *qv = part + (size_t)i * m;
@@ -208,6 +298,17 @@ __global__ void __launch_bounds__(kThreads, 1) bellman_tiled_kernel(
         }
         __syncthreads();
     }
+    if (*abortFlag && warp == kRowWarps && lane == 0) {
+        // Let the copies in flight land before the CTA exits (bounded): the
+        // last issue on each stage completes the phase of parity lastPar.
+        for (unsigned s = 0; s < kStages; s++) {
+            if (lastPar[s] > 1u) continue;
+            const long long t0 = clock64();
+            while (!mbar_try_wait(smem_addr(&bars[s]), lastPar[s]) && clock64() - t0 < kWaitCycles) {
+            }
+        }
+    }
+    __syncthreads();
     residual_commit(local, st, gridDim.x, tol, early_exit != 0);
 }
 
@@ -242,8 +343,12 @@ __global__ void vi_plan_scan_rows_kernel(unsigned n, unsigned m, unsigned ns, co
 }
 
 struct PlanGeometry {
-    unsigned n, m, ns, Vt, T, Sb, L;
+    unsigned n, m, ns, Vt, T, Sb, L, rowsPerWarp;
     float gamma;
+    // Slice (block, tile, row warp) of a row of the block.
+    __device__ __forceinline__ size_t slice(unsigned blk, unsigned t, unsigned rowLocal) const {
+        return ((size_t)blk * T + t) * kRowWarps + rowLocal / rowsPerWarp;
+    }
 };
 
 // Calls f(tile, first list index, run length) for every run of the row.
@@ -261,67 +366,50 @@ __device__ __forceinline__ void for_each_run(const int *Sr, unsigned ns, unsigne
     }
 }
 
-__device__ __forceinline__ unsigned run_cell(unsigned rowLocal, unsigned off) {
-    const unsigned qb = rowLocal & 31u, vb = off & 31u;
-    return qb * 32u + ((vb - qb) & 31u);
-}
-
-// Per chunk c = block * T + tile: levelCnt[c*L + q] = runs with more than q
-// records; cell[c*1024 + qb*32 + d] = single-record runs whose partial sum
-// is in bank qb at distance d; longCnt[c*(L+1) + len] = runs of len >= 2.
+// Per slice: levelCnt[sl*L + q] = runs with more than q records;
+// bucket[sl*32 + b] = single-record runs whose partial sum lies in shared-
+// memory bank b (row mod 32); longCnt[sl*(L+1) + len] = runs of len >= 2.
 __global__ void vi_plan_count_kernel(PlanGeometry g, const int *__restrict__ S, unsigned *__restrict__ levelCnt,
-                                     unsigned *__restrict__ cell, unsigned *__restrict__ longCnt) {
+                                     unsigned *__restrict__ bucket, unsigned *__restrict__ longCnt) {
     const unsigned long long row = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= (unsigned long long)g.n * g.m) return;
     const unsigned blk = (unsigned)(row / g.m) / g.Sb;
     const unsigned rowLocal = (unsigned)(row - (unsigned long long)blk * g.Sb * g.m);
     const int *Sr = S + row * g.ns;
-    for_each_run(Sr, g.ns, g.Vt, [&](unsigned t, unsigned l0, unsigned len) {
-        const size_t c = (size_t)blk * g.T + t;
-        for (unsigned q = 0; q < len; q++) atomicAdd(levelCnt + c * g.L + q, 1u);
-        if (len == 1) atomicAdd(cell + c * 1024 + run_cell(rowLocal, (unsigned)Sr[l0] - t * g.Vt), 1u);
-        else atomicAdd(longCnt + c * (g.L + 1) + len, 1u);
+    for_each_run(Sr, g.ns, g.Vt, [&](unsigned t, unsigned, unsigned len) {
+        const size_t sl = g.slice(blk, t, rowLocal);
+        for (unsigned q = 0; q < len; q++) atomicAdd(levelCnt + sl * g.L + q, 1u);
+        if (len == 1) atomicAdd(bucket + sl * 32 + (rowLocal & 31u), 1u);
+        else atomicAdd(longCnt + sl * (g.L + 1) + len, 1u);
     });
 }
 
-// Per chunk: its record count; each partial-sum bank's bucket size (bsize)
-// and, in place, the bucket's exclusive prefix over distances (cell); the
-// long runs' exclusive prefix by length, longest first (longCnt).
-__global__ void vi_plan_chunk_kernel(unsigned nChunks, unsigned L, const unsigned *__restrict__ levelCnt,
-                                     unsigned *__restrict__ cell, unsigned *__restrict__ bsize,
-                                     unsigned *__restrict__ longCnt, unsigned *__restrict__ chunkSize) {
-    const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nChunks) return;
+// Per slice: its record count, and the long runs' exclusive prefix by
+// length, longest first (in place in longCnt).
+__global__ void vi_plan_slice_kernel(size_t nSlices, unsigned L, const unsigned *__restrict__ levelCnt,
+                                     unsigned *__restrict__ longCnt, unsigned *__restrict__ sliceSize) {
+    const size_t sl = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (sl >= nSlices) return;
     unsigned total = 0;
-    for (unsigned q = 0; q < L; q++) total += levelCnt[c * L + q];
-    chunkSize[c] = total;
-    for (unsigned qb = 0; qb < 32; qb++) {
-        unsigned *b = cell + c * 1024 + qb * 32;
-        unsigned run = 0;
-        for (unsigned d = 0; d < 32; d++) {
-            const unsigned v = b[d];
-            b[d] = run;
-            run += v;
-        }
-        bsize[c * 32 + qb] = run;
-    }
+    for (unsigned q = 0; q < L; q++) total += levelCnt[sl * L + q];
+    sliceSize[sl] = total;
     unsigned run = 0;
     for (unsigned len = L; len >= 2; len--) {
-        unsigned *p = longCnt + c * (L + 1) + len;
+        unsigned *p = longCnt + sl * (L + 1) + len;
         const unsigned v = *p;
         *p = run;
         run += v;
     }
 }
 
-// Write every record at its place. The position j of a run in its chunk's
+// Write every record at its place. The position j of a run in its slice's
 // levels: long runs first, by length (ties in the order threads arrive,
-// which changes nothing: the rows of one chunk are distinct), then the
-// single-record runs dealt round-robin over the 32 partial-sum banks, the
-// k-th run of a bank's bucket (sorted by distance) in round k.
+// which changes nothing: the rows of one slice are distinct), then the
+// single-record runs dealt round-robin over the 32 banks, the k-th run of
+// bank b's bucket in round k.
 __global__ void vi_plan_fill_kernel(PlanGeometry g, const int *__restrict__ S, const float *__restrict__ Tm,
-                                    const unsigned *__restrict__ chunkStart, const unsigned *__restrict__ levelCnt,
-                                    unsigned *__restrict__ cell, const unsigned *__restrict__ bsize,
+                                    const unsigned *__restrict__ sliceStart, const unsigned *__restrict__ levelCnt,
+                                    const unsigned *__restrict__ bucket, unsigned *__restrict__ ticket,
                                     unsigned *__restrict__ longCnt, uint2 *__restrict__ rec) {
     const unsigned long long row = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (row >= (unsigned long long)g.n * g.m) return;
@@ -330,26 +418,25 @@ __global__ void vi_plan_fill_kernel(PlanGeometry g, const int *__restrict__ S, c
     const int *Sr = S + row * g.ns;
     const float *Tr = Tm + row * g.ns;
     for_each_run(Sr, g.ns, g.Vt, [&](unsigned t, unsigned l0, unsigned len) {
-        const size_t c = (size_t)blk * g.T + t;
+        const size_t sl = g.slice(blk, t, rowLocal);
         unsigned j;
         if (len >= 2) {
-            j = atomicAdd(longCnt + c * (g.L + 1) + len, 1u);
+            j = atomicAdd(longCnt + sl * (g.L + 1) + len, 1u);
         } else {
-            const unsigned ce = run_cell(rowLocal, (unsigned)Sr[l0] - t * g.Vt);
-            const unsigned qb = ce >> 5;
-            const unsigned rank = atomicAdd(cell + c * 1024 + ce, 1u);
-            j = g.L > 1 ? levelCnt[c * g.L + 1] : 0u;   // the long runs come first
-            const unsigned *bs = bsize + c * 32;
+            const unsigned qb = rowLocal & 31u;
+            const unsigned rank = atomicAdd(ticket + sl * 32 + qb, 1u);
+            j = g.L > 1 ? levelCnt[sl * g.L + 1] : 0u;   // the long runs come first
+            const unsigned *bs = bucket + sl * 32;
             for (unsigned b = 0; b < 32; b++) {
                 const unsigned sz = bs[b];
                 j += min(sz, rank) + ((b < qb && sz > rank) ? 1u : 0u);
             }
         }
-        unsigned base = chunkStart[c];
+        unsigned base = sliceStart[sl];
         for (unsigned q = 0; q < len; q++) {
             const unsigned sp = (unsigned)Sr[l0 + q];
             rec[base + j] = make_uint2((rowLocal << 16) | (sp - t * g.Vt), __float_as_uint(fmul(g.gamma, Tr[l0 + q])));
-            base += levelCnt[c * g.L + q];
+            base += levelCnt[sl * g.L + q];
         }
     });
 }
@@ -445,11 +532,11 @@ bool try_alloc(T **p, size_t count) {
 
 void release(ViTilePlan *plan) {
     cudaFree(plan->rec);
-    cudaFree(plan->chunkStart);
+    cudaFree(plan->sliceStart);
     cudaFree(plan->levelCnt);
     cudaFree(plan->flags);
     plan->rec = nullptr;
-    plan->chunkStart = plan->levelCnt = plan->flags = nullptr;
+    plan->sliceStart = plan->levelCnt = plan->flags = nullptr;
 }
 
 int scan_counts(const unsigned *counts, unsigned long long N, unsigned *out, cudaStream_t stream, const char *fn) {
@@ -502,7 +589,7 @@ int vi_plan_build(ViTilePlan *plan, const MDP *mdp, const int *S, const float *T
     unsigned Vt = setting ? setting : kDefaultTileStates;
     Vt = std::min<unsigned>(Vt, (unsigned)round_up(n, 4));
     const unsigned tiles = ceil_div(n, Vt);
-    const size_t fixed = 2 * (size_t)Vt * 4;
+    const size_t fixed = (size_t)kStages * Vt * 4 + 16 + kBarrierBytes;
     const size_t reserve = 1024;  // static shared memory of the residual reduction, with room to spare
     if ((size_t)optin < fixed + reserve + (size_t)m * 4) return NOVA_SUCCESS;
     const unsigned rowsMax = (unsigned)std::min<size_t>(((size_t)optin - fixed - reserve) / 4, kMaxRows);
@@ -511,7 +598,7 @@ int vi_plan_build(ViTilePlan *plan, const MDP *mdp, const int *S, const float *T
     const unsigned waves = ceil_div(n, (unsigned long long)sms * SbMax);
     const unsigned Sb = ceil_div(n, (unsigned long long)sms * waves);
     const unsigned blocks = ceil_div(n, Sb);
-    const size_t smemBytes = fixed + round_up((size_t)Sb * m * 4, 16);
+    const size_t smemBytes = round_up((size_t)kStages * Vt * 4 + (size_t)Sb * m * 4, 16) + kBarrierBytes;
 
     if (cudaFuncSetAttribute(bellman_tiled_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes) !=
             cudaSuccess) {
@@ -548,43 +635,45 @@ int vi_plan_build(ViTilePlan *plan, const MDP *mdp, const int *S, const float *T
         release(plan);
         return NOVA_SUCCESS;
     }
-    const PlanGeometry g{n, m, ns, Vt, tiles, Sb, L, mdp->gamma};
-    const unsigned long long nChunks = (unsigned long long)blocks * tiles;
-    if (nChunks * 1024ull >= (1ull << 32) || nChunks * (L + 1) >= (1ull << 32)) { release(plan); return NOVA_SUCCESS; }
+    const unsigned rowsPerWarp = ceil_div((unsigned long long)Sb * m, kRowWarps);
+    const PlanGeometry g{n, m, ns, Vt, tiles, Sb, L, rowsPerWarp, mdp->gamma};
+    const unsigned long long nSlices = (unsigned long long)blocks * tiles * kRowWarps;
+    if (nSlices * 32ull >= (1ull << 32) || nSlices * (L + 1) >= (1ull << 32)) { release(plan); return NOVA_SUCCESS; }
 
-    // Pass 2: per-chunk counts (levels, bank cells, long runs).
-    unsigned *cell = nullptr, *bsize = nullptr, *longCnt = nullptr, *chunkSize = nullptr;
+    // Pass 2: per-slice counts (levels, banks, long runs) and the slice starts.
+    unsigned *bucket = nullptr, *ticket = nullptr, *longCnt = nullptr, *sliceSize = nullptr;
     auto freeScratch = [&]() {
-        cudaFree(cell); cudaFree(bsize); cudaFree(longCnt); cudaFree(chunkSize);
-        cell = bsize = longCnt = chunkSize = nullptr;
+        cudaFree(bucket); cudaFree(ticket); cudaFree(longCnt); cudaFree(sliceSize);
+        bucket = ticket = longCnt = sliceSize = nullptr;
     };
-    if (!try_alloc(&plan->levelCnt, nChunks * L) || !try_alloc(&cell, nChunks * 1024) ||
-            !try_alloc(&bsize, nChunks * 32) || !try_alloc(&longCnt, nChunks * (L + 1)) ||
-            !try_alloc(&chunkSize, nChunks) || !try_alloc(&plan->chunkStart, nChunks + 1)) {
+    if (!try_alloc(&plan->levelCnt, nSlices * L) || !try_alloc(&bucket, nSlices * 32) ||
+            !try_alloc(&ticket, nSlices * 32) || !try_alloc(&longCnt, nSlices * (L + 1)) ||
+            !try_alloc(&sliceSize, nSlices) || !try_alloc(&plan->sliceStart, nSlices + 1)) {
         freeScratch();
         release(plan);
         return NOVA_SUCCESS;
     }
-    if (cudaMemsetAsync(plan->levelCnt, 0, nChunks * L * sizeof(unsigned), stream) != cudaSuccess ||
-            cudaMemsetAsync(cell, 0, nChunks * 1024 * sizeof(unsigned), stream) != cudaSuccess ||
-            cudaMemsetAsync(longCnt, 0, nChunks * (L + 1) * sizeof(unsigned), stream) != cudaSuccess) {
+    if (cudaMemsetAsync(plan->levelCnt, 0, nSlices * L * sizeof(unsigned), stream) != cudaSuccess ||
+            cudaMemsetAsync(bucket, 0, nSlices * 32 * sizeof(unsigned), stream) != cudaSuccess ||
+            cudaMemsetAsync(ticket, 0, nSlices * 32 * sizeof(unsigned), stream) != cudaSuccess ||
+            cudaMemsetAsync(longCnt, 0, nSlices * (L + 1) * sizeof(unsigned), stream) != cudaSuccess) {
         cudaGetLastError();
         freeScratch();
         release(plan);
         NOVA_ERR(fn, "Failed to clear the sweep plan counters.");
         return NOVA_ERROR_KERNEL_EXECUTION;
     }
-    vi_plan_count_kernel<<<rowBlocks, 256, 0, stream>>>(g, S, plan->levelCnt, cell, longCnt);
+    vi_plan_count_kernel<<<rowBlocks, 256, 0, stream>>>(g, S, plan->levelCnt, bucket, longCnt);
     rc = check_launch(fn, "sweep plan (count)");
     if (rc == NOVA_SUCCESS) {
-        vi_plan_chunk_kernel<<<ceil_div(nChunks, 128), 128, 0, stream>>>((unsigned)nChunks, L, plan->levelCnt, cell,
-                                                                         bsize, longCnt, chunkSize);
-        rc = check_launch(fn, "sweep plan (chunks)");
+        vi_plan_slice_kernel<<<ceil_div(nSlices, 256), 256, 0, stream>>>((size_t)nSlices, L, plan->levelCnt, longCnt,
+                                                                         sliceSize);
+        rc = check_launch(fn, "sweep plan (slices)");
     }
-    if (rc == NOVA_SUCCESS) rc = scan_counts(chunkSize, nChunks, plan->chunkStart, stream, fn);
+    if (rc == NOVA_SUCCESS) rc = scan_counts(sliceSize, nSlices, plan->sliceStart, stream, fn);
     unsigned total = 0;
     if (rc == NOVA_SUCCESS)
-        rc = d2h(&total, plan->chunkStart + nChunks, sizeof(unsigned), fn, "the sweep plan size");
+        rc = d2h(&total, plan->sliceStart + nSlices, sizeof(unsigned), fn, "the sweep plan size");
     // Pass 3: the records (two spare ones at the end for the bulk prefetch).
     if (rc == NOVA_SUCCESS && !try_alloc(&plan->rec, (size_t)total + 2)) rc = NOVA_ERROR_DEVICE_MALLOC;
     if (rc == NOVA_SUCCESS &&
@@ -593,7 +682,7 @@ int vi_plan_build(ViTilePlan *plan, const MDP *mdp, const int *S, const float *T
         rc = NOVA_ERROR_KERNEL_EXECUTION;
     }
     if (rc == NOVA_SUCCESS) {
-        vi_plan_fill_kernel<<<rowBlocks, 256, 0, stream>>>(g, S, T, plan->chunkStart, plan->levelCnt, cell, bsize,
+        vi_plan_fill_kernel<<<rowBlocks, 256, 0, stream>>>(g, S, T, plan->sliceStart, plan->levelCnt, bucket, ticket,
                                                            longCnt, plan->rec);
         rc = check_launch(fn, "sweep plan (fill)");
     }
@@ -621,11 +710,22 @@ int vi_tiled_sweep(const ViTilePlan *plan, const MDP *mdp, const float *R, const
                    ViDeviceState *st, double tol, int early_exit, cudaStream_t stream, const char *fn) {
     bellman_tiled_kernel<<<plan->grid, kThreads, plan->smemBytes, stream>>>(
         mdp->n, mdp->m, plan->tileStates, plan->tiles, plan->blockStates, plan->blocks, plan->levels, plan->rec,
-        plan->chunkStart, plan->levelCnt, R, V, Vp, pi, st, tol, early_exit);
+        plan->sliceStart, plan->levelCnt, R, V, Vp, pi, st, tol, early_exit);
     return check_launch(fn, "Bellman update (tiled)");
 }
 
 unsigned vi_last_plan_status() { return g_last_status.load(); }
+
+int vi_state_error(ViDeviceState *st, const char *fn) {
+    unsigned err = 0;
+    int rc = d2h(&err, &st->err, sizeof(unsigned), fn, "the sweep error word");
+    if (rc != NOVA_SUCCESS) return rc;
+    if (err == 0) return NOVA_SUCCESS;
+    const unsigned zero = 0;
+    h2d(&st->err, &zero, sizeof(unsigned), fn, "the sweep error word");
+    NOVA_ERR(fn, "A device-side wait of the Bellman sweep timed out; results are invalid.");
+    return NOVA_ERROR_KERNEL_EXECUTION;
+}
 
 }  // namespace nova_gb300
 

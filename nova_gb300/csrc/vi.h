@@ -15,7 +15,7 @@ struct ViDeviceState {
     unsigned int blocks_done;        // blocks finished in the current sweep
     unsigned int sweeps_done;        // sweeps that ran (early-exit mode)
     unsigned int converged;          // 1 once a sweep's residual fell below tol
-    unsigned int pad;
+    unsigned int err;                // 1 if a bounded wait of the tiled sweep ran out
     double last_resid;               // residual of the last finished sweep
 };
 
@@ -50,10 +50,10 @@ __device__ __forceinline__ void residual_commit(double local, ViDeviceState *st,
 #endif
 
 // Tile plan of the column-tiled sweep: the model's successor entries
-// regrouped by chunk (block of source states, tile of successor states) and,
-// within a chunk, by level, where level q holds the q-th successor of each
-// row inside the tile. Built once per solver from the device copies of S
-// and T.
+// regrouped by slice (block of source states, tile of successor states, row
+// warp) and, within a slice, by level, where level q holds the q-th
+// successor of each row inside the tile. Built once per solver from the
+// device copies of S and T.
 struct ViTilePlan {
     enum Status : unsigned { kNotBuilt = 0, kTiled = 1, kGather = 2 };
     Status status = kNotBuilt;
@@ -65,8 +65,8 @@ struct ViTilePlan {
     unsigned grid = 0;          // resident CTAs
     size_t smemBytes = 0;
     uint2 *rec = nullptr;          // [entries + 2] {row << 16 | offset in tile, bits of fl(gamma * T)}
-    unsigned *chunkStart = nullptr;  // [blocks*tiles + 1] first record of each (block, tile) chunk
-    unsigned *levelCnt = nullptr;    // [blocks*tiles][levels] runs of each chunk with more than q records
+    unsigned *sliceStart = nullptr;  // [blocks*tiles*rowWarps + 1] first record of each (block, tile, warp) slice
+    unsigned *levelCnt = nullptr;    // [slices][levels] runs of each slice with more than q records
     unsigned *flags = nullptr;     // build scratch: unsorted rows, out-of-range successor, longest run
     ~ViTilePlan();
 };
@@ -82,6 +82,10 @@ int vi_plan_build(ViTilePlan *plan, const nova::MDP *mdp, const int *S, const fl
 int vi_tiled_sweep(const ViTilePlan *plan, const nova::MDP *mdp, const float *R, const float *V, float *Vp,
                    unsigned *pi, ViDeviceState *st, double tol, int early_exit, cudaStream_t stream,
                    const char *fn);
+
+// Reads (and clears) the state's error word after the sweeps queued so far
+// finished: NOVA_ERROR_KERNEL_EXECUTION if a bounded wait ran out.
+int vi_state_error(ViDeviceState *st, const char *fn);
 
 // Status of the plan built last in this process (ViTilePlan::Status).
 unsigned vi_last_plan_status();
