@@ -768,12 +768,17 @@ def main():
     model, cfg = workload(args)
     p = POMDP.from_arrays(model)
     p.initialize_gpu()
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
     alg = POMDPPBVIGPU(p, GammaInitial=model["GammaInitial"])
     alg.set_scoring(npp.SCORING_FP16)  # the library's default tensor-core mode
 
     for _ in range(args.warmup):
         alg.update()
     torch.cuda.synchronize()
+    # Device memory the solver holds (scoring operand, projection table,
+    # candidate lists, alpha sets), beside the model's own arrays.
+    solver_bytes = free_before - torch.cuda.mem_get_info()[0]
 
     # ---- timed region: K backups, device-resident inputs --------------------
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -874,7 +879,11 @@ def main():
         fgemm = [(s["uniqueAlphas"], s["msGemm"]) for s in fst if s["msGemm"] > 0]
         fach = (sum(2.0 * r * u * n_pad * cfg["m"] * cfg["z"] for u, _ in fgemm) /
                 (sum(t for _, t in fgemm) * 1e-3) / 1e12) if fgemm else None
+        fgroups = [st["tcGroups"] for st in fst if st["msGemm"] > 0]
+        ftraffic, ftraffic_note = gemm_traffic(cfg["m"] * cfg["z"] * ((r + 127) // 128) * max(1, fgroups[-1]),
+                                               split=True) if fgroups else (None, None)
         bf16 = {"value": r * args.bf16_steps / (fms * 1e-3), "unit": UNIT, "steps": args.bf16_steps,
+                "gemm_traffic": ftraffic, "gemm_traffic_note": ftraffic_note,
                 "ms_per_step": fms / args.bf16_steps, "gemm_tflops_fp16_equivalent": fach,
                 "gemm_tflops": 2.0 * fach if fach else None,
                 "rows_rescored": fl["rowsMultiCand"], "rows_exact_scan": fl["rowsOverflow"],
@@ -942,6 +951,7 @@ def main():
         "clocks": clocks.summary(),
         "step_breakdown_ms": {k: last[k] for k in ("msDedup", "msProject", "msScore", "msGemm", "msRescore",
                                                    "msActions", "msAssemble", "msTotal")},
+        "solver_device_gb": solver_bytes / 1e9,
         "bf16_tc": bf16,
         "unique_alphas": [s["uniqueAlphas"] for s in stats],
         "rows_rescored": last["rowsMultiCand"], "pairs_full_exact": last["rowsOverflow"],
