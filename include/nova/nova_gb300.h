@@ -154,6 +154,22 @@ NOVA_API int pomdp_pbvi_execute_batched_graph_gpu(const POMDP *const *pomdps, PO
         POMDPAlphaVectors *const *policies, unsigned int count, unsigned int scoring,
         unsigned int hostThreads);
 
+/* As pomdp_pbvi_execute_batched_gpu (same arguments, same results), with the
+ * solvers' backups run in lock-step after a warm-up: each solver first runs
+ * ordinary updates on a pool of hostThreads host threads until its
+ * tensor-core schedule is tuned (a tuned solver whose exact scan could be
+ * cheaper also times one update with exact scoring and keeps it if it is);
+ * from then on every backup of every solver is queued without host
+ * read-backs on a stream of its own, and one persistent tcgen05 scoring
+ * launch (per candidate-list length) draws the work units of all
+ * tensor-core solvers from a device table of their tensor maps, shapes and
+ * candidate arrays. The batch runs in waves whose solvers fit in device
+ * memory together. Replaces the reference's one-solve-per-call structure
+ * (pomdp_pbvi_gpu.cu:361-441) for batches; no reference counterpart. */
+NOVA_API int pomdp_pbvi_execute_batched_persistent_gpu(const POMDP *const *pomdps, POMDPPBVIGPU *const *solvers,
+        POMDPAlphaVectors *const *policies, unsigned int count, unsigned int scoring,
+        unsigned int hostThreads);
+
 /* Random belief expansion seeds libc rand() with time(nullptr), as the
  * reference does (pomdp_expand_cpu.cpp:91, pomdp_expand_gpu.cu:139). With
  * fixed != 0, later expansions call srand(seed) instead, so runs repeat;

@@ -128,66 +128,98 @@ __device__ __forceinline__ void prefetch_l2(const uint2 *rec, unsigned b, unsign
 
 constexpr uint2 kNoRecord = {0xFFFFFFFFu, 0u};
 
-// First record and run counts of one slice: n0 runs, n1 of them longer than
-// one record.
-struct SliceHdr {
-    unsigned start, n0, n1;
-};
-__device__ __forceinline__ SliceHdr load_hdr(const unsigned *__restrict__ sliceStart,
-                                             const unsigned *__restrict__ levelCnt, unsigned L, size_t slice) {
-    SliceHdr h;
-    h.start = __ldg(sliceStart + slice);
-    h.n0 = __ldg(levelCnt + slice * L);
-    h.n1 = L > 1 ? __ldg(levelCnt + slice * L + 1) : 0u;
-    return h;
-}
-// The records a lane holds for one slice: the level-0 records of its runs
-// lane + 32 i (i < kSteps) and the level-1 record of run `lane`.
+// What a lane holds for one slice: the slice's first record and run counts
+// (n0 runs, n1 of them with a second record, n2 with a third), the level-0
+// records of its runs lane + 32 i (i < kSteps) and the level-1 record of run
+// `lane`.
 struct SliceRegs {
-    uint2 r0[kSteps];
+    uint2 r[kSteps];
     uint2 r1;
+    unsigned start, n0, n1, n2;
 };
-__device__ __forceinline__ void load_regs(SliceRegs &g, const uint2 *__restrict__ rec, const SliceHdr &h,
-                                          unsigned lane) {
+// hdr = {first record, n0, n1, n2} of the slice.
+__device__ __forceinline__ void load_slice(SliceRegs &g, const uint2 *__restrict__ rec, uint4 hdr, unsigned lane) {
+    g.start = hdr.x;
+    g.n0 = hdr.y;
+    g.n1 = hdr.z;
+    g.n2 = hdr.w;
 #pragma unroll
     for (int i = 0; i < kSteps; i++) {
         const unsigned j = lane + 32u * i;
-        g.r0[i] = j < h.n0 ? __ldg(rec + h.start + j) : kNoRecord;
+        g.r[i] = j < g.n0 ? __ldg(rec + g.start + j) : kNoRecord;
     }
-    g.r1 = lane < h.n1 ? __ldg(rec + h.start + h.n0 + lane) : kNoRecord;
+    g.r1 = lane < g.n1 ? __ldg(rec + g.start + g.n0 + lane) : kNoRecord;
 }
 
-// q + fl(gamma*T) * V[s'] for one record.
-__device__ __forceinline__ float apply_record(float q, uint2 r, const float *vtile, unsigned tileLen) {
-    const unsigned off = r.x & 0xFFFFu;
-    return off < tileLen ? fadd(q, fmul(__uint_as_float(r.y), vtile[off])) : q;
+// part[row] += fl(gamma*T) * V[s'] for one record.
+__device__ __forceinline__ void apply_record(uint2 r, const float *vtile, unsigned tileLen, float *part,
+                                             unsigned rows) {
+    const unsigned row = r.x >> 16, off = r.x & 0xFFFFu;
+    if (row < rows && off < tileLen) part[row] = fadd(part[row], fmul(__uint_as_float(r.y), vtile[off]));
 }
 
-// Run j of a slice: its level-0 record r0, then (j < n1) the further levels
-// in list order; r1 is the level-1 record when already loaded.
-__device__ __forceinline__ void apply_run(uint2 r0, bool have1, uint2 r1, unsigned j, const SliceHdr &h,
-                                          const uint2 *__restrict__ rec, const unsigned *__restrict__ levelCnt,
-                                          unsigned L, size_t slice, const float *vtile, unsigned tileLen,
-                                          float *part, unsigned rows) {
-    const unsigned row = r0.x >> 16;
-    if (row >= rows) return;
-    float q = apply_record(part[row], r0, vtile, tileLen);
-    if (j < h.n1) {
-        q = apply_record(q, have1 ? r1 : __ldg(rec + h.start + h.n0 + j), vtile, tileLen);
-        unsigned base = h.n0 + h.n1;
-        for (unsigned lv = 2; lv < L; lv++) {
-            const unsigned nq = __ldg(levelCnt + slice * L + lv);
-            if (j >= nq) break;
-            q = apply_record(q, __ldg(rec + h.start + base + j), vtile, tileLen);
-            base += nq;
-        }
+// Records of run j from level 1 on (run j has at least two), in list order.
+// Only the rare runs of three or more records read further level counts.
+__device__ __forceinline__ void apply_long_run(const SliceRegs &g, unsigned j, uint2 first1,
+                                               const uint2 *__restrict__ rec, const unsigned *__restrict__ levelCnt,
+                                               unsigned L, unsigned slice, const float *vtile, unsigned tileLen,
+                                               float *part, unsigned rows) {
+    apply_record(first1, vtile, tileLen, part, rows);
+    if (j >= g.n2) return;
+    unsigned base = g.n0 + g.n1;
+    apply_record(__ldg(rec + g.start + base + j), vtile, tileLen, part, rows);
+    base += g.n2;
+    for (unsigned lv = 3; lv < L; lv++) {
+        const unsigned nq = __ldg(levelCnt + (size_t)slice * L + lv);
+        if (j >= nq) break;
+        apply_record(__ldg(rec + g.start + base + j), vtile, tileLen, part, rows);
+        base += nq;
     }
-    part[row] = q;
+}
+
+// One slice: the level-0 record of every run, then the further records of
+// the long runs (runs 0 .. n1-1), each in list order after its level-0
+// record (the same lane applies both; no other run of the slice has that
+// row).
+__device__ __forceinline__ void apply_slice(const SliceRegs &g, const uint2 *__restrict__ rec,
+                                            const unsigned *__restrict__ levelCnt, unsigned L, unsigned slice,
+                                            const float *vtile, unsigned tileLen, float *part, unsigned rows,
+                                            unsigned lane) {
+#pragma unroll
+    for (int i = 0; i < kSteps; i++)
+        if (lane + 32u * i < g.n0) apply_record(g.r[i], vtile, tileLen, part, rows);
+    for (unsigned j = lane + 32u * kSteps; j < g.n0; j += 32u)
+        apply_record(__ldg(rec + g.start + j), vtile, tileLen, part, rows);
+    if (lane < g.n1) apply_long_run(g, lane, g.r1, rec, levelCnt, L, slice, vtile, tileLen, part, rows);
+    for (unsigned j = lane + 32u; j < g.n1; j += 32u)
+        apply_long_run(g, j, __ldg(rec + g.start + g.n0 + j), rec, levelCnt, L, slice, vtile, tileLen, part, rows);
+}
+
+// One tile of a row warp: load the next slice (and the header after it),
+// wait for the V tile, apply the current slice, release the buffer.
+__device__ __forceinline__ bool row_warp_tile(unsigned t, unsigned T, const SliceRegs &cur, SliceRegs &nxt,
+                                              uint4 &hNext, unsigned sl0, const uint2 *__restrict__ rec,
+                                              const uint4 *__restrict__ sliceHdr,
+                                              const unsigned *__restrict__ levelCnt, unsigned L, const float *vt,
+                                              unsigned Vt, unsigned n, float *part, unsigned rows, uint64_t *bars,
+                                              unsigned &sg, unsigned &ph, volatile int *abortFlag,
+                                              ViDeviceState *st, unsigned lane) {
+    if (t + 1 < T) {
+        load_slice(nxt, rec, hNext, lane);
+        hNext = t + 2 < T ? __ldg(sliceHdr + sl0 + (t + 2) * kRowWarps) : make_uint4(0u, 0u, 0u, 0u);
+    }
+    if (!mbar_wait(smem_addr(&bars[sg]), ph, abortFlag, st)) return false;
+    apply_slice(cur, rec, levelCnt, L, sl0 + t * kRowWarps, vt + (size_t)sg * Vt, min(Vt, n - t * Vt), part, rows,
+                lane);
+    __syncwarp();
+    if (lane == 0) mbar_arrive(smem_addr(&bars[kStages + sg]));
+    if (++sg == kStages) { sg = 0; ph ^= 1u; }
+    return true;
 }
 
 __global__ void __launch_bounds__(kThreads, 1) bellman_tiled_kernel(
         unsigned n, unsigned m, unsigned Vt, unsigned T, unsigned Sb, unsigned blocks, unsigned L,
-        const uint2 *__restrict__ rec, const unsigned *__restrict__ sliceStart,
+        const uint2 *__restrict__ rec, const unsigned *__restrict__ sliceStart, const uint4 *__restrict__ sliceHdr,
         const unsigned *__restrict__ levelCnt, const float *__restrict__ R, const float *__restrict__ V,
         float *__restrict__ Vp, unsigned *__restrict__ pi, ViDeviceState *st, double tol, int early_exit) {
     if (early_exit && *(volatile unsigned *)&st->converged) return;  // uniform across the grid
@@ -242,38 +274,21 @@ __global__ void __launch_bounds__(kThreads, 1) bellman_tiled_kernel(
             }
         } else {
             // ---- row warps ----
-            const size_t sl0 = c0 * kRowWarps + warp;   // slice of (blk, t) is sl0 + t * kRowWarps
-            SliceHdr hA = load_hdr(sliceStart, levelCnt, L, sl0);
-            SliceHdr hB = T > 1 ? load_hdr(sliceStart, levelCnt, L, sl0 + kRowWarps) : SliceHdr{0, 0, 0};
-            SliceRegs cur, nxt;
-            load_regs(cur, rec, hA, lane);
+            // Slice (blk, t) of this warp is sl0 + t * kRowWarps. Records of
+            // slice t+1 are loaded while slice t is applied; the two register
+            // sets alternate roles, so nothing is copied between tiles.
+            const unsigned sl0 = (unsigned)(c0 * kRowWarps) + warp;
+            SliceRegs ga, gb;
+            load_slice(ga, rec, __ldg(sliceHdr + sl0), lane);
+            uint4 hNext = T > 1 ? __ldg(sliceHdr + sl0 + kRowWarps) : make_uint4(0u, 0u, 0u, 0u);
             unsigned sg = stage, ph = phase;
-            for (unsigned t = 0; t < T; t++) {
-                const size_t slice = sl0 + (size_t)t * kRowWarps;
-                SliceHdr hC{0, 0, 0};
-                if (t + 1 < T) {
-                    load_regs(nxt, rec, hB, lane);
-                    if (t + 2 < T) hC = load_hdr(sliceStart, levelCnt, L, slice + 2 * kRowWarps);
-                }
-                if (!mbar_wait(smem_addr(&bars[sg]), ph, abortFlag, st)) break;
-                const float *vcur = vt + (size_t)sg * Vt;
-                const unsigned tileLen = min(Vt, n - t * Vt);
-#pragma unroll
-                for (int i = 0; i < kSteps; i++) {
-                    const unsigned j = lane + 32u * i;
-                    if (j < hA.n0)
-                        apply_run(cur.r0[i], i == 0, cur.r1, j, hA, rec, levelCnt, L, slice, vcur, tileLen, part,
-                                  rows);
-                }
-                for (unsigned j = lane + 32u * kSteps; j < hA.n0; j += 32u)
-                    apply_run(__ldg(rec + hA.start + j), false, kNoRecord, j, hA, rec, levelCnt, L, slice, vcur,
-                              tileLen, part, rows);
-                __syncwarp();
-                if (lane == 0) mbar_arrive(smem_addr(&bars[kStages + sg]));
-                if (++sg == kStages) { sg = 0; ph ^= 1u; }
-                cur = nxt;
-                hA = hB;
-                hB = hC;
+            for (unsigned t = 0; t < T; t += 2) {
+                if (!row_warp_tile(t, T, ga, gb, hNext, sl0, rec, sliceHdr, levelCnt, L, vt, Vt, n, part, rows, bars,
+                                   sg, ph, abortFlag, st, lane))
+                    break;
+                if (t + 1 < T && !row_warp_tile(t + 1, T, gb, ga, hNext, sl0, rec, sliceHdr, levelCnt, L, vt, Vt, n,
+                                                part, rows, bars, sg, ph, abortFlag, st, lane))
+                    break;
             }
         }
         // Every warp advances the ring by the block's T tiles.
@@ -400,6 +415,16 @@ __global__ void vi_plan_slice_kernel(size_t nSlices, unsigned L, const unsigned 
         *p = run;
         run += v;
     }
+}
+
+// Slice headers for the sweep: {first record, runs, runs with a second
+// record, runs with a third record}.
+__global__ void vi_plan_hdr_kernel(size_t nSlices, unsigned L, const unsigned *__restrict__ sliceStart,
+                                   const unsigned *__restrict__ levelCnt, uint4 *__restrict__ hdr) {
+    const size_t sl = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (sl >= nSlices) return;
+    hdr[sl] = make_uint4(sliceStart[sl], levelCnt[sl * L], L > 1 ? levelCnt[sl * L + 1] : 0u,
+                         L > 2 ? levelCnt[sl * L + 2] : 0u);
 }
 
 // Write every record at its place. The position j of a run in its slice's
@@ -533,10 +558,12 @@ bool try_alloc(T **p, size_t count) {
 void release(ViTilePlan *plan) {
     cudaFree(plan->rec);
     cudaFree(plan->sliceStart);
+    cudaFree(plan->sliceHdr);
     cudaFree(plan->levelCnt);
     cudaFree(plan->flags);
     plan->rec = nullptr;
     plan->sliceStart = plan->levelCnt = plan->flags = nullptr;
+    plan->sliceHdr = nullptr;
 }
 
 int scan_counts(const unsigned *counts, unsigned long long N, unsigned *out, cudaStream_t stream, const char *fn) {
@@ -671,6 +698,12 @@ int vi_plan_build(ViTilePlan *plan, const MDP *mdp, const int *S, const float *T
         rc = check_launch(fn, "sweep plan (slices)");
     }
     if (rc == NOVA_SUCCESS) rc = scan_counts(sliceSize, nSlices, plan->sliceStart, stream, fn);
+    if (rc == NOVA_SUCCESS && !try_alloc(&plan->sliceHdr, nSlices)) rc = NOVA_ERROR_DEVICE_MALLOC;
+    if (rc == NOVA_SUCCESS) {
+        vi_plan_hdr_kernel<<<ceil_div(nSlices, 256), 256, 0, stream>>>((size_t)nSlices, L, plan->sliceStart,
+                                                                       plan->levelCnt, plan->sliceHdr);
+        rc = check_launch(fn, "sweep plan (headers)");
+    }
     unsigned total = 0;
     if (rc == NOVA_SUCCESS)
         rc = d2h(&total, plan->sliceStart + nSlices, sizeof(unsigned), fn, "the sweep plan size");
@@ -710,7 +743,7 @@ int vi_tiled_sweep(const ViTilePlan *plan, const MDP *mdp, const float *R, const
                    ViDeviceState *st, double tol, int early_exit, cudaStream_t stream, const char *fn) {
     bellman_tiled_kernel<<<plan->grid, kThreads, plan->smemBytes, stream>>>(
         mdp->n, mdp->m, plan->tileStates, plan->tiles, plan->blockStates, plan->blocks, plan->levels, plan->rec,
-        plan->sliceStart, plan->levelCnt, R, V, Vp, pi, st, tol, early_exit);
+        plan->sliceStart, plan->sliceHdr, plan->levelCnt, R, V, Vp, pi, st, tol, early_exit);
     return check_launch(fn, "Bellman update (tiled)");
 }
 

@@ -1186,7 +1186,7 @@ bool BackupEngine::fixed_ready() const {
            (scoring == NOVA_SCORING_BF16 || scoring == NOVA_SCORING_FP16);
 }
 
-int BackupEngine::backup_fixed(const float *src, float *dst, unsigned *pi, const char *fn) {
+int BackupEngine::fixed_pre(const float *src, bool tensor, const char *fn) {
     int rc;
     const unsigned nU = md.r;
     dim3 grid(ceil_div(nU, 32), ceil_div(md.n, 32));
@@ -1198,12 +1198,52 @@ int BackupEngine::backup_fixed(const float *src, float *dst, unsigned *pi, const
         const unsigned zc = md.z >= 16 ? 32u : 8u;
         const size_t smemSM = (size_t)kProjTileS * (md.ns * zc + 4) * sizeof(float) +
                               (size_t)kProjTileS * md.ns * sizeof(int);
-        projStateMajor = state_major_wanted(smemSM);
+        projStateMajor = tensor && state_major_wanted(smemSM);
     }
     if ((rc = project(nU, fn)) != NOVA_SUCCESS) return rc;
-    if ((rc = tc_score_launch(*this, src, nU, false, fn)) != NOVA_SUCCESS) return rc;
-    if ((rc = scan_rows(tc_row_list(*this), md.m * md.z * md.r, nU, fn, itemCount)) != NOVA_SUCCESS) return rc;
+    return tensor ? tc_prepare(*this, src, nU, fn) : NOVA_SUCCESS;
+}
+
+int BackupEngine::fixed_post(const float *src, float *dst, unsigned *pi, bool tensor, const char *fn) {
+    int rc;
+    const unsigned nU = md.r;
+    if (tensor) {
+        if ((rc = tc_finish(*this, fn)) != NOVA_SUCCESS) return rc;
+        rc = scan_rows(tc_row_list(*this), md.m * md.z * md.r, nU, fn, itemCount);
+    } else {
+        rc = scan_rows(nullptr, md.m * md.z * md.r, nU, fn);
+    }
+    if (rc != NOVA_SUCCESS) return rc;
     return assemble(src, dst, pi, -1, nullptr, nullptr, fn);
+}
+
+int BackupEngine::backup_fixed(const float *src, float *dst, unsigned *pi, const char *fn) {
+    int rc;
+    if ((rc = fixed_pre(src, true, fn)) != NOVA_SUCCESS) return rc;
+    if ((rc = tc_gemm(*this, false, fn)) != NOVA_SUCCESS) return rc;
+    return fixed_post(src, dst, pi, true, fn);
+}
+
+int BackupEngine::fixed_setup(const char *fn) {
+    int rc;
+    if (!identityUniq) {
+        if ((rc = fill_items(0, md.r, fn)) != NOVA_SUCCESS) return rc;
+        if (cudaMemcpyAsync(uniqJ, items, (size_t)md.r * sizeof(unsigned), cudaMemcpyDeviceToDevice, stream) !=
+                cudaSuccess) {
+            cudaGetLastError();
+            return NOVA_ERROR_KERNEL_EXECUTION;
+        }
+        identityUniq = true;
+    }
+    const size_t rows = (size_t)md.m * md.z * md.r;
+    if (scanCap < rows) {
+        cudaFree(scanV); cudaFree(scanU);
+        scanV = nullptr; scanU = nullptr; scanCap = 0;
+        if ((rc = dev_alloc(&scanV, rows, fn, "the scan maxima")) != NOVA_SUCCESS) return rc;
+        if ((rc = dev_alloc(&scanU, rows, fn, "the scan arg-maxima")) != NOVA_SUCCESS) return rc;
+        scanCap = rows;
+    }
+    return NOVA_SUCCESS;
 }
 
 // Selections of the last backup: for belief i, the action a = pi[i] whose
@@ -1327,6 +1367,13 @@ static PbviGpuWorkspace *pbvi_gpu_ws(const POMDPPBVIGPU *pbvi) {
     std::lock_guard<std::mutex> lock(registry_mutex());
     return find_workspace<PbviGpuWorkspace>(pbvi);
 }
+
+namespace nova_gb300 {
+BackupEngine *pbvi_gpu_engine(const POMDPPBVIGPU *pbvi) {
+    PbviGpuWorkspace *ws = pbvi_gpu_ws(pbvi);
+    return ws != nullptr && ws->built ? &ws->eng : nullptr;
+}
+}  // namespace nova_gb300
 
 extern "C" int pomdp_pbvi_uninitialize_gpu(const POMDP *pomdp, POMDPPBVIGPU *pbvi) {
     (void)pomdp;
@@ -1453,23 +1500,7 @@ static bool graph_needs_capture(const BackupEngine &e, const float *src) {
 // Under capture_lock() held exclusively.
 static int graph_prepare(BackupEngine &e, const float *src, float *dst, unsigned *pi, const char *fn) {
     int rc;
-    if (!e.identityUniq) {
-        if ((rc = e.fill_items(0, e.md.r, fn)) != NOVA_SUCCESS) return rc;
-        if (cudaMemcpyAsync(e.uniqJ, e.items, (size_t)e.md.r * sizeof(unsigned), cudaMemcpyDeviceToDevice,
-                            e.stream) != cudaSuccess) {
-            cudaGetLastError();
-            return NOVA_ERROR_KERNEL_EXECUTION;
-        }
-        e.identityUniq = true;
-    }
-    const size_t rows = (size_t)e.md.m * e.md.z * e.md.r;
-    if (e.scanCap < rows) {
-        cudaFree(e.scanV); cudaFree(e.scanU);
-        e.scanV = nullptr; e.scanU = nullptr; e.scanCap = 0;
-        if ((rc = dev_alloc(&e.scanV, rows, fn, "the scan maxima")) != NOVA_SUCCESS) return rc;
-        if ((rc = dev_alloc(&e.scanU, rows, fn, "the scan arg-maxima")) != NOVA_SUCCESS) return rc;
-        e.scanCap = rows;
-    }
+    if ((rc = e.fixed_setup(fn)) != NOVA_SUCCESS) return rc;
     if (!e.fixed_ready()) {
         e.graphMode = false;
         return NOVA_SUCCESS;

@@ -9,6 +9,7 @@
 #include <shared_mutex>
 
 #include <nova/pomdp/pomdp.h>
+#include <nova/pomdp/algorithms/pomdp_pbvi_gpu.h>
 #include <nova/nova_gb300.h>
 
 namespace nova_gb300 {
@@ -115,6 +116,14 @@ struct BackupEngine {
     // scoring with the solver's fixed schedule, the exact scan sized on the
     // device. Same results as backup_all.
     int backup_fixed(const float *src, float *dst, unsigned *pi, const char *fn);
+    // backup_fixed in two halves around the scoring GEMM (tensor) or, with
+    // tensor false, an update that scans every row exactly; no host
+    // read-back in either.
+    int fixed_pre(const float *src, bool tensor, const char *fn);
+    int fixed_post(const float *src, float *dst, unsigned *pi, bool tensor, const char *fn);
+    // Identity unique-alpha map and exact-scan capacity for every row, which
+    // the fixed updates need.
+    int fixed_setup(const char *fn);
     // Ready for backup_fixed: tensor-core scoring built with a fixed
     // schedule, the projection table allocated for all r alphas.
     bool fixed_ready() const;
@@ -146,6 +155,10 @@ struct BackupEngine {
 // else that may run beside a capture in another host thread.
 std::shared_mutex &capture_lock();
 
+// The backup engine of an initialized device solver whose tables are built
+// (after its first update), or null.
+BackupEngine *pbvi_gpu_engine(const nova::POMDPPBVIGPU *pbvi);
+
 // Tensor-core scoring (pbvi_tc.cu). tc_supported: the shapes fit the GEMM.
 bool tc_supported(const DevModel &md);
 // Builds the BF16 operand tables once; returns NOVA_SUCCESS or an error.
@@ -159,6 +172,21 @@ int tc_build(BackupEngine &eng, const char *fn);
 // count stay on the device (eng.tc rowList, eng.itemCount); `timed` records
 // the GEMM events.
 int tc_score_launch(BackupEngine &eng, const float *src, unsigned nU, bool timed, const char *fn);
+// The three parts of tc_score_launch: packing, margins and schedule (kept in
+// the state for the other two), the GEMM of this solver alone, and the
+// merge with the exact-scan list.
+int tc_prepare(BackupEngine &eng, const float *src, unsigned nU, const char *fn);
+int tc_gemm(BackupEngine &eng, bool timed, const char *fn);
+int tc_finish(BackupEngine &eng, const char *fn);
+// One persistent scoring launch (per candidate-list length) over the work
+// units of many prepared solvers, drawn from a device table of their
+// tensor maps, shapes and candidate arrays; the table is built once from
+// the solvers' prepared launches and stays valid while their schedules,
+// operands and alpha counts do.
+struct TcBatch;
+int tc_batch_create(BackupEngine *const *engs, unsigned count, TcBatch **out, const char *fn);
+int tc_batch_gemm(TcBatch *batch, cudaStream_t stream, const char *fn);
+void tc_batch_release(TcBatch *batch);
 bool tc_schedule_fixed(const BackupEngine &eng);  // and built for eng.scoring
 const unsigned *tc_row_list(const BackupEngine &eng);
 int tc_score(BackupEngine &eng, const float *src, unsigned nU, unsigned *nRows, const unsigned **rowList,
@@ -170,6 +198,9 @@ int tc_row_detail(const BackupEngine &eng, unsigned *candidates, unsigned *exact
 // Feeds one tensor-core update's scoring time (GEMM, merge and the exact
 // scan it left) to the solver's alpha-group tuner.
 void tc_tune_feedback(BackupEngine &eng, float msScoring, unsigned nU);
+// Scoring time per unique alpha of the tuned schedule (ms), or a negative
+// value when the schedule was fixed without timing.
+float tc_tuned_cost(const BackupEngine &eng);
 unsigned tc_device_error();
 
 }  // namespace nova_gb300

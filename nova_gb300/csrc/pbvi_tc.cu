@@ -49,6 +49,8 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <mutex>
+#include <type_traits>
 #include <vector>
 #include <cmath>
 
@@ -120,7 +122,13 @@ struct TcState {
     unsigned tuneNext = 0;          // next trial
     bool tuneWarm = false;          // the first tensor-core update (lazy set-up) is not timed
     unsigned groupsUsed = 0;        // groups of the last launch
-    float tuneCost[3] = {0, 0, 0};   // one per tuned schedule
+    float tuneCost[3] = {0, 0, 0};  // one per tuned schedule
+    // The launch prepared by tc_prepare for tc_gemm / tc_finish.
+    struct Launch {
+        unsigned nU = 0, nTiles = 0, groups = 0, lists = 0, topk = 0, kSplit = 1;
+        bool fp16 = true;
+        CUtensorMap tmB;
+    } last;
 };
 
 // Schedules: alpha groups per row tile and entries per candidate list.
@@ -358,13 +366,74 @@ __device__ __forceinline__ float row_margin(const float *__restrict__ a1, const 
     return 2.0f * (a1[idx] * escale + d1[idx] * dscale);
 }
 
-template <int K>
+// What a work unit needs: its tensor maps, its place (a*z+o pair, 128-row
+// tile, alpha group and the group's 256-alpha tiles) and its solver's shapes,
+// bounds and candidate lists.
+struct UnitParams {
+    const CUtensorMap *tmA, *tmB;
+    unsigned ao, mt, g, nt0, nt1;
+    unsigned rPad, r, nU, kBlocks, kSplit;
+    const float *a1, *d1;
+    const unsigned *scal;
+    float *candV;
+    unsigned *candU;
+    float *candX;
+};
+
+// One solver's units (the tensor maps are kernel parameters).
+struct SingleUnits {
+    unsigned MZ, rPad, r, mTiles, nTiles, groups, nU, kBlocks, kSplit;
+    const float *a1, *d1;
+    const unsigned *scal;
+    float *candV;
+    unsigned *candU;
+    float *candX;
+    __device__ __forceinline__ unsigned total() const { return MZ * mTiles * groups; }
+    __device__ __forceinline__ void get(unsigned unit, UnitParams &p) const {
+        decode_unit(unit, groups, mTiles, nTiles, p.ao, p.mt, p.g, p.nt0, p.nt1);
+        p.rPad = rPad; p.r = r; p.nU = nU; p.kBlocks = kBlocks; p.kSplit = kSplit;
+        p.a1 = a1; p.d1 = d1; p.scal = scal; p.candV = candV; p.candU = candU; p.candX = candX;
+    }
+};
+
+// A solver of a batched launch: its tensor maps in global memory (64-byte
+// aligned) and its first unit in the launch's unit sequence.
+struct alignas(64) BatchModel {
+    CUtensorMap tmA, tmB;
+    unsigned unitStart, MZ, rPad, r, mTiles, nTiles, groups, nU, kBlocks, kSplit;
+    const float *a1, *d1;
+    const unsigned *scal;
+    float *candV;
+    unsigned *candU;
+    float *candX;
+};
+
+// The units of many solvers in one sequence (solver k owns units
+// [unitStart_k, unitStart_{k+1})): a device work table the persistent CTAs
+// draw from.
+struct BatchUnits {
+    const BatchModel *models;
+    unsigned nModels, totalUnits;
+    __device__ __forceinline__ unsigned total() const { return totalUnits; }
+    __device__ __forceinline__ void get(unsigned unit, UnitParams &p) const {
+        unsigned lo = 0, hi = nModels - 1;
+        while (lo < hi) {   // last model whose first unit is <= unit
+            const unsigned mid = (lo + hi + 1) >> 1;
+            if (models[mid].unitStart <= unit) lo = mid;
+            else hi = mid - 1;
+        }
+        const BatchModel &b = models[lo];
+        decode_unit(unit - b.unitStart, b.groups, b.mTiles, b.nTiles, p.ao, p.mt, p.g, p.nt0, p.nt1);
+        p.tmA = &b.tmA; p.tmB = &b.tmB;
+        p.rPad = b.rPad; p.r = b.r; p.nU = b.nU; p.kBlocks = b.kBlocks; p.kSplit = b.kSplit;
+        p.a1 = b.a1; p.d1 = b.d1; p.scal = b.scal; p.candV = b.candV; p.candU = b.candU; p.candX = b.candX;
+    }
+};
+
+template <int K, class Units>
 __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
         const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, uint32_t idesc,
-        unsigned MZ, unsigned rPad, unsigned r, unsigned mTiles, unsigned nTiles, unsigned groups, unsigned nU,
-        unsigned kBlocks, unsigned kSplit, const float *__restrict__ a1, const float *__restrict__ d1,
-        const unsigned *__restrict__ scal, float *__restrict__ candV, unsigned *__restrict__ candU,
-        float *__restrict__ candX) {
+        const Units units) {
     extern __shared__ uint8_t smemRaw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smemRaw) + 1023) & ~(uintptr_t)1023);
     uint8_t *sA = smem;
@@ -395,25 +464,31 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
     tc_fence_after();
     const uint32_t tmem = bar->tmemBase;
     volatile int *abortFlag = &bar->abortFlag;
-    const unsigned totalUnits = MZ * mTiles * groups;
+    const unsigned totalUnits = units.total();
+    // Units of a single solver take the tensor maps from the kernel
+    // parameters; a batch's from its work table.
+    auto unit_params = [&](unsigned unit, UnitParams &p) {
+        units.get(unit, p);
+        if constexpr (std::is_same<Units, SingleUnits>::value) { p.tmA = &tmA; p.tmB = &tmB; }
+    };
 
     if (warp == 0) {
         if (lane == 0) {
             // ---- TMA producer ----
             unsigned stage = 0, phase = 0;
             for (unsigned unit = blockIdx.x; unit < totalUnits && !*abortFlag; unit += gridDim.x) {
-                unsigned ao, mt, g, nt0, nt1;
-                decode_unit(unit, groups, mTiles, nTiles, ao, mt, g, nt0, nt1);
-                const int rowA = (int)(ao * rPad + mt * BM);
-                for (unsigned nt = nt0; nt < nt1 && !*abortFlag; nt++) {
+                UnitParams p;
+                unit_params(unit, p);
+                const int rowA = (int)(p.ao * p.rPad + p.mt * BM);
+                for (unsigned nt = p.nt0; nt < p.nt1 && !*abortFlag; nt++) {
                     // kSplit B blocks per A block: the split alphas carry a hi
                     // and a lo block for each 64-state block of A.
-                    for (unsigned kb = 0; kb < kBlocks * kSplit; kb++) {
+                    for (unsigned kb = 0; kb < p.kBlocks * p.kSplit; kb++) {
                         if (!mbar_wait(smem_u32(&bar->empty[stage]), phase ^ 1u, abortFlag)) break;
                         const uint32_t fb = smem_u32(&bar->full[stage]);
                         mbar_expect_tx(fb, A_STAGE_BYTES + B_STAGE_BYTES);
-                        tma_load_2d(smem_u32(sA + stage * A_STAGE_BYTES), &tmA, (int)((kb / kSplit) * BK), rowA, fb);
-                        tma_load_2d(smem_u32(sB + stage * B_STAGE_BYTES), &tmB, (int)(kb * BK), (int)(nt * BN), fb);
+                        tma_load_2d(smem_u32(sA + stage * A_STAGE_BYTES), p.tmA, (int)((kb / p.kSplit) * BK), rowA, fb);
+                        tma_load_2d(smem_u32(sB + stage * B_STAGE_BYTES), p.tmB, (int)(kb * BK), (int)(nt * BN), fb);
                         if (++stage == STAGES) { stage = 0; phase ^= 1u; }
                     }
                 }
@@ -424,13 +499,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
             // ---- MMA issuer ----
             unsigned stage = 0, phase = 0, acc = 0, accPhase = 0;
             for (unsigned unit = blockIdx.x; unit < totalUnits && !*abortFlag; unit += gridDim.x) {
-                unsigned ao, mt, g, nt0, nt1;
-                decode_unit(unit, groups, mTiles, nTiles, ao, mt, g, nt0, nt1);
-                for (unsigned nt = nt0; nt < nt1 && !*abortFlag; nt++) {
+                UnitParams p;
+                unit_params(unit, p);
+                for (unsigned nt = p.nt0; nt < p.nt1 && !*abortFlag; nt++) {
                     if (!mbar_wait(smem_u32(&bar->accEmpty[acc]), accPhase ^ 1u, abortFlag)) break;
                     tc_fence_after();
                     const uint32_t dtmem = tmem + acc * BN;
-                    for (unsigned kb = 0; kb < kBlocks * kSplit; kb++) {
+                    for (unsigned kb = 0; kb < p.kBlocks * p.kSplit; kb++) {
                         if (!mbar_wait(smem_u32(&bar->full[stage]), phase, abortFlag)) break;
                         tc_fence_after();
                         const uint64_t adesc = smem_desc_sw128(smem_u32(sA + stage * A_STAGE_BYTES));
@@ -466,23 +541,24 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
         const unsigned quarter = warp & 3u;   // TMEM lanes this warp may access
         const unsigned half = (warp - 2u) >> 2;
         const unsigned rowInTile = quarter * 32u + lane;
-        const float escale = __uint_as_float(scal[2]);
-        const float dscale = __uint_as_float(scal[7]);
         const float qnan = __uint_as_float(0x7fc00000u);
         unsigned acc = 0, accPhase = 0;
         TopList<K> top;
         for (unsigned unit = blockIdx.x; unit < totalUnits && !*abortFlag; unit += gridDim.x) {
-            unsigned ao, mt, g, nt0, nt1;
-            decode_unit(unit, groups, mTiles, nTiles, ao, mt, g, nt0, nt1);
+            UnitParams p;
+            unit_params(unit, p);
+            const unsigned ao = p.ao, g = p.g, r = p.r, nU = p.nU;
+            const float escale = __uint_as_float(p.scal[2]);
+            const float dscale = __uint_as_float(p.scal[7]);
             top.reset();
-            const unsigned iRow = mt * BM + rowInTile;
+            const unsigned iRow = p.mt * BM + rowInTile;
             // Same expression as the merge's margin. An infinite margin skips
             // nothing; a NaN one skips everything, and the merge sends such
             // rows to the exact scan whatever their lists hold.
-            const float thr = iRow < r ? row_margin(a1, d1, (size_t)ao * rPad + iRow, escale, dscale) : INFINITY;
+            const float thr = iRow < r ? row_margin(p.a1, p.d1, (size_t)ao * p.rPad + iRow, escale, dscale) : INFINITY;
             float best = -INFINITY, lim = -INFINITY;
             bool ok = true;
-            for (unsigned nt = nt0; nt < nt1; nt++) {
+            for (unsigned nt = p.nt0; nt < p.nt1; nt++) {
                 if (!mbar_wait(smem_u32(&bar->accFull[acc]), accPhase, abortFlag)) { ok = false; break; }
                 tc_fence_after();
                 const uint32_t base = tmem + ((quarter * 32u) << 16) + acc * BN;
@@ -529,11 +605,11 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) tc_score_gemm_kernel(
             if (!ok) break;
             if (iRow < r) {
                 const size_t slot = ((size_t)ao * r + iRow) * MAX_LISTS + 2u * g + half;
-                float *cv = candV + slot * MAX_TOPK;
-                unsigned *cu = candU + slot * MAX_TOPK;
+                float *cv = p.candV + slot * MAX_TOPK;
+                unsigned *cu = p.candU + slot * MAX_TOPK;
 #pragma unroll
                 for (int k = 0; k < K; k++) { cv[k] = top.v[k]; cu[k] = top.u[k]; }
-                candX[slot] = top.excl;
+                p.candX[slot] = top.excl;
             }
         }
     }
@@ -1042,6 +1118,24 @@ static int tc_build_operand(BackupEngine &eng, TcState *tc, const char *fn) {
     return encode_map(tc, &tc->tmA, tc->A, (size_t)tc->MZ * tc->rPad, tc->nPad, BM, fn);
 }
 
+// Dynamic shared memory of every scoring-kernel instantiation (once).
+static bool gemm_attributes_set() {
+    static std::once_flag once;
+    static bool ok = false;
+    std::call_once(once, [] {
+        const int b = (int)GEMM_SMEM;
+        const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+        ok = cudaFuncSetAttribute(tc_score_gemm_kernel<8, SingleUnits>, attr, b) == cudaSuccess &&
+             cudaFuncSetAttribute(tc_score_gemm_kernel<16, SingleUnits>, attr, b) == cudaSuccess &&
+             cudaFuncSetAttribute(tc_score_gemm_kernel<32, SingleUnits>, attr, b) == cudaSuccess &&
+             cudaFuncSetAttribute(tc_score_gemm_kernel<8, BatchUnits>, attr, b) == cudaSuccess &&
+             cudaFuncSetAttribute(tc_score_gemm_kernel<16, BatchUnits>, attr, b) == cudaSuccess &&
+             cudaFuncSetAttribute(tc_score_gemm_kernel<32, BatchUnits>, attr, b) == cudaSuccess;
+        if (!ok) cudaGetLastError();
+    });
+    return ok;
+}
+
 int tc_build(BackupEngine &eng, const char *fn) {
     if (eng.tc) return NOVA_SUCCESS;
     const DevModel &md = eng.md;
@@ -1094,12 +1188,7 @@ int tc_build(BackupEngine &eng, const char *fn) {
     tc->numSMs = prop.multiProcessorCount;
     cudaEventCreate(&tc->g0);
     cudaEventCreate(&tc->g1);
-    if (cudaFuncSetAttribute(tc_score_gemm_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(tc_score_gemm_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(tc_score_gemm_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GEMM_SMEM) !=
-            cudaSuccess) {
+    if (!gemm_attributes_set()) {
         cudaGetLastError();
         NOVA_ERR(fn, "Failed to configure the scoring kernel's shared memory.");
         return NOVA_ERROR_KERNEL_EXECUTION;
@@ -1108,7 +1197,7 @@ int tc_build(BackupEngine &eng, const char *fn) {
     return sync_device(fn);
 }
 
-int tc_score_launch(BackupEngine &eng, const float *src, unsigned nU, bool timed, const char *fn) {
+int tc_prepare(BackupEngine &eng, const float *src, unsigned nU, const char *fn) {
     int rc;
     if (!eng.tc && (rc = tc_build(eng, fn)) != NOVA_SUCCESS) return rc;
     TcState *tc = eng.tc;
@@ -1154,47 +1243,170 @@ int tc_score_launch(BackupEngine &eng, const float *src, unsigned nU, bool timed
     const float gN = (float)((double)(md.ns + md.rz + 3) * u24 * 1.01);
     tc_escale_kernel<<<1, 1, 0, eng.stream>>>(tc->scal, U, gN);
     if ((rc = check_launch(fn, "margin")) != NOVA_SUCCESS) return rc;
-    // ---- GEMM ----
-    CUtensorMap tmB;
-    if ((rc = encode_map(tc, &tmB, tc->Gb, nPadRows, tc->nPad * kSplit, BN, fn)) != NOVA_SUCCESS) return rc;
+    // ---- schedule and the alphas' tensor map ----
+    TcState::Launch &L = tc->last;
+    if ((rc = encode_map(tc, &L.tmB, tc->Gb, nPadRows, tc->nPad * kSplit, BN, fn)) != NOVA_SUCCESS) return rc;
     // Each alpha group leaves two lists per row (one per epilogue half).
     if (tc->schedFixed < 0 && tc->nPad > kTuneMaxNPad) tc->schedFixed = fp16 ? kDeepScheduleFp16 : kDeepScheduleBf16;
     const TcSchedule sched = kSchedules[tc->schedFixed >= 0 ? tc->schedFixed : (tc->tuneWarm ? (int)tc->tuneNext : 0)];
-    const unsigned groups = std::max(1u, std::min<unsigned>(sched.groups, nTiles));
-    const unsigned lists = 2u * groups;
-    tc->groupsUsed = groups;
-    const unsigned totalUnits = tc->MZ * tc->mTiles * groups;
+    L.nU = nU;
+    L.nTiles = nTiles;
+    L.groups = std::max(1u, std::min<unsigned>(sched.groups, nTiles));
+    L.lists = 2u * L.groups;
+    L.topk = sched.topk;
+    L.kSplit = kSplit;
+    L.fp16 = fp16;
+    tc->groupsUsed = L.groups;
+    return NOVA_SUCCESS;
+}
+
+// The scoring GEMM of one prepared solver on its stream.
+int tc_gemm(BackupEngine &eng, bool timed, const char *fn) {
+    TcState *tc = eng.tc;
+    const TcState::Launch &L = tc->last;
+    const unsigned totalUnits = tc->MZ * tc->mTiles * L.groups;
     const unsigned grid = std::min<unsigned>(totalUnits, (unsigned)tc->numSMs);
     if (timed) cudaEventRecord(tc->g0, eng.stream);
-    auto gemm = sched.topk == 32u ? tc_score_gemm_kernel<32>
-                : (sched.topk == 16u ? tc_score_gemm_kernel<16> : tc_score_gemm_kernel<8>);
-    gemm<<<grid, GEMM_THREADS, GEMM_SMEM, eng.stream>>>(
-        tc->tmA, tmB, make_idesc(fp16 ? 0u : 1u), tc->MZ, (unsigned)tc->rPad, md.r, tc->mTiles, nTiles, groups, nU,
-        (unsigned)(tc->nPad / BK), kSplit, tc->a1, tc->d1, tc->scal, tc->candV, tc->candU, tc->candX);
-    if ((rc = check_launch(fn, "tensor-core scoring")) != NOVA_SUCCESS) return rc;
+    auto gemm = L.topk == 32u ? tc_score_gemm_kernel<32, SingleUnits>
+                : (L.topk == 16u ? tc_score_gemm_kernel<16, SingleUnits> : tc_score_gemm_kernel<8, SingleUnits>);
+    const SingleUnits units{tc->MZ, (unsigned)tc->rPad, eng.md.r, tc->mTiles, L.nTiles, L.groups, L.nU,
+                            (unsigned)(tc->nPad / BK), L.kSplit, tc->a1, tc->d1, tc->scal, tc->candV, tc->candU,
+                            tc->candX};
+    gemm<<<grid, GEMM_THREADS, GEMM_SMEM, eng.stream>>>(tc->tmA, L.tmB, make_idesc(L.fp16 ? 0u : 1u), units);
+    int rc = check_launch(fn, "tensor-core scoring");
+    if (rc != NOVA_SUCCESS) return rc;
     if (timed) cudaEventRecord(tc->g1, eng.stream);
-    // ---- merge, margin, exact re-score of near ties ----
+    return NOVA_SUCCESS;
+}
+
+// After the GEMM: merge the lists, apply the margin, re-score near ties
+// exactly, and list the rows left to the exact scan (count in eng.itemCount).
+int tc_finish(BackupEngine &eng, const char *fn) {
+    TcState *tc = eng.tc;
+    const TcState::Launch &L = tc->last;
+    const DevModel &md = eng.md;
+    int rc;
     const size_t rows = (size_t)tc->MZ * md.r;
     cudaMemsetAsync(tc->rowFlag, 0, rows * sizeof(unsigned), eng.stream);
     tc_merge_kernel<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, eng.stream>>>(
-        md, eng.suppLen, eng.proj_view(), eng.uniqJ, lists, sched.topk, tc->rPad, tc->a1, tc->d1, tc->a1raw, tc->scal,
-        tc->candV,
-        tc->candU,
-        tc->candX, eng.ustar, eng.jstar, tc->rowFlag, tc->rowCand, tc->scal + 3, tc->badModel);
+        md, eng.suppLen, eng.proj_view(), eng.uniqJ, L.lists, L.topk, tc->rPad, tc->a1, tc->d1, tc->a1raw, tc->scal,
+        tc->candV, tc->candU, tc->candX, eng.ustar, eng.jstar, tc->rowFlag, tc->rowCand, tc->scal + 3,
+        tc->badModel);
     if ((rc = check_launch(fn, "candidate merge")) != NOVA_SUCCESS) return rc;
     // The list can hold every row: it is sized m*z*r like the flags.
-    {
-        const unsigned nChunks = ceil_div(rows, kCompactChunk);
-        tc_compact_count_kernel<<<nChunks, 1024, 0, eng.stream>>>(tc->rowFlag, (unsigned)rows, tc->chunkCount);
-        if ((rc = check_launch(fn, "exact-scan list (count)")) != NOVA_SUCCESS) return rc;
-        tc_compact_scan_kernel<<<1, 1024, 0, eng.stream>>>(tc->chunkCount, nChunks, eng.itemCount);
-        if ((rc = check_launch(fn, "exact-scan list (scan)")) != NOVA_SUCCESS) return rc;
-        tc_compact_write_kernel<<<nChunks, 1024, 0, eng.stream>>>(tc->rowFlag, (unsigned)rows, tc->chunkCount,
-                                                                  tc->rowList);
-        if ((rc = check_launch(fn, "exact-scan list (write)")) != NOVA_SUCCESS) return rc;
+    const unsigned nChunks = ceil_div(rows, kCompactChunk);
+    tc_compact_count_kernel<<<nChunks, 1024, 0, eng.stream>>>(tc->rowFlag, (unsigned)rows, tc->chunkCount);
+    if ((rc = check_launch(fn, "exact-scan list (count)")) != NOVA_SUCCESS) return rc;
+    tc_compact_scan_kernel<<<1, 1024, 0, eng.stream>>>(tc->chunkCount, nChunks, eng.itemCount);
+    if ((rc = check_launch(fn, "exact-scan list (scan)")) != NOVA_SUCCESS) return rc;
+    tc_compact_write_kernel<<<nChunks, 1024, 0, eng.stream>>>(tc->rowFlag, (unsigned)rows, tc->chunkCount,
+                                                              tc->rowList);
+    return check_launch(fn, "exact-scan list (write)");
+}
+
+int tc_score_launch(BackupEngine &eng, const float *src, unsigned nU, bool timed, const char *fn) {
+    int rc;
+    if ((rc = tc_prepare(eng, src, nU, fn)) != NOVA_SUCCESS) return rc;
+    if ((rc = tc_gemm(eng, timed, fn)) != NOVA_SUCCESS) return rc;
+    return tc_finish(eng, fn);
+}
+
+// ---------------------------------------------------------------------------
+// Batched scoring: one persistent launch over the work units of many solvers
+// ---------------------------------------------------------------------------
+
+struct TcBatch {
+    struct Group {
+        unsigned topk = 0, totalUnits = 0, nModels = 0;
+        bool fp16 = true;
+        BatchModel *models = nullptr;   // device work table
+    };
+    std::vector<Group> groups;   // one per list length and operand form
+    int numSMs = 0;
+    ~TcBatch() {
+        for (auto &g : groups) cudaFree(g.models);
+    }
+};
+
+int tc_batch_create(BackupEngine *const *engs, unsigned count, TcBatch **out, const char *fn) {
+    std::unique_ptr<TcBatch> b(new TcBatch());
+    std::vector<std::vector<BatchModel>> host;
+    for (unsigned k = 0; k < count; k++) {
+        const BackupEngine &e = *engs[k];
+        const TcState *tc = e.tc;
+        if (tc == nullptr || tc->last.topk == 0) {
+            NOVA_ERR(fn, "A solver of the batch has no prepared tensor-core launch.");
+            return NOVA_ERROR_INVALID_DATA;
+        }
+        const TcState::Launch &L = tc->last;
+        if (L.topk != 8u && L.topk != 16u && L.topk != 32u) {
+            NOVA_ERR(fn, "Unsupported candidate-list length for a batched launch.");
+            return NOVA_ERROR_INVALID_DATA;
+        }
+        size_t gi = 0;
+        while (gi < b->groups.size() && (b->groups[gi].topk != L.topk || b->groups[gi].fp16 != L.fp16)) gi++;
+        if (gi == b->groups.size()) {
+            b->groups.emplace_back();
+            b->groups.back().topk = L.topk;
+            b->groups.back().fp16 = L.fp16;
+            host.emplace_back();
+        }
+        TcBatch::Group &g = b->groups[gi];
+        BatchModel m;
+        memset(&m, 0, sizeof(m));
+        m.tmA = tc->tmA;
+        m.tmB = L.tmB;
+        m.unitStart = g.totalUnits;
+        m.MZ = tc->MZ;
+        m.rPad = (unsigned)tc->rPad;
+        m.r = e.md.r;
+        m.mTiles = tc->mTiles;
+        m.nTiles = L.nTiles;
+        m.groups = L.groups;
+        m.nU = L.nU;
+        m.kBlocks = (unsigned)(tc->nPad / BK);
+        m.kSplit = L.kSplit;
+        m.a1 = tc->a1; m.d1 = tc->d1; m.scal = tc->scal;
+        m.candV = tc->candV; m.candU = tc->candU; m.candX = tc->candX;
+        const unsigned long long units = (unsigned long long)m.MZ * m.mTiles * m.groups;
+        if ((unsigned long long)g.totalUnits + units >= (1ull << 31)) {
+            NOVA_ERR(fn, "Too many work units for one batched launch.");
+            return NOVA_ERROR_INVALID_DATA;
+        }
+        g.totalUnits += (unsigned)units;
+        g.nModels++;
+        host[gi].push_back(m);
+        b->numSMs = tc->numSMs;
+    }
+    for (size_t gi = 0; gi < b->groups.size(); gi++) {
+        int rc;
+        if ((rc = dev_alloc(&b->groups[gi].models, host[gi].size(), fn, "the batch work table")) != NOVA_SUCCESS)
+            return rc;
+        if ((rc = h2d(b->groups[gi].models, host[gi].data(), host[gi].size() * sizeof(BatchModel), fn,
+                      "the batch work table")) != NOVA_SUCCESS)
+            return rc;
+    }
+    *out = b.release();
+    return NOVA_SUCCESS;
+}
+
+int tc_batch_gemm(TcBatch *b, cudaStream_t stream, const char *fn) {
+    for (const auto &g : b->groups) {
+        if (g.totalUnits == 0) continue;
+        const BatchUnits units{g.models, g.nModels, g.totalUnits};
+        const unsigned grid = std::min<unsigned>(g.totalUnits, (unsigned)b->numSMs);
+        CUtensorMap unused;
+        memset(&unused, 0, sizeof(unused));
+        auto kern = g.topk == 32u ? tc_score_gemm_kernel<32, BatchUnits>
+                    : (g.topk == 16u ? tc_score_gemm_kernel<16, BatchUnits> : tc_score_gemm_kernel<8, BatchUnits>);
+        kern<<<grid, GEMM_THREADS, GEMM_SMEM, stream>>>(unused, unused, make_idesc(g.fp16 ? 0u : 1u), units);
+        int rc = check_launch(fn, "batched tensor-core scoring");
+        if (rc != NOVA_SUCCESS) return rc;
     }
     return NOVA_SUCCESS;
 }
+
+void tc_batch_release(TcBatch *b) { delete b; }
 
 bool tc_schedule_fixed(const BackupEngine &eng) {
     // Fixed, and the operand is built for the solver's current mode (a
@@ -1251,6 +1463,14 @@ int tc_row_detail(const BackupEngine &eng, unsigned *candidates, unsigned *exact
         exactRows[i] += flag[row] ? 1u : 0u;
     }
     return NOVA_SUCCESS;
+}
+
+float tc_tuned_cost(const BackupEngine &eng) {
+    const TcState *tc = eng.tc;
+    if (tc == nullptr || tc->schedFixed < 0 || tc->schedFixed >= kTunedSchedules ||
+            tc->tuneNext < (unsigned)kTunedSchedules)
+        return -1.0f;
+    return tc->tuneCost[tc->schedFixed];
 }
 
 void tc_tune_feedback(BackupEngine &eng, float msScoring, unsigned nU) {

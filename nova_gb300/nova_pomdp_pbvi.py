@@ -88,3 +88,4 @@ _nova.pomdp_pbvi_execute_batched_gpu.argtypes = (ct.POINTER(_P), ct.POINTER(_G),
                                                  ct.POINTER(ct.POINTER(_npav.NovaPOMDPAlphaVectors)), ct.c_uint,
                                                  ct.c_uint, ct.c_uint)
 _nova.pomdp_pbvi_execute_batched_graph_gpu.argtypes = _nova.pomdp_pbvi_execute_batched_gpu.argtypes
+_nova.pomdp_pbvi_execute_batched_persistent_gpu.argtypes = _nova.pomdp_pbvi_execute_batched_gpu.argtypes

@@ -171,12 +171,15 @@ class POMDPPBVIGPU(npp.NovaPOMDPPBVIGPU):
         return "currentHorizon: %i\n\nnumThreads: %i\n\n" % (self.currentHorizon, self.numThreads)
 
 
-def solve_batched(pomdps, scoring=npp.SCORING_FP16, hostThreads=0, GammaInitials=None, graph=False):
+def solve_batched(pomdps, scoring=npp.SCORING_FP16, hostThreads=0, GammaInitials=None, graph=False,
+                  persistent=False):
     """ Solve independent POMDPs (each already copied to the device with
     initialize_gpu) with pomdp_pbvi_execute_batched_gpu (graph=True:
     pomdp_pbvi_execute_batched_graph_gpu, horizon loops replayed as CUDA
-    graphs); returns one POMDPAlphaVectors per POMDP, as each
-    POMDPPBVIGPU(p).solve() would. """
+    graphs; persistent=True: pomdp_pbvi_execute_batched_persistent_gpu,
+    lock-step backups with one persistent scoring launch for the batch);
+    returns one POMDPAlphaVectors per POMDP, as each POMDPPBVIGPU(p).solve()
+    would. """
     from . import pomdp_alpha_vectors as pav
     count = len(pomdps)
     solvers, bufs = [], []
@@ -194,7 +197,8 @@ def solve_batched(pomdps, scoring=npp.SCORING_FP16, hostThreads=0, GammaInitials
     A = (ct.POINTER(npp._npav.NovaPOMDPAlphaVectors) * count)(*[ct.cast(ct.pointer(a),
                                                                          ct.POINTER(npp._npav.NovaPOMDPAlphaVectors))
                                                                  for a in policies])
-    entry = npp._nova.pomdp_pbvi_execute_batched_graph_gpu if graph else npp._nova.pomdp_pbvi_execute_batched_gpu
+    entry = (npp._nova.pomdp_pbvi_execute_batched_persistent_gpu if persistent else
+             npp._nova.pomdp_pbvi_execute_batched_graph_gpu if graph else npp._nova.pomdp_pbvi_execute_batched_gpu)
     result = entry(P, G, A, count, int(scoring), int(hostThreads))
     _ = bufs
     if result != 0:

@@ -126,3 +126,29 @@ def test_graph_mode_survives_scoring_change():
     G, pi = orc.pbvi_solve(md)
     np.testing.assert_array_equal(bits(pol.gamma_array()), bits(G))
     np.testing.assert_array_equal(pol.pi_array(), pi)
+
+
+@pytest.mark.parametrize("mode", [npp.SCORING_FP16, npp.SCORING_BF16, npp.SCORING_EXACT])
+def test_persistent_batched_solves_equal_reference(mode):
+    """Lock-step batched solve (pomdp_pbvi_execute_batched_persistent_gpu): after
+    the warm-up that tunes each solver, every backup of the batch scores its
+    tensor-core solvers in one persistent launch from a device work table;
+    uneven n, r, m and z, one deep model (n = 2100: fixed schedule, the
+    state-contiguous table) and horizons long enough for many lock-step
+    backups. Every policy equals nova's."""
+    models = synth.batch_pomdps(count=9, seed=23, n_range=(16, 180), r_range=(40, 260), m_range=(2, 5),
+                                z_range=(2, 7), horizon=14)
+    deep = synth.random_pomdp(n=2100, m=2, z=3, ns=5, r=72, rz=6, gamma=0.95, horizon=9, seed=29)
+    deep["GammaInitial"] = np.random.default_rng(3).normal(-3.0, 1.0, size=(72, 2100)).astype(np.float32)
+    models.append(deep)
+    pomdps = []
+    for md in models:
+        p = POMDP.from_arrays(md)
+        p.initialize_gpu()
+        pomdps.append(p)
+    inits = [md["GammaInitial"] for md in models]
+    policies = solve_batched(pomdps, scoring=mode, hostThreads=4, GammaInitials=inits, persistent=True)
+    for md, pol in zip(models, policies):
+        G, pi = orc.pbvi_solve(md)
+        np.testing.assert_array_equal(bits(pol.gamma_array()), bits(G))
+        np.testing.assert_array_equal(pol.pi_array(), pi)
