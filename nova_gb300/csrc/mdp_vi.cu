@@ -168,10 +168,11 @@ static int launch_sweep(const MDP *mdp, const int *S, const float *T, const floa
                         ViTilePlan *plan, const char *fn) {
     if (plan != nullptr) {
         // The plan is built at the solver's first sweep from the model as it
-        // is then; the tiled sweep needs V 16-byte aligned for cp.async.
+        // is then; the tiled sweep needs V and R 16-byte aligned for its bulk
+        // copies.
         int rc = vi_plan_build(plan, mdp, S, T, stream, fn);
         if (rc != NOVA_SUCCESS) return rc;
-        if (plan->status == ViTilePlan::kTiled && ((uintptr_t)V % 16u) == 0u)
+        if (plan->status == ViTilePlan::kTiled && ((uintptr_t)V % 16u) == 0u && ((uintptr_t)R % 16u) == 0u)
             return vi_tiled_sweep(plan, mdp, R, V, Vp, pi, st, tol, early_exit, stream, fn);
     }
     const unsigned n = mdp->n, ns = mdp->ns, m = mdp->m;

@@ -7,13 +7,17 @@
 //
 //   * Source states are cut into blocks of Sb states (one CTA at a time per
 //     block; its m*Sb partial sums Q(s,a) live in shared memory, seeded with
-//     R(s,a)). Successor states are cut into tiles of Vt states. One warp of
-//     the CTA stages V tile after tile into a ring of shared-memory buffers
-//     with bulk copies (cp.async.bulk, completion on an mbarrier); the other
-//     31 warps each own a fixed range of the block's rows and add, tile
-//     after tile, the products of their rows' successors that fall in the
-//     tile. A warp releases a buffer (mbarrier arrive) when it is done with
-//     it, so warps run independently of each other, up to the ring's depth.
+//     R(s,a) by one bulk copy, the next block's R prefetched into L2).
+//     Successor states are cut into tiles of Vt states. One warp of the CTA
+//     stages V tile after tile into a ring of shared-memory buffers with bulk
+//     copies (cp.async.bulk, completion on an mbarrier), across block
+//     boundaries; the other kRowWarps warps each own a fixed range of the
+//     block's rows and add, tile after tile, the products of their rows'
+//     successors that fall in the tile. A warp releases a buffer (mbarrier
+//     arrive) when it is done with it, so warps run independently of each
+//     other, up to the ring's depth. At the end of a block the row warps
+//     meet at a named barrier, scan the actions (Vp, pi, residual) and
+//     release Q to the staging warp (mbarrier) for the next block's R.
 //   * A row's successors inside one tile form a run (consecutive in the
 //     row's list). The plan, built once per solver, stores for every slice
 //     (block, tile, warp) the 8-byte records {row << 16 | offset in tile,
@@ -26,8 +30,9 @@
 //     slices run in tile order, so every row receives its products in list
 //     order. Records stream from HBM exactly once per sweep (the same 8
 //     bytes per entry as S and T): each warp loads its next slice's records
-//     while it applies the current one, and the staging warp prefetches the
-//     records of the tile after that into L2 with one bulk prefetch.
+//     into registers while it applies the current one, and the staging warp
+//     prefetches the records of the tile kAhead tiles on into L2 with one
+//     bulk prefetch.
 //   * The single-record runs of a slice are dealt round-robin over the 32
 //     shared-memory banks of their partial sums (row mod 32), so a warp's 32
 //     runs of one step update distinct banks.
@@ -57,17 +62,19 @@ namespace nova_gb300 {
 
 namespace {
 
-constexpr unsigned kThreads = 1024;
+constexpr unsigned kThreads = 512;
 constexpr unsigned kWarps = kThreads / 32;
 constexpr unsigned kRowWarps = kWarps - 1;        // warps that apply records; the last one stages V
-constexpr int kSteps = 4;                         // groups of 32 records a warp holds per slice in registers
+constexpr int kSteps = 9;                         // groups of 32 records a warp holds per slice in registers
 constexpr unsigned kStages = 3;                   // V tiles in flight
+constexpr unsigned kAhead = 4;                    // tiles between a slice's L2 prefetch and its use
+constexpr unsigned kDepth = 1;                    // tiles between a slice's register load and its use
 constexpr unsigned kMaxRows = 65535u;             // rows of one block (16-bit row field)
 constexpr unsigned kMaxLevels = 31u;              // longest run of one row inside one tile
-constexpr unsigned kDefaultTileStates = 8192u;
+constexpr unsigned kDefaultTileStates = 9216u;
 constexpr unsigned long long kAutoMinEntries = 1ull << 22;
 constexpr long long kWaitCycles = 4000000000ll;   // ~2 s at 2 GHz
-constexpr size_t kBarrierBytes = 64;              // full[kStages], empty[kStages], abort flag
+constexpr size_t kBarrierBytes = 96;              // full[kStages], empty[kStages], qReady, qFree, two flags
 
 std::atomic<unsigned> g_mode{NOVA_VI_TILING_AUTO};
 std::atomic<unsigned> g_tile_states{0};
@@ -84,25 +91,41 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
+// try_wait, with a suspend-time hint when kHintNs > 0: a waiting thread may
+// sleep up to the hint until the phase completes instead of spinning on
+// issue slots.
+constexpr uint32_t kSuspendNs = 20000;
+template <uint32_t kHintNs>
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
+    if constexpr (kHintNs > 0) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity), "r"(kHintNs)
+            : "memory");
+    } else {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+    }
     return ok != 0;
 }
 // Bounded wait: false (after raising the abort flag and the error word) if
 // the phase does not complete in ~2 s, or if the CTA already aborted.
+template <uint32_t kHintNs = kSuspendNs>
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abortFlag,
                                           ViDeviceState *st) {
-    if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait<kHintNs>(bar, parity)) return true;
     const long long t0 = clock64();
     while (true) {
-        if (mbar_try_wait(bar, parity)) return true;
+        if (mbar_try_wait<kHintNs>(bar, parity)) return true;
         if (*abortFlag) return false;
         if (clock64() - t0 > kWaitCycles) {
             *abortFlag = 1;
@@ -125,16 +148,18 @@ __device__ __forceinline__ void prefetch_l2(const uint2 *rec, unsigned b, unsign
     const uintptr_t hi = (reinterpret_cast<uintptr_t>(rec + e) + 15) & ~(uintptr_t)15;
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((unsigned)(hi - lo)) : "memory");
 }
-
-constexpr uint2 kNoRecord = {0xFFFFFFFFu, 0u};
+// Bulk prefetch into L2 of `bytes` (a multiple of 16) at a 16-byte aligned p.
+__device__ __forceinline__ void prefetch_l2_bytes(const void *p, unsigned bytes) {
+    if (bytes) asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
 
 // What a lane holds for one slice: the slice's first record and run counts
 // (n0 runs, n1 of them with a second record, n2 with a third), the level-0
-// records of its runs lane + 32 i (i < kSteps) and the level-1 record of run
-// `lane`.
+// records of its runs lane + 32 i (i < kSteps, those that exist) and the
+// level-1 and level-2 records of run `lane` (when it has them).
 struct SliceRegs {
     uint2 r[kSteps];
-    uint2 r1;
+    uint2 r1, r2;
     unsigned start, n0, n1, n2;
 };
 // hdr = {first record, n0, n1, n2} of the slice.
@@ -143,78 +168,229 @@ __device__ __forceinline__ void load_slice(SliceRegs &g, const uint2 *__restrict
     g.n0 = hdr.y;
     g.n1 = hdr.z;
     g.n2 = hdr.w;
+    const uint2 *p = rec + hdr.x + lane;
+    const int c = (int)hdr.y - (int)lane;
 #pragma unroll
-    for (int i = 0; i < kSteps; i++) {
-        const unsigned j = lane + 32u * i;
-        g.r[i] = j < g.n0 ? __ldg(rec + g.start + j) : kNoRecord;
-    }
-    g.r1 = lane < g.n1 ? __ldg(rec + g.start + g.n0 + lane) : kNoRecord;
+    for (int i = 0; i < kSteps; i++)
+        if (c > 32 * i) g.r[i] = __ldg(p + 32 * i);
+    if (lane < hdr.z) g.r1 = __ldg(p + hdr.y);
+    if (lane < hdr.w) g.r2 = __ldg(p + hdr.y + hdr.z);
 }
 
 // part[row] += fl(gamma*T) * V[s'] for one record.
-__device__ __forceinline__ void apply_record(uint2 r, const float *vtile, unsigned tileLen, float *part,
-                                             unsigned rows) {
-    const unsigned row = r.x >> 16, off = r.x & 0xFFFFu;
-    if (row < rows && off < tileLen) part[row] = fadd(part[row], fmul(__uint_as_float(r.y), vtile[off]));
+__device__ __forceinline__ void apply_record(uint2 r, const float *vtile, float *part) {
+    part[r.x >> 16] = fadd(part[r.x >> 16], fmul(__uint_as_float(r.y), vtile[r.x & 0xFFFFu]));
 }
 
-// Records of run j from level 1 on (run j has at least two), in list order.
-// Only the rare runs of three or more records read further level counts.
-__device__ __forceinline__ void apply_long_run(const SliceRegs &g, unsigned j, uint2 first1,
-                                               const uint2 *__restrict__ rec, const unsigned *__restrict__ levelCnt,
-                                               unsigned L, unsigned slice, const float *vtile, unsigned tileLen,
-                                               float *part, unsigned rows) {
-    apply_record(first1, vtile, tileLen, part, rows);
-    if (j >= g.n2) return;
-    unsigned base = g.n0 + g.n1;
-    apply_record(__ldg(rec + g.start + base + j), vtile, tileLen, part, rows);
-    base += g.n2;
+// Records of run j from level 3 on (run j has at least three). Only the rare
+// runs of four or more records read level counts.
+__device__ __forceinline__ void apply_levels_from3(const SliceRegs &g, unsigned j, const uint2 *__restrict__ rec,
+                                                   const unsigned *__restrict__ levelCnt, unsigned L,
+                                                   unsigned slice, const float *vtile, float *part) {
+    unsigned base = g.n0 + g.n1 + g.n2;
     for (unsigned lv = 3; lv < L; lv++) {
         const unsigned nq = __ldg(levelCnt + (size_t)slice * L + lv);
         if (j >= nq) break;
-        apply_record(__ldg(rec + g.start + base + j), vtile, tileLen, part, rows);
+        apply_record(__ldg(rec + g.start + base + j), vtile, part);
         base += nq;
     }
 }
 
-// One slice: the level-0 record of every run, then the further records of
-// the long runs (runs 0 .. n1-1), each in list order after its level-0
-// record (the same lane applies both; no other run of the slice has that
-// row).
+// One slice. The level-0 records a lane holds belong to distinct runs, hence
+// distinct rows, and the level-1 and level-2 records of run `lane` to the
+// row of its level-0 record r[0]: all their shared-memory reads are issued
+// before any write, and the row of r[0] takes its two or three products in
+// list order in registers. Then, each in list order after the records
+// before it: the level-0 records of runs past 32 kSteps, the further records
+// of run `lane`, and the long runs past 32 (rare; records read from L2).
+// The plan guarantees every record's row and offset lie inside the block's
+// rows and the tile.
 __device__ __forceinline__ void apply_slice(const SliceRegs &g, const uint2 *__restrict__ rec,
                                             const unsigned *__restrict__ levelCnt, unsigned L, unsigned slice,
-                                            const float *vtile, unsigned tileLen, float *part, unsigned rows,
-                                            unsigned lane) {
+                                            const float *vtile, float *part, unsigned lane) {
+    const int c = (int)g.n0 - (int)lane;
+    const bool h1 = lane < g.n1, h2 = lane < g.n2;
+    float q[kSteps], v[kSteps], v1 = 0.0f, v2 = 0.0f;
+#pragma unroll
+    for (int i = 0; i < kSteps; i++) {
+        q[i] = v[i] = 0.0f;
+        if (c > 32 * i) {
+            v[i] = vtile[g.r[i].x & 0xFFFFu];
+            q[i] = part[g.r[i].x >> 16];
+        }
+    }
+    if (h1) v1 = vtile[g.r1.x & 0xFFFFu];
+    if (h2) v2 = vtile[g.r2.x & 0xFFFFu];
 #pragma unroll
     for (int i = 0; i < kSteps; i++)
-        if (lane + 32u * i < g.n0) apply_record(g.r[i], vtile, tileLen, part, rows);
-    for (unsigned j = lane + 32u * kSteps; j < g.n0; j += 32u)
-        apply_record(__ldg(rec + g.start + j), vtile, tileLen, part, rows);
-    if (lane < g.n1) apply_long_run(g, lane, g.r1, rec, levelCnt, L, slice, vtile, tileLen, part, rows);
-    for (unsigned j = lane + 32u; j < g.n1; j += 32u)
-        apply_long_run(g, j, __ldg(rec + g.start + g.n0 + j), rec, levelCnt, L, slice, vtile, tileLen, part, rows);
+        if (c > 32 * i) q[i] = fadd(q[i], fmul(__uint_as_float(g.r[i].y), v[i]));
+    if (h1) q[0] = fadd(q[0], fmul(__uint_as_float(g.r1.y), v1));
+    if (h2) q[0] = fadd(q[0], fmul(__uint_as_float(g.r2.y), v2));
+#pragma unroll
+    for (int i = 0; i < kSteps; i++)
+        if (c > 32 * i) part[g.r[i].x >> 16] = q[i];
+    if (c > 32 * kSteps)
+        for (unsigned j = lane + 32u * kSteps; j < g.n0; j += 32u) apply_record(__ldg(rec + g.start + j), vtile, part);
+    if (h2 && L > 3) apply_levels_from3(g, lane, rec, levelCnt, L, slice, vtile, part);
+    if (g.n1 > 32u)
+        for (unsigned j = lane + 32u; j < g.n1; j += 32u) {
+            apply_record(__ldg(rec + g.start + g.n0 + j), vtile, part);
+            if (j < g.n2) {
+                apply_record(__ldg(rec + g.start + g.n0 + g.n1 + j), vtile, part);
+                apply_levels_from3(g, j, rec, levelCnt, L, slice, vtile, part);
+            }
+        }
 }
 
-// One tile of a row warp: load the next slice (and the header after it),
-// wait for the V tile, apply the current slice, release the buffer.
-__device__ __forceinline__ bool row_warp_tile(unsigned t, unsigned T, const SliceRegs &cur, SliceRegs &nxt,
+// One tile of a row warp: load the slice kDepth tiles ahead (and the header
+// after it), wait for the V tile, apply the current slice, release the
+// buffer.
+__device__ __forceinline__ bool row_warp_tile(unsigned t, unsigned T, const SliceRegs &cur, SliceRegs &ahead,
                                               uint4 &hNext, unsigned sl0, const uint2 *__restrict__ rec,
                                               const uint4 *__restrict__ sliceHdr,
                                               const unsigned *__restrict__ levelCnt, unsigned L, const float *vt,
-                                              unsigned Vt, unsigned n, float *part, unsigned rows, uint64_t *bars,
-                                              unsigned &sg, unsigned &ph, volatile int *abortFlag,
-                                              ViDeviceState *st, unsigned lane) {
-    if (t + 1 < T) {
-        load_slice(nxt, rec, hNext, lane);
-        hNext = t + 2 < T ? __ldg(sliceHdr + sl0 + (t + 2) * kRowWarps) : make_uint4(0u, 0u, 0u, 0u);
+                                              unsigned Vt, float *part, uint64_t *bars, unsigned &sg, unsigned &ph,
+                                              volatile int *abortFlag, ViDeviceState *st, unsigned lane) {
+    if (t + kDepth < T) {
+        load_slice(ahead, rec, hNext, lane);
+        hNext = t + kDepth + 1 < T ? __ldg(sliceHdr + sl0 + (t + kDepth + 1) * kRowWarps)
+                                   : make_uint4(0u, 0u, 0u, 0u);
     }
     if (!mbar_wait(smem_addr(&bars[sg]), ph, abortFlag, st)) return false;
-    apply_slice(cur, rec, levelCnt, L, sl0 + t * kRowWarps, vt + (size_t)sg * Vt, min(Vt, n - t * Vt), part, rows,
-                lane);
+    apply_slice(cur, rec, levelCnt, L, sl0 + t * kRowWarps, vt + (size_t)sg * Vt, part, lane);
     __syncwarp();
     if (lane == 0) mbar_arrive(smem_addr(&bars[kStages + sg]));
     if (++sg == kStages) { sg = 0; ph ^= 1u; }
     return true;
+}
+
+// A row warp's pass over the block's T tiles. Slice (blk, t) of the warp is
+// sl0 + t * kRowWarps. The records of slice t + kDepth are loaded while
+// slice t is applied: kDepth + 1 register sets rotate roles, indexed by
+// compile-time constants in the unrolled loop, so nothing is copied.
+__device__ __forceinline__ bool row_warp_pass(unsigned T, unsigned sl0, const uint2 *__restrict__ rec,
+                                              const uint4 *__restrict__ sliceHdr,
+                                              const unsigned *__restrict__ levelCnt, unsigned L, const float *vt,
+                                              unsigned Vt, float *part, uint64_t *bars, unsigned &sg, unsigned &ph,
+                                              volatile int *abortFlag, ViDeviceState *st, unsigned lane) {
+    SliceRegs g[kDepth + 1];
+#pragma unroll
+    for (unsigned u = 0; u <= kDepth; u++) g[u] = SliceRegs{};
+#pragma unroll
+    for (unsigned u = 0; u < kDepth; u++)
+        if (u < T) load_slice(g[u], rec, __ldg(sliceHdr + sl0 + u * kRowWarps), lane);
+    uint4 hNext = kDepth < T ? __ldg(sliceHdr + sl0 + kDepth * kRowWarps) : make_uint4(0u, 0u, 0u, 0u);
+    for (unsigned t = 0; t < T; t += kDepth + 1) {
+#pragma unroll
+        for (unsigned u = 0; u <= kDepth; u++) {
+            if (t + u >= T) return true;
+            if (!row_warp_tile(t + u, T, g[u], g[(u + kDepth) % (kDepth + 1)], hNext, sl0, rec, sliceHdr, levelCnt,
+                               L, vt, Vt, part, bars, sg, ph, abortFlag, st, lane))
+                return false;
+        }
+    }
+    return true;
+}
+
+// Action scan of state i of the block for m = M, a power of two up to 32:
+// the thread reads Q(i, .) starting at action rot, so that the 32 lanes of a
+// warp (consecutive states) hit 32 distinct banks, rotates the values back
+// into action order in registers (log2 M select stages), and scans them as
+// mdp_vi_cpu.cpp:55-58 does (first strict maximum).
+template <unsigned M>
+__device__ __forceinline__ void scan_state_pow2(const float *part, unsigned i, float &best, unsigned &besta) {
+    constexpr unsigned LG = M >= 32 ? 5 : M >= 16 ? 4 : M >= 8 ? 3 : M >= 4 ? 2 : M >= 2 ? 1 : 0;
+    const unsigned rot = (i >> (5 - LG)) & (M - 1);
+    const float *qv = part + (size_t)i * M;
+    float q[M];
+#pragma unroll
+    for (unsigned k = 0; k < M; k++) q[k] = qv[(k + rot) & (M - 1)];  // q[k] = Q(i, k + rot)
+#pragma unroll
+    for (int b = 0; b < (int)LG; b++) {
+        // Rotate right by 2^b when bit b of rot is set.
+        const bool on = (rot >> b) & 1u;
+        float r[M];
+#pragma unroll
+        for (unsigned k = 0; k < M; k++) r[k] = on ? q[(k + M - (1u << b)) & (M - 1)] : q[k];
+#pragma unroll
+        for (unsigned k = 0; k < M; k++) q[k] = r[k];
+    }
+    best = q[0];
+    besta = 0;
+#pragma unroll
+    for (unsigned a = 1; a < M; a++)
+        if (q[a] > best) { best = q[a]; besta = a; }
+}
+
+// Largest |Vp - V| over a thread's states, as (Vp, V) of the largest: the
+// rounded float difference orders the exact ones except on ties, which are
+// settled in double (a zero difference is exact). NaN differences are
+// skipped, as fmax skips them.
+struct ResidualMax {
+    float d = 0.0f, a = 0.0f, b = 0.0f;
+    __device__ __forceinline__ void add(float x, float y) {
+        const float e = fabsf(__fsub_rn(x, y));
+        if (e > d || (e == d && e != 0.0f && fabs((double)x - (double)y) > fabs((double)a - (double)b))) {
+            d = e;
+            a = x;
+            b = y;
+        }
+    }
+    __device__ __forceinline__ double value() const { return fabs((double)a - (double)b); }
+};
+
+// Action scan of the block's nsb states by the row-warp threads (rt of
+// kRowWarps * 32, one state each in turn): Vp, pi and the largest |Vp - V|.
+// The V of kBatch states is loaded before they are scanned.
+template <unsigned M>
+__device__ __forceinline__ double scan_block_m(const float *part, unsigned nsb, unsigned m, unsigned s0,
+                                               const float *__restrict__ V, float *__restrict__ Vp,
+                                               unsigned *__restrict__ pi, unsigned rt, double local) {
+    constexpr unsigned kStride = kRowWarps * 32, kBatch = M >= 32 ? 2 : M >= 16 ? 4 : 8;
+    ResidualMax res;
+    for (unsigned i0 = rt; i0 < nsb; i0 += kStride * kBatch) {
+        float vOld[kBatch];
+#pragma unroll
+        for (unsigned b = 0; b < kBatch; b++) {
+            const unsigned i = i0 + b * kStride;
+            vOld[b] = i < nsb ? __ldg(V + s0 + i) : 0.0f;
+        }
+#pragma unroll
+        for (unsigned b = 0; b < kBatch; b++) {
+            const unsigned i = i0 + b * kStride;
+            if (i >= nsb) break;
+            float best;
+            unsigned besta;
+            if constexpr (M != 0) {
+                scan_state_pow2<M>(part, i, best, besta);
+            } else {
+                // Any other m: mdp_vi_cpu.cpp:55-58 as written (lowest action on ties).
+                const float *qv = part + (size_t)i * m;
+                best = qv[0];
+                besta = 0;
+                for (unsigned a = 1; a < m; a++)
+                    if (qv[a] > best) { best = qv[a]; besta = a; }
+            }
+            Vp[s0 + i] = best;
+            pi[s0 + i] = besta;
+            res.add(best, vOld[b]);
+        }
+    }
+    return fmax(local, res.value());
+}
+
+__device__ __forceinline__ double scan_block(const float *part, unsigned nsb, unsigned m, unsigned s0,
+                                             const float *__restrict__ V, float *__restrict__ Vp,
+                                             unsigned *__restrict__ pi, unsigned rt, double local) {
+    switch (m) {
+        case 1: return scan_block_m<1>(part, nsb, m, s0, V, Vp, pi, rt, local);
+        case 2: return scan_block_m<2>(part, nsb, m, s0, V, Vp, pi, rt, local);
+        case 4: return scan_block_m<4>(part, nsb, m, s0, V, Vp, pi, rt, local);
+        case 8: return scan_block_m<8>(part, nsb, m, s0, V, Vp, pi, rt, local);
+        case 16: return scan_block_m<16>(part, nsb, m, s0, V, Vp, pi, rt, local);
+        case 32: return scan_block_m<32>(part, nsb, m, s0, V, Vp, pi, rt, local);
+        default: return scan_block_m<0>(part, nsb, m, s0, V, Vp, pi, rt, local);
+    }
 }
 
 __global__ void __launch_bounds__(kThreads, 1) bellman_tiled_kernel(
@@ -228,36 +404,63 @@ __global__ void __launch_bounds__(kThreads, 1) bellman_tiled_kernel(
     float *part = vt + (size_t)kStages * Vt;                                  // [Sb*m]
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + (((size_t)kStages * Vt + (size_t)Sb * m) * 4 + 15) /
                                                              16 * 16);
-    volatile int *abortFlag = reinterpret_cast<volatile int *>(bars + 2 * kStages);
+    // bars: full[kStages], empty[kStages], qReady, qFree; then two flags.
+    const uint32_t qReady = smem_addr(&bars[2 * kStages]), qFree = smem_addr(&bars[2 * kStages + 1]);
+    volatile int *abortFlag = reinterpret_cast<volatile int *>(bars + 2 * kStages + 2);
+    volatile int *rowAbort = abortFlag + 1;
     const unsigned tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         for (unsigned s = 0; s < kStages; s++) {
             mbar_init(smem_addr(&bars[s]), 1);                 // full: the staging lane's arrival + bytes
             mbar_init(smem_addr(&bars[kStages + s]), kRowWarps);  // empty: one arrival per row warp
         }
+        mbar_init(qReady, 1);          // the block's R in Q: the staging lane's arrival + bytes
+        mbar_init(qFree, kRowWarps);   // the block's scan done: one arrival per row warp
         *abortFlag = 0;
+        *rowAbort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    unsigned stage = 0, phase = 0;   // ring position, advanced identically by every warp
-    unsigned lastPar[kStages];       // staging lane: parity of the last copy issued per stage (2: none)
-#pragma unroll
-    for (unsigned s = 0; s < kStages; s++) lastPar[s] = 2u;
     double local = 0.0;
-    for (unsigned blk = blockIdx.x; blk < blocks && !*abortFlag; blk += gridDim.x) {
-        const unsigned s0 = blk * Sb;
-        const unsigned nsb = min(Sb, n - s0);
-        const unsigned rows = nsb * m;
-        for (unsigned i = tid; i < rows; i += blockDim.x) part[i] = __ldg(R + (size_t)s0 * m + i);
-        __syncthreads();
-        const size_t c0 = (size_t)blk * T;
-        if (warp == kRowWarps) {
-            // ---- staging warp: V tiles into the ring, records into L2 ----
-            if (lane == 0) {
-                prefetch_l2(rec, __ldg(sliceStart + c0 * kRowWarps), __ldg(sliceStart + (c0 + min(T, 2u)) * kRowWarps));
-                unsigned sg = stage, ph = phase;
-                for (unsigned t = 0; t < T; t++) {
-                    if (!mbar_wait(smem_addr(&bars[kStages + sg]), ph ^ 1u, abortFlag, st)) break;
+    if (warp == kRowWarps) {
+        // ---- staging warp (lane 0): per block, R into Q once the previous
+        // block's scan released it (one bulk copy; the next block's R is
+        // prefetched into L2), and V tile after tile into the ring, which
+        // runs on across block boundaries; records into L2 kAhead tiles
+        // ahead of the row warps.
+        if (lane == 0) {
+            unsigned lastPar[kStages];  // parity of the last copy issued per stage (2: none)
+#pragma unroll
+            for (unsigned s = 0; s < kStages; s++) lastPar[s] = 2u;
+            unsigned rLastPar = 2u;     // parity of the last R copy issued (2: none)
+            unsigned sg = 0, ph = 0, it = 0;
+            bool ok = true;
+            for (unsigned blk = blockIdx.x; ok && blk < blocks; blk += gridDim.x, it++) {
+                const unsigned s0 = blk * Sb, nsb = min(Sb, n - s0), rows = nsb * m;
+                const size_t c0 = (size_t)blk * T;
+                if (it == 0)
+                    prefetch_l2(rec, __ldg(sliceStart + c0 * kRowWarps),
+                                __ldg(sliceStart + (c0 + min(T, kAhead)) * kRowWarps));
+                // R goes in after the first kStages tiles of the block were
+                // issued (their slots were freed by the previous block's
+                // last tiles, before its scan).
+                for (unsigned t = 0; t <= T; t++) {
+                    if (t == min(T, kStages)) {
+                        if (it > 0 && !mbar_wait<0>(qFree, (it - 1) & 1u, abortFlag, st)) { ok = false; break; }
+                        const float *src = R + (size_t)s0 * m;
+                        const unsigned body = rows & ~3u;
+                        for (unsigned k = body; k < rows; k++) part[k] = __ldg(src + k);
+                        mbar_expect_tx(qReady, body * 4u);
+                        if (body) bulk_copy(smem_addr(part), src, body * 4u, qReady);
+                        rLastPar = it & 1u;
+                        if (blk + gridDim.x < blocks) {
+                            const unsigned nb = blk + gridDim.x;
+                            const unsigned nrows = min(Sb, n - nb * Sb) * m;
+                            prefetch_l2_bytes(R + (size_t)nb * Sb * m, (nrows * 4u) & ~15u);
+                        }
+                    }
+                    if (t == T) break;
+                    if (!mbar_wait(smem_addr(&bars[kStages + sg]), ph ^ 1u, abortFlag, st)) { ok = false; break; }
                     const unsigned base = t * Vt, cnt = min(Vt, n - base);
                     const unsigned body = cnt & ~3u;
                     float *dst = vt + (size_t)sg * Vt;
@@ -266,61 +469,55 @@ __global__ void __launch_bounds__(kThreads, 1) bellman_tiled_kernel(
                     mbar_expect_tx(fb, body * 4u);
                     if (body) bulk_copy(smem_addr(dst), V + base, body * 4u, fb);
                     lastPar[sg] = ph;
-                    if (t + 2 < T)
-                        prefetch_l2(rec, __ldg(sliceStart + (c0 + t + 2) * kRowWarps),
-                                    __ldg(sliceStart + (c0 + t + 3) * kRowWarps));
+                    {
+                        const unsigned ahead = t + kAhead;
+                        size_t pc = ~(size_t)0;
+                        if (ahead < T) pc = c0 + ahead;
+                        else if (blk + gridDim.x < blocks && ahead - T < T) pc = (size_t)(blk + gridDim.x) * T + (ahead - T);
+                        if (pc != ~(size_t)0)
+                            prefetch_l2(rec, __ldg(sliceStart + pc * kRowWarps), __ldg(sliceStart + (pc + 1) * kRowWarps));
+                    }
                     if (++sg == kStages) { sg = 0; ph ^= 1u; }
                 }
             }
-        } else {
-            // ---- row warps ----
-            // Slice (blk, t) of this warp is sl0 + t * kRowWarps. Records of
-            // slice t+1 are loaded while slice t is applied; the two register
-            // sets alternate roles, so nothing is copied between tiles.
-            const unsigned sl0 = (unsigned)(c0 * kRowWarps) + warp;
-            SliceRegs ga, gb;
-            load_slice(ga, rec, __ldg(sliceHdr + sl0), lane);
-            uint4 hNext = T > 1 ? __ldg(sliceHdr + sl0 + kRowWarps) : make_uint4(0u, 0u, 0u, 0u);
-            unsigned sg = stage, ph = phase;
-            for (unsigned t = 0; t < T; t += 2) {
-                if (!row_warp_tile(t, T, ga, gb, hNext, sl0, rec, sliceHdr, levelCnt, L, vt, Vt, n, part, rows, bars,
-                                   sg, ph, abortFlag, st, lane))
-                    break;
-                if (t + 1 < T && !row_warp_tile(t + 1, T, gb, ga, hNext, sl0, rec, sliceHdr, levelCnt, L, vt, Vt, n,
-                                                part, rows, bars, sg, ph, abortFlag, st, lane))
-                    break;
+            if (*abortFlag) {
+                // Let the copies in flight land before the CTA exits
+                // (bounded): the last issue on each barrier completes the
+                // phase of the parity recorded.
+                for (unsigned s = 0; s < kStages; s++) {
+                    if (lastPar[s] > 1u) continue;
+                    const long long t0 = clock64();
+                    while (!mbar_try_wait<0>(smem_addr(&bars[s]), lastPar[s]) && clock64() - t0 < kWaitCycles) {
+                    }
+                }
+                if (rLastPar <= 1u) {
+                    const long long t0 = clock64();
+                    while (!mbar_try_wait<0>(qReady, rLastPar) && clock64() - t0 < kWaitCycles) {
+                    }
+                }
             }
         }
-        // Every warp advances the ring by the block's T tiles.
-        {
-            const unsigned adv = stage + T;
-            phase ^= (adv / kStages) & 1u;
-            stage = adv % kStages;
-        }
-        __syncthreads();
-        if (*abortFlag) break;
-        // Action scan of mdp_vi_cpu.cpp:55-58 (lowest action on ties).
-        for (unsigned i = tid; i < nsb; i += blockDim.x) {
-            const float *qv = part + (size_t)i * m;
-            float best = qv[0];
-            unsigned besta = 0;
-            for (unsigned a = 1; a < m; a++)
-                if (qv[a] > best) { best = qv[a]; besta = a; }
-            const unsigned s = s0 + i;
-            Vp[s] = best;
-            pi[s] = besta;
-            local = fmax(local, fabs((double)best - (double)__ldg(V + s)));
-        }
-        __syncthreads();
-    }
-    if (*abortFlag && warp == kRowWarps && lane == 0) {
-        // Let the copies in flight land before the CTA exits (bounded): the
-        // last issue on each stage completes the phase of parity lastPar.
-        for (unsigned s = 0; s < kStages; s++) {
-            if (lastPar[s] > 1u) continue;
-            const long long t0 = clock64();
-            while (!mbar_try_wait(smem_addr(&bars[s]), lastPar[s]) && clock64() - t0 < kWaitCycles) {
-            }
+    } else {
+        // ---- row warps ----
+        // Per block: wait for R in Q, apply the block's slices tile after
+        // tile, meet at a named barrier, scan, release Q. The decision to
+        // stop is taken from rowAbort, which only row warps write and only
+        // before the barrier, so every row warp takes it alike.
+        unsigned sg = 0, ph = 0, it = 0;
+        for (unsigned blk = blockIdx.x; blk < blocks; blk += gridDim.x, it++) {
+            const unsigned s0 = blk * Sb, nsb = min(Sb, n - s0);
+            bool ok = mbar_wait<0>(qReady, it & 1u, abortFlag, st);
+            if (ok)
+                ok = row_warp_pass(T, (unsigned)((size_t)blk * T * kRowWarps) + warp, rec, sliceHdr, levelCnt, L, vt,
+                                   Vt, part, bars, sg, ph, abortFlag, st, lane);
+            if (!ok && lane == 0) *rowAbort = 1;
+            asm volatile("bar.sync 1, %0;" ::"r"(kRowWarps * 32) : "memory");
+            if (*rowAbort) break;
+            local = scan_block(part, nsb, m, s0, V, Vp, pi, warp * 32 + lane, local);
+            // Q is next written by the bulk copy (async proxy).
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(qFree);
         }
     }
     __syncthreads();
@@ -623,7 +820,12 @@ int vi_plan_build(ViTilePlan *plan, const MDP *mdp, const int *S, const float *T
     const unsigned SbMax = rowsMax / m;
     if (SbMax == 0) return NOVA_SUCCESS;
     const unsigned waves = ceil_div(n, (unsigned long long)sms * SbMax);
-    const unsigned Sb = ceil_div(n, (unsigned long long)sms * waves);
+    // Sb * m a multiple of 4, so that every block's R starts 16-byte aligned
+    // (one bulk copy per block).
+    const unsigned qAlign = (m % 4u == 0u) ? 1u : (m % 2u == 0u) ? 2u : 4u;
+    unsigned Sb = (unsigned)round_up(ceil_div(n, (unsigned long long)sms * waves), qAlign);
+    if (Sb > SbMax) Sb = SbMax / qAlign * qAlign;
+    if (Sb == 0) return NOVA_SUCCESS;
     const unsigned blocks = ceil_div(n, Sb);
     const size_t smemBytes = round_up((size_t)kStages * Vt * 4 + (size_t)Sb * m * 4, 16) + kBarrierBytes;
 

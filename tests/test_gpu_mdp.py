@@ -212,6 +212,29 @@ def test_unsorted_rows_keep_gather_sweep(tiling):
     np.testing.assert_array_equal(pol.pi_array(), pi)
 
 
+@pytest.mark.parametrize("n,m_actions,ns,tile", [(60000, 32, 4, 16384), (300000, 5, 6, 16384),
+                                                 (100000, 16, 5, 16384), (500000, 3, 4, 16384),
+                                                 (250000, 24, 4, 8192), (30000, 64, 3, 16384)])
+def test_tiled_equals_gather_multi_wave(tiling, n, m_actions, ns, tile):
+    """Models large enough for several source blocks per CTA at this tile
+    size (more than one block of Q per SM's shared memory), so every CTA
+    carries its V ring, R copies and scans across block boundaries; m covers
+    the warp scan (powers of two up to 32) and the per-thread scan (5, 3, 24,
+    64), and n = 30000 has fewer tiles than ring stages. Six tiled sweeps
+    equal six per-row sweeps bit for bit."""
+    md = synth.random_mdp(n=n, m=m_actions, ns=ns, gamma=0.95, horizon=6, seed=n + m_actions)
+    m = MDP.from_arrays(md)
+    m.initialize_gpu()
+    out = {}
+    for mode in (nmvi.TILING_ALWAYS, nmvi.TILING_NEVER):
+        tiling.set_tiling(mode, tile)
+        pol = MDPValueIterationGPU(m, Vinitial=np.zeros(md["n"], np.float32)).solve()
+        out[mode] = (pol.V_array().copy(), pol.pi_array().copy(), tiling.tiling_status())
+    assert out[nmvi.TILING_ALWAYS][2] == 1 and out[nmvi.TILING_NEVER][2] == 2
+    np.testing.assert_array_equal(bits(out[nmvi.TILING_ALWAYS][0]), bits(out[nmvi.TILING_NEVER][0]))
+    np.testing.assert_array_equal(out[nmvi.TILING_ALWAYS][1], out[nmvi.TILING_NEVER][1])
+
+
 def test_tiled_equals_gather_at_full_size(tiling):
     """n = 2^20, m = 8, ns = 16: the tiled sweep (chosen automatically) and the
     per-row sweep give the same bits after 12 sweeps, and the first sweep
