@@ -20,8 +20,8 @@
 //     release Q to the staging warp (mbarrier) for the next block's R.
 //   * A row's successors inside one tile form a run (consecutive in the
 //     row's list). The plan, built once per solver, stores for every slice
-//     (block, tile, warp) the 8-byte records {row << 16 | offset in tile,
-//     fl(gamma * T)} (the reference's first rounding, done once) of its
+//     (block, tile, warp) the 8-byte records {row << 16 | byte offset in
+//     tile, fl(gamma * T)} (the reference's first rounding, done once) of its
 //     runs, level after level: level q holds the q-th record of every run
 //     with more than q records, runs ordered by length (longest first), so
 //     run j has its level-q record at position j of level q. Lane l of the
@@ -177,9 +177,14 @@ __device__ __forceinline__ void load_slice(SliceRegs &g, const uint2 *__restrict
     if (lane < hdr.w) g.r2 = __ldg(p + hdr.y + hdr.z);
 }
 
+// V[s'] of a record: its low half is the byte offset of s' in the tile.
+__device__ __forceinline__ float tile_value(const float *vtile, unsigned x) {
+    return *reinterpret_cast<const float *>(reinterpret_cast<const char *>(vtile) + (x & 0xFFFFu));
+}
+
 // part[row] += fl(gamma*T) * V[s'] for one record.
 __device__ __forceinline__ void apply_record(uint2 r, const float *vtile, float *part) {
-    part[r.x >> 16] = fadd(part[r.x >> 16], fmul(__uint_as_float(r.y), vtile[r.x & 0xFFFFu]));
+    part[r.x >> 16] = fadd(part[r.x >> 16], fmul(__uint_as_float(r.y), tile_value(vtile, r.x)));
 }
 
 // Records of run j from level 3 on (run j has at least three). Only the rare
@@ -215,12 +220,12 @@ __device__ __forceinline__ void apply_slice(const SliceRegs &g, const uint2 *__r
     for (int i = 0; i < kSteps; i++) {
         q[i] = v[i] = 0.0f;
         if (c > 32 * i) {
-            v[i] = vtile[g.r[i].x & 0xFFFFu];
+            v[i] = tile_value(vtile, g.r[i].x);
             q[i] = part[g.r[i].x >> 16];
         }
     }
-    if (h1) v1 = vtile[g.r1.x & 0xFFFFu];
-    if (h2) v2 = vtile[g.r2.x & 0xFFFFu];
+    if (h1) v1 = tile_value(vtile, g.r1.x);
+    if (h2) v2 = tile_value(vtile, g.r2.x);
 #pragma unroll
     for (int i = 0; i < kSteps; i++)
         if (c > 32 * i) q[i] = fadd(q[i], fmul(__uint_as_float(g.r[i].y), v[i]));
@@ -657,7 +662,7 @@ __global__ void vi_plan_fill_kernel(PlanGeometry g, const int *__restrict__ S, c
         unsigned base = sliceStart[sl];
         for (unsigned q = 0; q < len; q++) {
             const unsigned sp = (unsigned)Sr[l0 + q];
-            rec[base + j] = make_uint2((rowLocal << 16) | (sp - t * g.Vt), __float_as_uint(fmul(g.gamma, Tr[l0 + q])));
+            rec[base + j] = make_uint2((rowLocal << 16) | ((sp - t * g.Vt) * 4u), __float_as_uint(fmul(g.gamma, Tr[l0 + q])));
             base += levelCnt[sl * g.L + q];
         }
     });
@@ -967,6 +972,7 @@ int vi_state_error(ViDeviceState *st, const char *fn) {
 extern "C" int mdp_vi_set_tiling_gpu(unsigned int mode, unsigned int tileStates) {
     if (mode > NOVA_VI_TILING_NEVER ||
             (tileStates != 0 && (tileStates % 4 != 0 || tileStates < 64 || tileStates > 16384))) {
+        // (A record's byte offset in its tile, below 4 * 16384, fits its 16-bit field.)
         NOVA_ERR("mdp_vi_set_tiling_gpu", "Invalid arguments.");
         return NOVA_ERROR_INVALID_DATA;
     }

@@ -64,7 +64,7 @@ struct ViTilePlan {
     unsigned levels = 0;        // longest run of one row's successors inside one tile
     unsigned grid = 0;          // resident CTAs
     size_t smemBytes = 0;
-    uint2 *rec = nullptr;          // [entries + 2] {row << 16 | offset in tile, bits of fl(gamma * T)}
+    uint2 *rec = nullptr;          // [entries + 2] {row << 16 | byte offset in tile, bits of fl(gamma * T)}
     unsigned *sliceStart = nullptr;  // [blocks*tiles*rowWarps + 1] first record of each (block, tile, warp) slice
     uint4 *sliceHdr = nullptr;       // [slices] {first record, runs, runs with 2+ records, runs with 3+}
     unsigned *levelCnt = nullptr;    // [slices][levels] runs of each slice with more than q records
