@@ -40,6 +40,25 @@ NOVA_NS_BEGIN
  * All modes give bit-identical results. */
 NOVA_API int pomdp_pbvi_set_scoring_gpu(POMDPPBVIGPU *pbvi, unsigned int mode);
 
+/* Projection table of a GPU PBVI solver (new in nova-gb300; replaces no
+ * reference entry point). The table holds fl(gamma * sum_l C1 * alpha(S))
+ * for every (action, observation, state, unique alpha): 4*m*z*n*|Gamma|
+ * bytes (68.7 GB at n = 4096, m = 16, z = 32, |Gamma| = 8192). Exact scores
+ * of the tensor-core candidates, the exact scan and the assembly read it.
+ *  NOVA_PBVI_TABLE_AUTO (default): built when it fits in free device memory
+ *        (with 1 GB to spare).
+ *  NOVA_PBVI_TABLE_NEVER: never built (an existing one is freed). Tensor-core
+ *        updates then re-score their candidates, score the rows their margin
+ *        leaves open and assemble the new alphas straight from the model and
+ *        the alphas; the exact form scores every (belief, action) pair from
+ *        the alphas. Results are bit-identical either way; this is also what
+ *        AUTO does when the table does not fit.
+ * Returns NOVA_ERROR_INVALID_DATA for a null or uninitialized solver or an
+ * unknown mode. */
+#define NOVA_PBVI_TABLE_AUTO  0u
+#define NOVA_PBVI_TABLE_NEVER 1u
+NOVA_API int pomdp_pbvi_set_table_gpu(POMDPPBVIGPU *pbvi, unsigned int mode);
+
 /* Graph mode for later pomdp_pbvi_update_gpu calls on this solver (default
  * off). Once the solver scores on the tensor cores with a fixed schedule (its
  * first tensor-core updates tune it), each update replays a CUDA graph of the

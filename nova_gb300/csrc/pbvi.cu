@@ -934,7 +934,7 @@ int BackupEngine::exact_score(const unsigned *itemList, unsigned nItems, unsigne
 }
 
 bool BackupEngine::ensure_proj(unsigned nU) {
-    if (projUnavailable) return false;
+    if (projUnavailable || tableNever) return false;
     const size_t cols = round_up(std::max(nU, 1u), 32);
     const size_t sCols = round_up(md.n, kProjTileS);
     projSCols = sCols;
@@ -1032,6 +1032,25 @@ int BackupEngine::scan_rows(const unsigned *rowList, unsigned nRows, unsigned nU
     return check_launch(fn, "sentinel fixup");
 }
 
+int BackupEngine::scan_rows_direct(const unsigned *rowList, unsigned nRows, unsigned nU, const char *fn) {
+    if (nRows == 0) return NOVA_SUCCESS;
+    int rc;
+    const size_t allItems = (size_t)md.r * md.m;
+    if ((rc = tc_rows_to_items(*this, rowList, nRows, fn)) != NOVA_SUCCESS) return rc;
+    unsigned nItems = 0;
+    if (cudaMemcpyAsync(&nItems, itemCount, sizeof(unsigned), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+            cudaStreamSynchronize(stream) != cudaSuccess) {
+        cudaGetLastError();
+        NOVA_ERR(fn, "Failed to read the number of (belief, action) pairs to score.");
+        return NOVA_ERROR_MEMCPY_TO_HOST;
+    }
+    if (nItems > allItems) {
+        NOVA_ERR(fn, "Inconsistent (belief, action) list.");
+        return NOVA_ERROR_KERNEL_EXECUTION;
+    }
+    return exact_score(items, nItems, nU, fn);
+}
+
 int BackupEngine::fill_items(unsigned first, unsigned count, const char *fn) {
     if (count == 0) return NOVA_SUCCESS;
     iota_items_kernel<<<ceil_div(count, 256), 256, 0, stream>>>(items, count, first);
@@ -1110,10 +1129,11 @@ int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsi
     // With room for the projection table every exact score is a 64-term
     // dot product over it: the plain form scans every row over it, and the
     // tensor-core form re-scores its near-ties and scans its unresolved rows
-    // with it. Without room, every (belief, action) pair is scored from the
-    // alphas directly.
+    // with it. Without it, the tensor-core form re-scores its near-ties from
+    // the alphas directly and scores the (belief, action) pairs of its
+    // unresolved rows in full, and the plain form scores every pair so.
     useProjNow = ensure_proj(nU);
-    const bool wantTc = (scoring == NOVA_SCORING_BF16 || scoring == NOVA_SCORING_FP16) && useProjNow &&
+    const bool wantTc = (scoring == NOVA_SCORING_BF16 || scoring == NOVA_SCORING_FP16) &&
                         tc_supported(md) && nU >= kTcMinUnique && !tcUnavailable;
     // Tensor-core updates of large models read the table by candidate and by
     // chosen alpha (assembly reads whole columns) and, in FP16, leave almost
@@ -1138,7 +1158,11 @@ int BackupEngine::backup_all(const float *src, unsigned rGamma, float *dst, unsi
         stats.scoring = scoring;
         stats.rowsOverflow = nRows;
         lastScanFrac = (float)nRows / (float)((size_t)md.m * md.z * md.r);
-        if ((rc = scan_rows(rowList, nRows, nU, fn)) != NOVA_SUCCESS) return rc;
+        if (useProjNow) {
+            if ((rc = scan_rows(rowList, nRows, nU, fn)) != NOVA_SUCCESS) return rc;
+        } else if ((rc = scan_rows_direct(rowList, nRows, nU, fn)) != NOVA_SUCCESS) {
+            return rc;
+        }
     } else if (useProjNow) {
         cudaEventRecord(ev[5], stream);
         stats.scoring = NOVA_SCORING_EXACT;
@@ -1695,6 +1719,37 @@ extern "C" int pomdp_pbvi_set_scoring_gpu(POMDPPBVIGPU *pbvi, unsigned int mode)
         }
     }
     ws->eng.scoring = mode;
+    return NOVA_SUCCESS;
+}
+
+extern "C" int pomdp_pbvi_set_table_gpu(POMDPPBVIGPU *pbvi, unsigned int mode) {
+    if (pbvi == nullptr || (mode != NOVA_PBVI_TABLE_AUTO && mode != NOVA_PBVI_TABLE_NEVER)) {
+        NOVA_ERR("pomdp_pbvi_set_table_gpu", "Invalid arguments.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    PbviGpuWorkspace *ws = pbvi_gpu_ws(pbvi);
+    if (ws == nullptr) {
+        NOVA_ERR("pomdp_pbvi_set_table_gpu", "The solver is not initialized.");
+        return NOVA_ERROR_INVALID_DATA;
+    }
+    BackupEngine &e = ws->eng;
+    const bool never = mode == NOVA_PBVI_TABLE_NEVER;
+    if (e.tableNever != never) {
+        // Captured updates read (or skip) the old table.
+        for (int d = 0; d < 2; d++) {
+            if (e.graph[d]) cudaGraphExecDestroy(e.graph[d]);
+            e.graph[d] = nullptr;
+            e.graphSrc[d] = nullptr;
+        }
+    }
+    e.tableNever = never;
+    if (never && e.Proj != nullptr) {
+        cudaStreamSynchronize(e.stream);
+        cudaFree(e.Proj);
+        e.Proj = nullptr;
+        e.projCap = 0;
+        e.projCols = 0;
+    }
     return NOVA_SUCCESS;
 }
 

@@ -66,6 +66,7 @@ struct BackupEngine {
     bool projStateMajor = false;         // this update's table is state-contiguous
     size_t projSCols = 0;                // states per column in the state-contiguous layout (n rounded to 8)
     bool projUnavailable = false, useProjNow = false;
+    bool tableNever = false;             // NOVA_PBVI_TABLE_NEVER: no projection table, ever
     float *scanV = nullptr;              // running best of the chunked row scan
     unsigned *scanU = nullptr;
     size_t scanCap = 0;
@@ -100,6 +101,9 @@ struct BackupEngine {
     int dedup(const float *src, unsigned rows, unsigned *nUnique, const char *fn);
     // Exact scoring of the listed (belief, action) items over the unique rows.
     int exact_score(const unsigned *items, unsigned nItems, unsigned nU, const char *fn);
+    // Without the table: exact scoring of the (belief, action) items of the
+    // listed (a*z+o)*r + i rows (count on the device in itemCount).
+    int scan_rows_direct(const unsigned *rowList, unsigned nRows, unsigned nU, const char *fn);
     // Projection table for nU unique alphas (false if it does not fit).
     bool ensure_proj(unsigned nU);
     int project(unsigned nU, const char *fn);
@@ -178,6 +182,9 @@ int tc_score_launch(BackupEngine &eng, const float *src, unsigned nU, bool timed
 int tc_prepare(BackupEngine &eng, const float *src, unsigned nU, const char *fn);
 int tc_gemm(BackupEngine &eng, bool timed, const char *fn);
 int tc_finish(BackupEngine &eng, const char *fn);
+// The distinct (belief, action) items of the listed rows into eng.items
+// (count in eng.itemCount, on the device).
+int tc_rows_to_items(BackupEngine &eng, const unsigned *rowList, unsigned nRows, const char *fn);
 // One persistent scoring launch (per candidate-list length) over the work
 // units of many prepared solvers, drawn from a device table of their
 // tensor maps, shapes and candidate arrays; the table is built once from

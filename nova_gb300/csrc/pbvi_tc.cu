@@ -852,13 +852,41 @@ __device__ __forceinline__ float proj_row_score(const float *__restrict__ P, con
     return v;
 }
 
+// Without the projection table: the same exact score straight from the
+// model and the transposed alphas, in the table's order (each state's
+// entry fl(gamma * sum_l C1 * alpha(S)), proj_state_lanes_kernel), then the
+// support sum in support order.
+struct DirectScorer {
+    const unsigned *succLen;
+    const float *C1, *Gt;
+    size_t gtCols;
+    __device__ __forceinline__ float score(const DevModel &md, unsigned a, unsigned o, unsigned u,
+                                           const float *__restrict__ bk, const int *__restrict__ sk,
+                                           unsigned Li) const {
+        float v = 0.0f;
+        for (unsigned k = 0; k < Li; k++) {
+            const unsigned s = (unsigned)sk[k];
+            const unsigned Ls = __ldg(succLen + (size_t)s * md.m + a);
+            const float *c = C1 + (((size_t)a * md.n + s) * md.ns) * md.z + o;
+            const int *sp = md.S + ((size_t)s * md.m + a) * md.ns;
+            float vt = 0.0f;
+            for (unsigned l = 0; l < Ls; l++)
+                vt = fadd(vt, fmul(__ldg(c + (size_t)l * md.z), __ldg(Gt + (size_t)__ldg(sp + l) * gtCols + u)));
+            v = fadd(v, fmul(fmul(vt, md.gamma), bk[k]));
+        }
+        return v;
+    }
+};
+
 // One warp per row; returns (in every lane) the number of candidates it
 // re-scored exactly, 0 when the row was settled without re-scoring or sent to
 // the exact scan. The row's lists hold K entries each; entry e of the warp's
 // view is entry e / nLists of list e % nLists, so the lists' leading entries
 // (where the candidates are) spread over the lanes.
+template <bool kDirect>
 __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevModel md,
                                               const unsigned *__restrict__ suppLen, const ProjView pv,
+                                              const DirectScorer ds,
                                               const unsigned *__restrict__ uniqJ, unsigned nLists,
                                               unsigned K, size_t rPad, const float *__restrict__ a1,
                                               const float *__restrict__ d1,
@@ -923,7 +951,7 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
         return 0u;
     }
     // Several candidates: each lane re-scores its own in the exact order.
-    const float *P = pv.slab(ao);
+    const float *P = kDirect ? nullptr : pv.slab(ao);
     const unsigned Li = suppLen[i];
     const int *sk = md.Z + (size_t)i * md.rz;
     const float *bk = md.B + (size_t)i * md.rz;
@@ -932,7 +960,9 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
 #pragma unroll
     for (int j = 0; j < kLaneEntries; j++) {
         if (c[j]) {
-            const float w = proj_row_score(P, pv, u[j], bk, sk, Li);
+            float w;
+            if constexpr (kDirect) w = ds.score(md, a, o, u[j], bk, sk, Li);
+            else w = proj_row_score(P, pv, u[j], bk, sk, Li);
             if (bu == kNoneU || w > best || (w == best && u[j] < bu)) { best = w; bu = u[j]; }
         }
     }
@@ -954,8 +984,10 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
 
 // Rows re-scored and candidates re-scored are counted per block in shared
 // memory, then added to the global counters once per block.
+template <bool kDirect>
 __global__ void __launch_bounds__(256) tc_merge_kernel(DevModel md, const unsigned *__restrict__ suppLen,
-                                const ProjView pv, const unsigned *__restrict__ uniqJ, unsigned nLists, unsigned K,
+                                const ProjView pv, const DirectScorer ds, const unsigned *__restrict__ uniqJ,
+                                unsigned nLists, unsigned K,
                                 size_t rPad, const float *__restrict__ a1, const float *__restrict__ d1,
                                 const float *__restrict__ a1raw, const unsigned *__restrict__ scal,
                                 const float *__restrict__ candV, const unsigned *__restrict__ candU,
@@ -971,8 +1003,8 @@ __global__ void __launch_bounds__(256) tc_merge_kernel(DevModel md, const unsign
     const size_t rows = (size_t)md.m * md.z * md.r;
     unsigned rescored = 0;
     if (row < rows)
-        rescored = merge_row(row, lane, md, suppLen, pv, uniqJ, nLists, K, rPad, a1, d1, a1raw, scal, candV,
-                             candU, candX, ustar, jstar, rowFlag, badModel);
+        rescored = merge_row<kDirect>(row, lane, md, suppLen, pv, ds, uniqJ, nLists, K, rPad, a1, d1, a1raw, scal,
+                                      candV, candU, candX, ustar, jstar, rowFlag, badModel);
     if (lane == 0 && row < rows) rowCand[row] = rescored;
     if (lane == 0 && rescored) {
         atomicAdd(&blockCount[0], 1u);
@@ -1288,10 +1320,12 @@ int tc_finish(BackupEngine &eng, const char *fn) {
     int rc;
     const size_t rows = (size_t)tc->MZ * md.r;
     cudaMemsetAsync(tc->rowFlag, 0, rows * sizeof(unsigned), eng.stream);
-    tc_merge_kernel<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, eng.stream>>>(
-        md, eng.suppLen, eng.proj_view(), eng.uniqJ, L.lists, L.topk, tc->rPad, tc->a1, tc->d1, tc->a1raw, tc->scal,
-        tc->candV, tc->candU, tc->candX, eng.ustar, eng.jstar, tc->rowFlag, tc->rowCand, tc->scal + 3,
-        tc->badModel);
+    const DirectScorer ds{eng.succLen, eng.C1, eng.Gt, eng.gtCols};
+    auto merge = eng.useProjNow ? tc_merge_kernel<false> : tc_merge_kernel<true>;
+    merge<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, eng.stream>>>(
+        md, eng.suppLen, eng.useProjNow ? eng.proj_view() : ProjView{}, ds, eng.uniqJ, L.lists, L.topk, tc->rPad,
+        tc->a1, tc->d1, tc->a1raw, tc->scal, tc->candV, tc->candU, tc->candX, eng.ustar, eng.jstar, tc->rowFlag,
+        tc->rowCand, tc->scal + 3, tc->badModel);
     if ((rc = check_launch(fn, "candidate merge")) != NOVA_SUCCESS) return rc;
     // The list can hold every row: it is sized m*z*r like the flags.
     const unsigned nChunks = ceil_div(rows, kCompactChunk);
@@ -1302,6 +1336,37 @@ int tc_finish(BackupEngine &eng, const char *fn) {
     tc_compact_write_kernel<<<nChunks, 1024, 0, eng.stream>>>(tc->rowFlag, (unsigned)rows, tc->chunkCount,
                                                               tc->rowList);
     return check_launch(fn, "exact-scan list (write)");
+}
+
+// Flag the (belief, action) item of every listed row.
+__global__ void tc_row_items_kernel(const unsigned *__restrict__ rowList, unsigned nRows, unsigned r, unsigned m,
+                                    unsigned z, unsigned *__restrict__ itemFlag) {
+    const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nRows) return;
+    const unsigned row = rowList[t];
+    const unsigned ao = row / r, i = row % r;
+    itemFlag[(size_t)i * m + ao / z] = 1u;
+}
+
+// The distinct (belief, action) items of the listed rows, in increasing
+// order, into eng.items (count in eng.itemCount). The row flags are free
+// again once the row list is written, and hold the item flags.
+int tc_rows_to_items(BackupEngine &eng, const unsigned *rowList, unsigned nRows, const char *fn) {
+    TcState *tc = eng.tc;
+    const DevModel &md = eng.md;
+    const unsigned count = md.r * md.m;
+    int rc;
+    cudaMemsetAsync(tc->rowFlag, 0, (size_t)count * sizeof(unsigned), eng.stream);
+    tc_row_items_kernel<<<ceil_div(nRows, 256), 256, 0, eng.stream>>>(rowList, nRows, md.r, md.m, md.z,
+                                                                      tc->rowFlag);
+    if ((rc = check_launch(fn, "rows to items")) != NOVA_SUCCESS) return rc;
+    const unsigned nChunks = ceil_div(count, kCompactChunk);
+    tc_compact_count_kernel<<<nChunks, 1024, 0, eng.stream>>>(tc->rowFlag, count, tc->chunkCount);
+    if ((rc = check_launch(fn, "item list (count)")) != NOVA_SUCCESS) return rc;
+    tc_compact_scan_kernel<<<1, 1024, 0, eng.stream>>>(tc->chunkCount, nChunks, eng.itemCount);
+    if ((rc = check_launch(fn, "item list (scan)")) != NOVA_SUCCESS) return rc;
+    tc_compact_write_kernel<<<nChunks, 1024, 0, eng.stream>>>(tc->rowFlag, count, tc->chunkCount, eng.items);
+    return check_launch(fn, "item list (write)");
 }
 
 int tc_score_launch(BackupEngine &eng, const float *src, unsigned nU, bool timed, const char *fn) {

@@ -55,6 +55,8 @@ class NovaPBVIStats(ct.Structure):
 SCORING_EXACT = 0
 SCORING_BF16 = 1
 SCORING_FP16 = 2
+TABLE_AUTO = 0
+TABLE_NEVER = 1
 
 _P = ct.POINTER(pomdp.POMDP)
 _C = ct.POINTER(NovaPOMDPPBVICPU)
@@ -70,6 +72,7 @@ for _suffix, _S in (("cpu", _C), ("gpu", _G)):
 
 _nova.nova_gb300_kernel_launches.restype = ct.c_ulonglong
 _nova.pomdp_pbvi_set_scoring_gpu.argtypes = (_G, ct.c_uint)
+_nova.pomdp_pbvi_set_table_gpu.argtypes = (_G, ct.c_uint)
 _nova.pomdp_pbvi_set_graph_gpu.argtypes = (_G, ct.c_uint)
 _nova.pomdp_pbvi_get_stats_gpu.argtypes = (_G, ct.POINTER(NovaPBVIStats))
 _nova.pomdp_pbvi_row_detail_gpu.argtypes = (_G, ct.POINTER(ct.c_uint), ct.POINTER(ct.c_uint))

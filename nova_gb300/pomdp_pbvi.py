@@ -108,6 +108,13 @@ class POMDPPBVIGPU(npp.NovaPOMDPPBVIGPU):
         if result != 0:
             raise RuntimeError("pomdp_pbvi_set_scoring_gpu failed with code %d" % result)
 
+    def set_table(self, mode):
+        """ npp.TABLE_AUTO (build the projection table when it fits) or npp.TABLE_NEVER
+            (score and assemble straight from the alphas; same bits) (pomdp_pbvi_set_table_gpu). """
+        result = npp._nova.pomdp_pbvi_set_table_gpu(self, int(mode))
+        if result != 0:
+            raise RuntimeError("pomdp_pbvi_set_table_gpu failed with code %d" % result)
+
     def set_graph(self, enable=True):
         """ Graph mode for later updates (pomdp_pbvi_set_graph_gpu): once the tensor-core
             schedule is tuned, each update replays a captured CUDA graph. """

@@ -176,11 +176,12 @@ def test_numthreads_must_be_multiple_of_32():
     assert npp._nova.pomdp_pbvi_execute_gpu(alg.pomdpPtr, alg, pol) == 2  # NOVA_ERROR_INVALID_CUDA_PARAM
 
 
-def _run_mode(model, mode, steps):
+def _run_mode(model, mode, steps, table=npp.TABLE_AUTO):
     p = POMDP.from_arrays(model)
     p.initialize_gpu()
     alg = POMDPPBVIGPU(p, GammaInitial=model["GammaInitial"])
     alg.set_scoring(mode)
+    alg.set_table(table)
     out, stats = [], []
     for _ in range(steps):
         alg.update()
@@ -225,3 +226,33 @@ def test_tensor_core_scoring_many_unresolved_rows(mode):
         np.testing.assert_array_equal(bits(Gt), bits(Ge))
         np.testing.assert_array_equal(pt, pe)
     assert any(s["scoring"] == mode for s in stats)
+
+
+@pytest.mark.parametrize("mode", [npp.SCORING_BF16, npp.SCORING_FP16, npp.SCORING_EXACT])
+@pytest.mark.parametrize("shape", [dict(n=300, m=6, z=12, ns=12, r=700, rz=20, horizon=6, seed=5),
+                                   dict(n=512, m=8, z=16, ns=16, r=1024, rz=32, horizon=4, seed=5)])
+def test_without_projection_table_same_bits(mode, shape):
+    """NOVA_PBVI_TABLE_NEVER: tensor-core updates re-score their candidates,
+    score their open rows' (belief, action) pairs and assemble straight from
+    the alphas; the exact form scores every pair so. Every step equals the
+    table-backed exact form bit for bit, and no projection time is spent."""
+    m = synth.random_pomdp(gamma=0.95, **shape)
+    ref, _ = _run_mode(m, npp.SCORING_EXACT, m["horizon"])
+    out, stats = _run_mode(m, mode, m["horizon"], table=npp.TABLE_NEVER)
+    for (Ge, pe), (Gt, pt) in zip(ref, out):
+        np.testing.assert_array_equal(bits(Gt), bits(Ge))
+        np.testing.assert_array_equal(pt, pe)
+    assert stats[-1]["msProject"] < 0.1, stats  # (the first tensor-core step builds its operands there)
+    if mode != npp.SCORING_EXACT:
+        assert any(s["scoring"] == mode for s in stats), stats
+
+
+def test_set_table_rejects_bad_arguments():
+    m = synth.random_pomdp(n=40, m=3, z=4, ns=5, r=64, rz=8, gamma=0.9, horizon=2, seed=1)
+    p = POMDP.from_arrays(m)
+    p.initialize_gpu()
+    alg = POMDPPBVIGPU(p, GammaInitial=m["GammaInitial"])
+    assert npp._nova.pomdp_pbvi_set_table_gpu(alg, 7) != 0
+    assert npp._nova.pomdp_pbvi_set_table_gpu(None, npp.TABLE_NEVER) != 0
+    alg.set_table(npp.TABLE_NEVER)
+    alg.set_table(npp.TABLE_AUTO)
