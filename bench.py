@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--config", default="pbvi_n4096")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--table-free-steps", type=int, default=2,
+                    help="FP16 updates timed without the projection table (NOVA_PBVI_TABLE_NEVER)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-mdp", action="store_true")
@@ -851,8 +853,9 @@ def main():
 
     # ---- a device solver for the parity check and the BF16 and plain legs ---
     parity = {}
-    second = args.bf16_steps > 0 or args.plain_steps > 0 or args.parity_beliefs > 0
+    second = args.bf16_steps > 0 or args.plain_steps > 0 or args.parity_beliefs > 0 or args.table_free_steps > 0
     if second:
+        free_before2 = torch.cuda.mem_get_info()[0]
         alg = POMDPPBVIGPU(p, GammaInitial=Gnow)
         alg.set_scoring(npp.SCORING_FP16)
         alg.update()  # builds the operands and tables; not timed
@@ -914,6 +917,36 @@ def main():
                  "ms_per_step": pms / args.plain_steps,
                  "form": "FP32 SIMT scoring of every unique alpha in nova's operation order"}
         alg.set_scoring(npp.SCORING_FP16)
+
+    # ---- FP16 without the projection table, on the same state ----------------
+    table_free = None
+    if args.table_free_steps > 0:
+        alg.set_scoring(npp.SCORING_FP16)
+        alg.set_table(npp.TABLE_NEVER)  # frees the table
+        alg.update()  # not timed
+        torch.cuda.synchronize()
+        held = free_before2 - torch.cuda.mem_get_info()[0]
+        t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        tst = []
+        t0e.record()
+        for _ in range(args.table_free_steps):
+            alg.update()
+            tst.append(alg.stats())
+        t1e.record()
+        torch.cuda.synchronize()
+        tms = t0e.elapsed_time(t1e)
+        tl = tst[-1]
+        table_free = {"value": r * args.table_free_steps / (tms * 1e-3), "unit": UNIT,
+                      "steps": args.table_free_steps, "ms_per_step": tms / args.table_free_steps,
+                      "solver_device_gb": held / 1e9,
+                      "rows_rescored": tl["rowsMultiCand"], "candidates_rescored": tl["candidates"],
+                      "rows_exact_scan": tl["rowsOverflow"],
+                      "form": "FP16 tensor-core scoring; candidates re-scored, open rows' (belief, action) pairs "
+                              "scored and new alphas assembled straight from the alphas "
+                              "(pomdp_pbvi_set_table_gpu NOVA_PBVI_TABLE_NEVER; same bits)",
+                      "step_breakdown_ms": {k: tl[k] for k in ("msDedup", "msProject", "msScore", "msGemm",
+                                                               "msRescore", "msActions", "msAssemble", "msTotal")}}
+        alg.set_table(npp.TABLE_AUTO)
     if second:
         del alg  # frees the second device solver before the remaining legs
         torch.cuda.synchronize()
@@ -954,6 +987,7 @@ def main():
                                                    "msActions", "msAssemble", "msTotal")},
         "solver_device_gb": solver_bytes / 1e9,
         "bf16_tc": bf16,
+        "table_free": table_free,
         "unique_alphas": [s["uniqueAlphas"] for s in stats],
         "rows_rescored": last["rowsMultiCand"], "pairs_full_exact": last["rowsOverflow"],
         "mdp_vi": mdp,
