@@ -215,10 +215,9 @@ __device__ __forceinline__ void apply_slice(const SliceRegs &g, const uint2 *__r
                                             const float *vtile, float *part, unsigned lane) {
     const int c = (int)g.n0 - (int)lane;
     const bool h1 = lane < g.n1, h2 = lane < g.n2;
-    float q[kSteps], v[kSteps], v1 = 0.0f, v2 = 0.0f;
+    float q[kSteps], v[kSteps], v1 = 0.0f, v2 = 0.0f;  // q[i], v[i] are read only where written
 #pragma unroll
     for (int i = 0; i < kSteps; i++) {
-        q[i] = v[i] = 0.0f;
         if (c > 32 * i) {
             v[i] = tile_value(vtile, g.r[i].x);
             q[i] = part[g.r[i].x >> 16];
@@ -258,8 +257,9 @@ __device__ __forceinline__ bool row_warp_tile(unsigned t, unsigned T, const Slic
                                               volatile int *abortFlag, ViDeviceState *st, unsigned lane) {
     if (t + kDepth < T) {
         load_slice(ahead, rec, hNext, lane);
-        hNext = t + kDepth + 1 < T ? __ldg(sliceHdr + sl0 + (t + kDepth + 1) * kRowWarps)
-                                   : make_uint4(0u, 0u, 0u, 0u);
+        // Past the block's last tile this reads the next block's header (or
+        // the zeroed padding after the last slice): loaded, never used.
+        hNext = __ldg(sliceHdr + sl0 + (t + kDepth + 1) * kRowWarps);
     }
     if (!mbar_wait(smem_addr(&bars[sg]), ph, abortFlag, st)) return false;
     apply_slice(cur, rec, levelCnt, L, sl0 + t * kRowWarps, vt + (size_t)sg * Vt, part, lane);
@@ -284,7 +284,7 @@ __device__ __forceinline__ bool row_warp_pass(unsigned T, unsigned sl0, const ui
 #pragma unroll
     for (unsigned u = 0; u < kDepth; u++)
         if (u < T) load_slice(g[u], rec, __ldg(sliceHdr + sl0 + u * kRowWarps), lane);
-    uint4 hNext = kDepth < T ? __ldg(sliceHdr + sl0 + kDepth * kRowWarps) : make_uint4(0u, 0u, 0u, 0u);
+    uint4 hNext = __ldg(sliceHdr + sl0 + kDepth * kRowWarps);  // padded past the last slice
     for (unsigned t = 0; t < T; t += kDepth + 1) {
 #pragma unroll
         for (unsigned u = 0; u <= kDepth; u++) {
@@ -905,7 +905,15 @@ int vi_plan_build(ViTilePlan *plan, const MDP *mdp, const int *S, const float *T
         rc = check_launch(fn, "sweep plan (slices)");
     }
     if (rc == NOVA_SUCCESS) rc = scan_counts(sliceSize, nSlices, plan->sliceStart, stream, fn);
-    if (rc == NOVA_SUCCESS && !try_alloc(&plan->sliceHdr, nSlices)) rc = NOVA_ERROR_DEVICE_MALLOC;
+    // Headers, with (kDepth + 1) * kRowWarps zeroed ones after the last slice
+    // for the row warps' unconditional look-ahead loads.
+    const size_t hdrPad = (size_t)(kDepth + 1) * kRowWarps;
+    if (rc == NOVA_SUCCESS && !try_alloc(&plan->sliceHdr, nSlices + hdrPad)) rc = NOVA_ERROR_DEVICE_MALLOC;
+    if (rc == NOVA_SUCCESS &&
+            cudaMemsetAsync(plan->sliceHdr + nSlices, 0, hdrPad * sizeof(uint4), stream) != cudaSuccess) {
+        cudaGetLastError();
+        rc = NOVA_ERROR_KERNEL_EXECUTION;
+    }
     if (rc == NOVA_SUCCESS) {
         vi_plan_hdr_kernel<<<ceil_div(nSlices, 256), 256, 0, stream>>>((size_t)nSlices, L, plan->sliceStart,
                                                                        plan->levelCnt, plan->sliceHdr);

@@ -66,7 +66,7 @@ struct ViTilePlan {
     size_t smemBytes = 0;
     uint2 *rec = nullptr;          // [entries + 2] {row << 16 | byte offset in tile, bits of fl(gamma * T)}
     unsigned *sliceStart = nullptr;  // [blocks*tiles*rowWarps + 1] first record of each (block, tile, warp) slice
-    uint4 *sliceHdr = nullptr;       // [slices] {first record, runs, runs with 2+ records, runs with 3+}
+    uint4 *sliceHdr = nullptr;       // [slices + pad] {first record, runs, runs with 2+ records, runs with 3+}
     unsigned *levelCnt = nullptr;    // [slices][levels] runs of each slice with more than q records
     unsigned *flags = nullptr;     // build scratch: unsorted rows, out-of-range successor, longest run
     ~ViTilePlan();
