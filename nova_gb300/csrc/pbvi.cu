@@ -337,7 +337,9 @@ __device__ __forceinline__ float projected(const DevModel &md, const float *__re
 }
 
 // One warp per (belief, action) item: alpha_a on the belief support, then
-// value = sum_k alpha_a(s_k) * b_k in support order.
+// value = sum_k alpha_a(s_k) * b_k in support order. Each lane holds two
+// support states; observations run in the outer loop, so the warp's gathers
+// of one observation's chosen alpha stay within one row.
 __global__ void action_value_kernel(DevModel md, const unsigned *__restrict__ succLen,
                                     const unsigned *__restrict__ suppLen, const float *__restrict__ C3,
                                     const float *__restrict__ G, const unsigned *__restrict__ jstar,
@@ -350,20 +352,24 @@ __global__ void action_value_kernel(DevModel md, const unsigned *__restrict__ su
     const unsigned i = ia / md.m, a = ia % md.m;
     const unsigned Li = suppLen[i];
     float value = 0.0f;
-    for (unsigned k0 = 0; k0 < Li; k0 += 32) {
-        const unsigned k = k0 + lane;
-        float p = 0.0f;
-        if (k < Li) {
-            const int s = md.Z[(size_t)i * md.rz + k];
-            float alpha = md.R[(size_t)s * md.m + a];
-            for (unsigned o = 0; o < md.z; o++) {
-                const unsigned j = jstar[(size_t)ia * md.z + o];
-                alpha = fadd(alpha, projected(md, C3, succLen, G + (size_t)j * md.n, a, o, (unsigned)s));
-            }
-            p = fmul(alpha, md.B[(size_t)i * md.rz + k]);
+    for (unsigned k0 = 0; k0 < Li; k0 += 64) {
+        const unsigned k1 = k0 + lane, k2 = k0 + 32 + lane;
+        const bool v1 = k1 < Li, v2 = k2 < Li;
+        const unsigned s1 = v1 ? (unsigned)md.Z[(size_t)i * md.rz + k1] : 0u;
+        const unsigned s2 = v2 ? (unsigned)md.Z[(size_t)i * md.rz + k2] : 0u;
+        float al1 = v1 ? md.R[(size_t)s1 * md.m + a] : 0.0f;
+        float al2 = v2 ? md.R[(size_t)s2 * md.m + a] : 0.0f;
+        for (unsigned o = 0; o < md.z; o++) {
+            const float *Gj = G + (size_t)jstar[(size_t)ia * md.z + o] * md.n;
+            if (v1) al1 = fadd(al1, projected(md, C3, succLen, Gj, a, o, s1));
+            if (v2) al2 = fadd(al2, projected(md, C3, succLen, Gj, a, o, s2));
         }
-        const unsigned cnt = min(32u, Li - k0);
-        for (unsigned t = 0; t < cnt; t++) value = fadd(value, __shfl_sync(0xffffffffu, p, t));
+        const float p1 = v1 ? fmul(al1, md.B[(size_t)i * md.rz + k1]) : 0.0f;
+        const float p2 = v2 ? fmul(al2, md.B[(size_t)i * md.rz + k2]) : 0.0f;
+        const unsigned c1 = min(32u, Li - k0);
+        for (unsigned t = 0; t < c1; t++) value = fadd(value, __shfl_sync(0xffffffffu, p1, t));
+        const unsigned c2 = Li > k0 + 32 ? min(32u, Li - k0 - 32) : 0u;
+        for (unsigned t = 0; t < c2; t++) value = fadd(value, __shfl_sync(0xffffffffu, p2, t));
     }
     if (lane == 0) actVal[ia] = value;
 }

@@ -93,6 +93,7 @@ struct TcState {
     size_t nPad = 0, rPad = 0, capN = 0;
     unsigned MZ = 0, mTiles = 0;
     unsigned mode = 0;              // NOVA_SCORING_BF16 or NOVA_SCORING_FP16: element type of A and Gb
+    const float *src = nullptr;     // alpha set of the last prepared launch (rows of n)
     uint16_t *A = nullptr;          // [MZ][rPad][nPad] BF16 or FP16 bits, each row scaled by a power of 2
     float *a1 = nullptr;            // [MZ][rPad] bound of sum_s |A| in the row's scaled units
     float *a1raw = nullptr;         // [MZ][rPad] the same bound unscaled
@@ -852,28 +853,23 @@ __device__ __forceinline__ float proj_row_score(const float *__restrict__ P, con
     return v;
 }
 
-// Without the projection table: the same exact score straight from the
-// model and the transposed alphas, in the table's order (each state's
-// entry fl(gamma * sum_l C1 * alpha(S)), proj_state_lanes_kernel), then the
-// support sum in support order.
+// Without the projection table: the same exact scores straight from the
+// model and the alpha rows, in the table's order: each support state's
+// entry fl(gamma * sum_l C * alpha(S)) (proj_state_lanes_kernel; C3 holds the
+// same products as C1, successor-contiguous), times b_k, summed in support
+// order.
+constexpr unsigned kDirectNs = 32;  // successors per state the direct re-score holds in registers
+
 struct DirectScorer {
     const unsigned *succLen;
-    const float *C1, *Gt;
-    size_t gtCols;
-    __device__ __forceinline__ float score(const DevModel &md, unsigned a, unsigned o, unsigned u,
-                                           const float *__restrict__ bk, const int *__restrict__ sk,
-                                           unsigned Li) const {
+    const float *C3, *G;  // G: the update's alpha set, rows of n
+    __device__ __forceinline__ float vt(const DevModel &md, unsigned a, unsigned o, unsigned s,
+                                        const float *__restrict__ Gj) const {
+        const unsigned Ls = __ldg(succLen + (size_t)s * md.m + a);
+        const float *c = C3 + (((size_t)a * md.z + o) * md.n + s) * md.ns;
+        const int *sp = md.S + ((size_t)s * md.m + a) * md.ns;
         float v = 0.0f;
-        for (unsigned k = 0; k < Li; k++) {
-            const unsigned s = (unsigned)sk[k];
-            const unsigned Ls = __ldg(succLen + (size_t)s * md.m + a);
-            const float *c = C1 + (((size_t)a * md.n + s) * md.ns) * md.z + o;
-            const int *sp = md.S + ((size_t)s * md.m + a) * md.ns;
-            float vt = 0.0f;
-            for (unsigned l = 0; l < Ls; l++)
-                vt = fadd(vt, fmul(__ldg(c + (size_t)l * md.z), __ldg(Gt + (size_t)__ldg(sp + l) * gtCols + u)));
-            v = fadd(v, fmul(fmul(vt, md.gamma), bk[k]));
-        }
+        for (unsigned l = 0; l < Ls; l++) v = fadd(v, fmul(__ldg(c + l), __ldg(Gj + __ldg(sp + l))));
         return v;
     }
 };
@@ -886,7 +882,7 @@ struct DirectScorer {
 template <bool kDirect>
 __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevModel md,
                                               const unsigned *__restrict__ suppLen, const ProjView pv,
-                                              const DirectScorer ds,
+                                              const DirectScorer ds, float *scratch,
                                               const unsigned *__restrict__ uniqJ, unsigned nLists,
                                               unsigned K, size_t rPad, const float *__restrict__ a1,
                                               const float *__restrict__ d1,
@@ -950,21 +946,88 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
         if (lane == 0) { ustar[js] = uu; jstar[js] = uniqJ[uu]; }
         return 0u;
     }
-    // Several candidates: each lane re-scores its own in the exact order.
-    const float *P = kDirect ? nullptr : pv.slab(ao);
     const unsigned Li = suppLen[i];
     const int *sk = md.Z + (size_t)i * md.rz;
     const float *bk = md.B + (size_t)i * md.rz;
     float best = -INFINITY;
     unsigned bu = kNoneU;
+    if constexpr (!kDirect) {
+        // Several candidates: each lane re-scores its own in the exact order.
+        const float *P = pv.slab(ao);
 #pragma unroll
-    for (int j = 0; j < kLaneEntries; j++) {
-        if (c[j]) {
-            float w;
-            if constexpr (kDirect) w = ds.score(md, a, o, u[j], bk, sk, Li);
-            else w = proj_row_score(P, pv, u[j], bk, sk, Li);
-            if (bu == kNoneU || w > best || (w == best && u[j] < bu)) { best = w; bu = u[j]; }
+        for (int j = 0; j < kLaneEntries; j++) {
+            if (c[j]) {
+                const float w = proj_row_score(P, pv, u[j], bk, sk, Li);
+                if (bu == kNoneU || w > best || (w == best && u[j] < bu)) { best = w; bu = u[j]; }
+            }
         }
+    } else {
+        // Without the table the warp scores its candidates together, up to
+        // 32 at a time (candidate t held by lane t): for every 32 support
+        // states, lane k computes state k's term for each candidate of the
+        // batch into the warp's scratch (the gathers of one candidate stay
+        // in one alpha row), then lane t adds candidate t's terms in support
+        // order.
+        unsigned myU = kNoneU, nb = 0;
+        auto flush = [&]() {
+            float total = 0.0f;
+            for (unsigned k0 = 0; k0 < Li; k0 += 32u) {
+                const unsigned k = k0 + lane;
+                const bool kv = k < Li;
+                const unsigned s = kv ? (unsigned)sk[k] : 0u;
+                const float b = kv ? bk[k] : 0.0f;
+                if (md.ns <= kDirectNs) {
+                    // The state's coefficients and successors, loaded once for
+                    // the whole batch.
+                    const unsigned Ls = kv ? __ldg(ds.succLen + (size_t)s * md.m + a) : 0u;
+                    const float *cp = ds.C3 + (((size_t)a * md.z + o) * md.n + s) * md.ns;
+                    const int *spp = md.S + ((size_t)s * md.m + a) * md.ns;
+                    float cc[kDirectNs];
+                    int ss[kDirectNs];
+#pragma unroll
+                    for (unsigned l = 0; l < kDirectNs; l++) {
+                        cc[l] = l < Ls ? __ldg(cp + l) : 0.0f;
+                        ss[l] = l < Ls ? __ldg(spp + l) : 0;
+                    }
+                    for (unsigned t = 0; t < nb; t++) {
+                        const unsigned uu = __shfl_sync(0xffffffffu, myU, t);
+                        const float *Gj = ds.G + (size_t)__ldg(uniqJ + uu) * md.n;
+                        float v = 0.0f;
+#pragma unroll
+                        for (unsigned l = 0; l < kDirectNs; l++)
+                            if (l < Ls) v = fadd(v, fmul(cc[l], __ldg(Gj + ss[l])));
+                        scratch[t * 32u + lane] = kv ? fmul(fmul(v, md.gamma), b) : 0.0f;
+                    }
+                } else {
+                    for (unsigned t = 0; t < nb; t++) {
+                        const unsigned uu = __shfl_sync(0xffffffffu, myU, t);
+                        float p = 0.0f;
+                        if (kv) p = fmul(fmul(ds.vt(md, a, o, s, ds.G + (size_t)__ldg(uniqJ + uu) * md.n), md.gamma), b);
+                        scratch[t * 32u + lane] = p;
+                    }
+                }
+                __syncwarp();
+                if (lane < nb) {
+                    const unsigned cnt = min(32u, Li - k0);
+                    for (unsigned q = 0; q < cnt; q++) total = fadd(total, scratch[lane * 32u + q]);
+                }
+                __syncwarp();
+            }
+            if (lane < nb && (bu == kNoneU || total > best || (total == best && myU < bu))) { best = total; bu = myU; }
+            nb = 0;
+        };
+#pragma unroll
+        for (int j = 0; j < kLaneEntries; j++) {
+            unsigned msk = __ballot_sync(0xffffffffu, c[j]);
+            while (msk) {
+                const unsigned src = __ffs(msk) - 1;
+                msk &= msk - 1;
+                const unsigned uu = __shfl_sync(0xffffffffu, u[j], src);
+                if (lane == nb) myU = uu;
+                if (++nb == 32u) flush();
+            }
+        }
+        if (nb) flush();
     }
     for (int off = 16; off > 0; off >>= 1) {
         const float b2 = __shfl_xor_sync(0xffffffffu, best, off);
@@ -985,7 +1048,7 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
 // Rows re-scored and candidates re-scored are counted per block in shared
 // memory, then added to the global counters once per block.
 template <bool kDirect>
-__global__ void __launch_bounds__(256) tc_merge_kernel(DevModel md, const unsigned *__restrict__ suppLen,
+__global__ void __launch_bounds__(256, kDirect ? 1 : 2) tc_merge_kernel(DevModel md, const unsigned *__restrict__ suppLen,
                                 const ProjView pv, const DirectScorer ds, const unsigned *__restrict__ uniqJ,
                                 unsigned nLists, unsigned K,
                                 size_t rPad, const float *__restrict__ a1, const float *__restrict__ d1,
@@ -996,6 +1059,7 @@ __global__ void __launch_bounds__(256) tc_merge_kernel(DevModel md, const unsign
                                 unsigned *__restrict__ rowCand, unsigned *__restrict__ counters,
                                 const unsigned *__restrict__ badModel) {
     __shared__ unsigned blockCount[2];
+    extern __shared__ float mergeScratch[];  // direct form: [warps][32 candidates][32 states]
     if (threadIdx.x == 0) { blockCount[0] = 0u; blockCount[1] = 0u; }
     __syncthreads();
     const unsigned lane = threadIdx.x & 31;
@@ -1003,8 +1067,9 @@ __global__ void __launch_bounds__(256) tc_merge_kernel(DevModel md, const unsign
     const size_t rows = (size_t)md.m * md.z * md.r;
     unsigned rescored = 0;
     if (row < rows)
-        rescored = merge_row<kDirect>(row, lane, md, suppLen, pv, ds, uniqJ, nLists, K, rPad, a1, d1, a1raw, scal,
-                                      candV, candU, candX, ustar, jstar, rowFlag, badModel);
+        rescored = merge_row<kDirect>(row, lane, md, suppLen, pv, ds, mergeScratch + (threadIdx.x >> 5) * 1024u,
+                                      uniqJ, nLists, K, rPad, a1, d1, a1raw, scal, candV, candU, candX, ustar, jstar,
+                                      rowFlag, badModel);
     if (lane == 0 && row < rows) rowCand[row] = rescored;
     if (lane == 0 && rescored) {
         atomicAdd(&blockCount[0], 1u);
@@ -1234,6 +1299,7 @@ int tc_prepare(BackupEngine &eng, const float *src, unsigned nU, const char *fn)
     if (!eng.tc && (rc = tc_build(eng, fn)) != NOVA_SUCCESS) return rc;
     TcState *tc = eng.tc;
     if (tc->mode != eng.scoring && (rc = tc_build_operand(eng, tc, fn)) != NOVA_SUCCESS) return rc;
+    tc->src = src;
     const DevModel &md = eng.md;
     const bool fp16 = tc->mode == NOVA_SCORING_FP16;
     // BF16 carries the alphas as two BF16 terms (split); FP16 as one.
@@ -1320,9 +1386,10 @@ int tc_finish(BackupEngine &eng, const char *fn) {
     int rc;
     const size_t rows = (size_t)tc->MZ * md.r;
     cudaMemsetAsync(tc->rowFlag, 0, rows * sizeof(unsigned), eng.stream);
-    const DirectScorer ds{eng.succLen, eng.C1, eng.Gt, eng.gtCols};
+    const DirectScorer ds{eng.succLen, eng.C3, tc->src};
     auto merge = eng.useProjNow ? tc_merge_kernel<false> : tc_merge_kernel<true>;
-    merge<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, eng.stream>>>(
+    const size_t mergeSmem = eng.useProjNow ? 0 : (256 / 32) * 1024 * sizeof(float);
+    merge<<<(unsigned)ceil_div(rows * 32, 256), 256, mergeSmem, eng.stream>>>(
         md, eng.suppLen, eng.useProjNow ? eng.proj_view() : ProjView{}, ds, eng.uniqJ, L.lists, L.topk, tc->rPad,
         tc->a1, tc->d1, tc->a1raw, tc->scal, tc->candV, tc->candU, tc->candX, eng.ustar, eng.jstar, tc->rowFlag,
         tc->rowCand, tc->scal + 3, tc->badModel);

@@ -230,12 +230,15 @@ def test_tensor_core_scoring_many_unresolved_rows(mode):
 
 @pytest.mark.parametrize("mode", [npp.SCORING_BF16, npp.SCORING_FP16, npp.SCORING_EXACT])
 @pytest.mark.parametrize("shape", [dict(n=300, m=6, z=12, ns=12, r=700, rz=20, horizon=6, seed=5),
-                                   dict(n=512, m=8, z=16, ns=16, r=1024, rz=32, horizon=4, seed=5)])
+                                   dict(n=512, m=8, z=16, ns=16, r=1024, rz=32, horizon=4, seed=5),
+                                   dict(n=200, m=4, z=8, ns=40, r=512, rz=40, horizon=5, seed=7)])
 def test_without_projection_table_same_bits(mode, shape):
     """NOVA_PBVI_TABLE_NEVER: tensor-core updates re-score their candidates,
     score their open rows' (belief, action) pairs and assemble straight from
     the alphas; the exact form scores every pair so. Every step equals the
-    table-backed exact form bit for bit, and no projection time is spent."""
+    table-backed exact form bit for bit, and no projection time is spent
+    (ns = 40 takes the re-score's path for more than 32 successors, rz = 40
+    its support chunks past 32)."""
     m = synth.random_pomdp(gamma=0.95, **shape)
     ref, _ = _run_mode(m, npp.SCORING_EXACT, m["horizon"])
     out, stats = _run_mode(m, mode, m["horizon"], table=npp.TABLE_NEVER)
