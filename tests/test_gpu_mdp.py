@@ -260,3 +260,48 @@ def test_tiled_equals_gather_at_full_size(tiling):
     V1, pi1 = orc.mdp_vi_sweep(md, np.zeros(md["n"], np.float32))
     np.testing.assert_array_equal(bits(pol.V_array()), bits(V1))
     np.testing.assert_array_equal(pol.pi_array(), pi1)
+
+
+@pytest.mark.parametrize("m_actions", [8, 5, 16])
+def test_tiled_scan_nan_inf_and_ties(tiling, m_actions):
+    """Rewards with NaN, +-inf and exact ties: the tiled sweep's action scan
+    (rotated reads for power-of-two m, the reference's strict '>' in action
+    order, a NaN at action 0 kept) and its residual (NaN differences skipped,
+    as fmax skips them) equal the oracle's sweeps bit for bit."""
+    tiling.set_tiling(nmvi.TILING_ALWAYS, 512)
+    md = synth.random_mdp(n=3000, m=m_actions, ns=6, gamma=0.9, horizon=3, seed=31 + m_actions)
+    R = md["R"].copy()
+    rng = np.random.default_rng(m_actions)
+    rows = rng.choice(md["n"], 60, replace=False)
+    R[rows[:3], 0] = np.nan
+    R[rows[15:30], rng.integers(1, m_actions, 15)] = np.nan
+    R[rows[30:40], rng.integers(0, m_actions, 10)] = np.inf
+    R[rows[40:50], rng.integers(0, m_actions, 10)] = -np.inf
+    R[rows[50:], :] = 0.25  # every action ties before the successor terms
+    md["R"] = R
+    m = MDP.from_arrays(md)
+    m.initialize_gpu()
+    alg = MDPValueIterationGPU(m, Vinitial=np.zeros(md["n"], np.float32))
+    V = np.zeros(md["n"], np.float32)
+    for h in range(3):
+        assert nmvi._nova.mdp_vi_update_gpu(alg.mdpPtr, alg) == 0
+        assert tiling.tiling_status(alg) == 1
+        Vn, pi = orc.mdp_vi_sweep(md, V)
+        resid = ct.c_double(0)
+        assert nmvi._nova.mdp_vi_residual_gpu(alg.mdpPtr, alg, ct.byref(resid)) == 0
+        with np.errstate(invalid="ignore"):
+            d = np.abs(Vn.astype(np.float64) - V.astype(np.float64))
+        d = d[~np.isnan(d)]
+        assert resid.value == (np.max(d) if d.size else 0.0)
+        V = Vn
+    from nova_gb300 import mdp_value_function as mvf
+    pol = mvf.MDPValueFunction()
+    assert nmvi._nova.mdp_vi_get_policy_gpu(alg.mdpPtr, alg, pol) == 0
+    Vg = pol.V_array()
+    # NaN payloads differ between the GPU (canonical NaN) and x86; NaN
+    # positions and every other bit must match.
+    nan = np.isnan(V)
+    assert nan.any() and not nan.all()
+    np.testing.assert_array_equal(np.isnan(Vg), nan)
+    np.testing.assert_array_equal(bits(Vg[~nan]), bits(V[~nan]))
+    np.testing.assert_array_equal(pol.pi_array(), pi)
