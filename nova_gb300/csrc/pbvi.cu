@@ -336,11 +336,48 @@ __device__ __forceinline__ float projected(const DevModel &md, const float *__re
     return fmul(vt, md.gamma);
 }
 
+// The same term with state s's successors already in registers (ss, Ls of
+// them, at most kRegNs) and its coefficients read as float4 (ns a multiple
+// of 4, rows 16-byte aligned): same operations in the same order.
+constexpr unsigned kRegNs = 32;
+__device__ __forceinline__ bool reg_form(const DevModel &md) { return md.ns <= kRegNs && md.ns % 4u == 0u; }
+__device__ __forceinline__ float projected_regs(const DevModel &md, const float *__restrict__ C3,
+                                                const int (&ss)[kRegNs], unsigned Ls, const float *__restrict__ Gj,
+                                                unsigned a, unsigned o, unsigned s) {
+    const float4 *c4 = reinterpret_cast<const float4 *>(C3 + (((size_t)a * md.z + o) * md.n + s) * md.ns);
+    float g[kRegNs], c[kRegNs];
+#pragma unroll
+    for (unsigned q = 0; q < kRegNs / 4; q++) {
+        if (4u * q < Ls) {
+            const float4 v = __ldg(c4 + q);
+            c[4 * q] = v.x; c[4 * q + 1] = v.y; c[4 * q + 2] = v.z; c[4 * q + 3] = v.w;
+        }
+    }
+#pragma unroll
+    for (unsigned l = 0; l < kRegNs; l++)
+        if (l < Ls) g[l] = __ldg(Gj + ss[l]);
+    float vt = 0.0f;
+#pragma unroll
+    for (unsigned l = 0; l < kRegNs; l++)
+        if (l < Ls) vt = fadd(vt, fmul(c[l], g[l]));
+    return fmul(vt, md.gamma);
+}
+
+// State s's successors under action a into registers (the first Ls).
+__device__ __forceinline__ unsigned load_succ(const DevModel &md, const unsigned *__restrict__ succLen, unsigned a,
+                                              unsigned s, int (&ss)[kRegNs]) {
+    const unsigned Ls = __ldg(succLen + (size_t)s * md.m + a);
+    const int *sp = md.S + ((size_t)s * md.m + a) * md.ns;
+#pragma unroll
+    for (unsigned l = 0; l < kRegNs; l++) ss[l] = l < Ls ? __ldg(sp + l) : 0;
+    return Ls;
+}
+
 // One warp per (belief, action) item: alpha_a on the belief support, then
-// value = sum_k alpha_a(s_k) * b_k in support order. Each lane holds two
-// support states; observations run in the outer loop, so the warp's gathers
+// value = sum_k alpha_a(s_k) * b_k in support order. Lane k takes support
+// state k0 + k; observations run in the outer loop, so the warp's gathers
 // of one observation's chosen alpha stay within one row.
-__global__ void action_value_kernel(DevModel md, const unsigned *__restrict__ succLen,
+__global__ void __launch_bounds__(256) action_value_kernel(DevModel md, const unsigned *__restrict__ succLen,
                                     const unsigned *__restrict__ suppLen, const float *__restrict__ C3,
                                     const float *__restrict__ G, const unsigned *__restrict__ jstar,
                                     const unsigned *__restrict__ items, unsigned nItems,
@@ -351,25 +388,29 @@ __global__ void action_value_kernel(DevModel md, const unsigned *__restrict__ su
     const unsigned ia = items ? items[warpGlobal] : warpGlobal;
     const unsigned i = ia / md.m, a = ia % md.m;
     const unsigned Li = suppLen[i];
+    const bool regs = reg_form(md);
     float value = 0.0f;
-    for (unsigned k0 = 0; k0 < Li; k0 += 64) {
-        const unsigned k1 = k0 + lane, k2 = k0 + 32 + lane;
-        const bool v1 = k1 < Li, v2 = k2 < Li;
-        const unsigned s1 = v1 ? (unsigned)md.Z[(size_t)i * md.rz + k1] : 0u;
-        const unsigned s2 = v2 ? (unsigned)md.Z[(size_t)i * md.rz + k2] : 0u;
-        float al1 = v1 ? md.R[(size_t)s1 * md.m + a] : 0.0f;
-        float al2 = v2 ? md.R[(size_t)s2 * md.m + a] : 0.0f;
-        for (unsigned o = 0; o < md.z; o++) {
-            const float *Gj = G + (size_t)jstar[(size_t)ia * md.z + o] * md.n;
-            if (v1) al1 = fadd(al1, projected(md, C3, succLen, Gj, a, o, s1));
-            if (v2) al2 = fadd(al2, projected(md, C3, succLen, Gj, a, o, s2));
+    for (unsigned k0 = 0; k0 < Li; k0 += 32) {
+        const unsigned k = k0 + lane;
+        const bool v = k < Li;
+        const unsigned s = v ? (unsigned)md.Z[(size_t)i * md.rz + k] : 0u;
+        float alpha = v ? md.R[(size_t)s * md.m + a] : 0.0f;
+        if (regs) {
+            int ss[kRegNs];
+            const unsigned Ls = v ? load_succ(md, succLen, a, s, ss) : 0u;
+            for (unsigned o = 0; o < md.z; o++) {
+                const float *Gj = G + (size_t)jstar[(size_t)ia * md.z + o] * md.n;
+                if (v) alpha = fadd(alpha, projected_regs(md, C3, ss, Ls, Gj, a, o, s));
+            }
+        } else {
+            for (unsigned o = 0; o < md.z; o++) {
+                const float *Gj = G + (size_t)jstar[(size_t)ia * md.z + o] * md.n;
+                if (v) alpha = fadd(alpha, projected(md, C3, succLen, Gj, a, o, s));
+            }
         }
-        const float p1 = v1 ? fmul(al1, md.B[(size_t)i * md.rz + k1]) : 0.0f;
-        const float p2 = v2 ? fmul(al2, md.B[(size_t)i * md.rz + k2]) : 0.0f;
-        const unsigned c1 = min(32u, Li - k0);
-        for (unsigned t = 0; t < c1; t++) value = fadd(value, __shfl_sync(0xffffffffu, p1, t));
-        const unsigned c2 = Li > k0 + 32 ? min(32u, Li - k0 - 32) : 0u;
-        for (unsigned t = 0; t < c2; t++) value = fadd(value, __shfl_sync(0xffffffffu, p2, t));
+        const float p = v ? fmul(alpha, md.B[(size_t)i * md.rz + k]) : 0.0f;
+        const unsigned cnt = min(32u, Li - k0);
+        for (unsigned t = 0; t < cnt; t++) value = fadd(value, __shfl_sync(0xffffffffu, p, t));
     }
     if (lane == 0) actVal[ia] = value;
 }
@@ -403,6 +444,18 @@ __global__ void assemble_kernel(DevModel md, const unsigned *__restrict__ succLe
     const unsigned *js = jstar + ((size_t)i * md.m + a) * md.z;
     for (unsigned o = threadIdx.x; o < md.z; o += blockDim.x) jsh[o] = js[o];
     __syncthreads();
+    if (reg_form(md)) {
+        // The state's successors stay in registers across the observations.
+        for (unsigned s = threadIdx.x; s < md.n; s += blockDim.x) {
+            int ss[kRegNs];
+            const unsigned Ls = load_succ(md, succLen, a, s, ss);
+            float alpha = md.R[(size_t)s * md.m + a];
+            for (unsigned o = 0; o < md.z; o++)
+                alpha = fadd(alpha, projected_regs(md, C3, ss, Ls, G + (size_t)jsh[o] * md.n, a, o, s));
+            out[s] = alpha;
+        }
+        return;
+    }
     for (unsigned s = threadIdx.x; s < md.n; s += blockDim.x) {
         float alpha = md.R[(size_t)s * md.m + a];
         for (unsigned o = 0; o < md.z; o++)
