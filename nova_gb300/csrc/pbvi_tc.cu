@@ -989,14 +989,32 @@ __device__ __forceinline__ unsigned merge_row(size_t row, unsigned lane, DevMode
                         cc[l] = l < Ls ? __ldg(cp + l) : 0.0f;
                         ss[l] = l < Ls ? __ldg(spp + l) : 0;
                     }
-                    for (unsigned t = 0; t < nb; t++) {
-                        const unsigned uu = __shfl_sync(0xffffffffu, myU, t);
-                        const float *Gj = ds.G + (size_t)__ldg(uniqJ + uu) * md.n;
-                        float v = 0.0f;
+                    // Two candidates at a time: their gathers are issued
+                    // together, their sums are two independent chains.
+                    for (unsigned t = 0; t < nb; t += 2) {
+                        const unsigned t1 = t + 1 < nb ? t + 1 : t;
+                        const unsigned u0 = __shfl_sync(0xffffffffu, myU, t);
+                        const unsigned u1 = __shfl_sync(0xffffffffu, myU, t1);
+                        const float *G0 = ds.G + (size_t)__ldg(uniqJ + u0) * md.n;
+                        const float *G1 = ds.G + (size_t)__ldg(uniqJ + u1) * md.n;
+                        float g0[kDirectNs], g1[kDirectNs];
 #pragma unroll
-                        for (unsigned l = 0; l < kDirectNs; l++)
-                            if (l < Ls) v = fadd(v, fmul(cc[l], __ldg(Gj + ss[l])));
-                        scratch[t * 32u + lane] = kv ? fmul(fmul(v, md.gamma), b) : 0.0f;
+                        for (unsigned l = 0; l < kDirectNs; l++) {
+                            if (l < Ls) {
+                                g0[l] = __ldg(G0 + ss[l]);
+                                g1[l] = __ldg(G1 + ss[l]);
+                            }
+                        }
+                        float v0 = 0.0f, v1 = 0.0f;
+#pragma unroll
+                        for (unsigned l = 0; l < kDirectNs; l++) {
+                            if (l < Ls) {
+                                v0 = fadd(v0, fmul(cc[l], g0[l]));
+                                v1 = fadd(v1, fmul(cc[l], g1[l]));
+                            }
+                        }
+                        scratch[t * 32u + lane] = kv ? fmul(fmul(v0, md.gamma), b) : 0.0f;
+                        if (t1 != t) scratch[t1 * 32u + lane] = kv ? fmul(fmul(v1, md.gamma), b) : 0.0f;
                     }
                 } else {
                     for (unsigned t = 0; t < nb; t++) {
