@@ -397,9 +397,10 @@ struct SingleUnits {
     }
 };
 
-// A solver of a batched launch: its tensor maps in global memory (64-byte
-// aligned) and its first unit in the launch's unit sequence.
-struct alignas(64) BatchModel {
+// A solver of a batched launch: its tensor maps in global memory (aligned as
+// CUtensorMap requires, which the struct inherits) and its first unit in the
+// launch's unit sequence.
+struct BatchModel {
     CUtensorMap tmA, tmB;
     unsigned unitStart, MZ, rPad, r, mTiles, nTiles, groups, nU, kBlocks, kSplit;
     const float *a1, *d1;
