@@ -448,9 +448,11 @@ __global__ void __launch_bounds__(kThreads, 1) bellman_tiled_kernel(
                                 __ldg(sliceStart + (c0 + min(T, kAhead)) * kRowWarps));
                 // R goes in after the first kStages tiles of the block were
                 // issued (their slots were freed by the previous block's
-                // last tiles, before its scan).
+                // last tiles, before its scan); the CTA's first block copies
+                // it before its first V tiles.
+                const unsigned rAt = it == 0 ? 0u : min(T, kStages);
                 for (unsigned t = 0; t <= T; t++) {
-                    if (t == min(T, kStages)) {
+                    if (t == rAt) {
                         if (it > 0 && !mbar_wait<0>(qFree, (it - 1) & 1u, abortFlag, st)) { ok = false; break; }
                         const float *src = R + (size_t)s0 * m;
                         const unsigned body = rows & ~3u;
