@@ -34,8 +34,9 @@
 //     prefetches the records of the tile kAhead tiles on into L2 with one
 //     bulk prefetch.
 //   * The single-record runs of a slice are dealt round-robin over the 32
-//     shared-memory banks of their partial sums (row mod 32), so a warp's 32
-//     runs of one step update distinct banks.
+//     shared-memory banks of their partial sums (row mod 32), so the 32 runs
+//     of one step mostly update distinct banks (a step may span the end of
+//     one round and the start of the next).
 //
 // Order of operations: the reference computes Q = R(s,a), then for each
 // successor in list order Q += (gamma * T) * V[s'] (mdp_vi_cpu.cpp:45-52).
