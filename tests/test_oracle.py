@@ -117,6 +117,28 @@ def test_live_against_reference_library(seed):
     np.testing.assert_array_equal(q1, q2)
 
 
+@pytest.mark.skipif(not orc.ref_available(), reason="reference sources not present on this machine")
+def test_mdp_nan_inf_and_ties_against_reference_library():
+    """Rewards with NaN (at action 0 and later actions), +-inf and exact ties:
+    the oracle's VI keeps the reference's semantics (a NaN at action 0 stays,
+    later NaNs lose every strict comparison), bit for bit with the payloads."""
+    md = synth.random_mdp(n=400, m=6, ns=5, gamma=0.9, horizon=3, seed=77)
+    R = md["R"].copy()
+    rng = np.random.default_rng(77)
+    rows = rng.choice(md["n"], 40, replace=False)
+    R[rows[:2], 0] = np.nan
+    R[rows[2:12], rng.integers(1, 6, 10)] = np.nan
+    R[rows[12:20], rng.integers(0, 6, 8)] = np.inf
+    R[rows[20:28], rng.integers(0, 6, 8)] = -np.inf
+    R[rows[28:], :] = 0.25
+    md["R"] = R
+    V1, q1 = orc.ref_mdp_vi_solve(md)
+    V2, q2 = orc.mdp_vi_solve(md)
+    assert np.isnan(V1).any() and not np.isnan(V1).all()
+    np.testing.assert_array_equal(bits(V1), bits(V2))
+    np.testing.assert_array_equal(q1, q2)
+
+
 def test_oracle_detects_a_planted_mistake():
     """A perturbed model must change the oracle's answer (the checker is not vacuous)."""
     g = load_golden("pbvi_n64_h5")
