@@ -68,7 +68,7 @@ constexpr unsigned kWarps = kThreads / 32;
 constexpr unsigned kRowWarps = kWarps - 1;        // warps that apply records; the last one stages V
 constexpr int kSteps = 9;                         // groups of 32 records a warp holds per slice in registers
 constexpr unsigned kStages = 3;                   // V tiles in flight
-constexpr unsigned kAhead = 4;                    // tiles between a slice's L2 prefetch and its use
+constexpr unsigned kAhead = 2;                    // tiles between a slice's L2 prefetch and its use
 constexpr unsigned kDepth = 1;                    // tiles between a slice's register load and its use
 constexpr unsigned kMaxRows = 65535u;             // rows of one block (16-bit row field)
 constexpr unsigned kMaxLevels = 31u;              // longest run of one row inside one tile
