@@ -254,7 +254,9 @@ NOVA_API int mdp_vi_residual_gpu(const MDP *mdp, const MDPVIGPU *vi, double *res
  *        successor entries), NOVA_VI_TILING_ALWAYS (whenever the model
  *        qualifies), NOVA_VI_TILING_NEVER.
  *  tileStates: states per shared-memory tile of V, a multiple of 4 in
- *        [64, 16384], or 0 for the default 9216.
+ *        [64, 16384], or 0 for the default: the largest tile of 8192 to
+ *        10240 states (steps of 256) that needs no more rounds of source
+ *        blocks over the SMs than 8192 states does.
  * The setting is process-wide and applies to plans built after the call. */
 #define NOVA_VI_TILING_AUTO   0u
 #define NOVA_VI_TILING_ALWAYS 1u

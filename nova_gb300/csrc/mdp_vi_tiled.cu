@@ -72,7 +72,8 @@ constexpr unsigned kAhead = 2;                    // tiles between a slice's L2 
 constexpr unsigned kDepth = 1;                    // tiles between a slice's register load and its use
 constexpr unsigned kMaxRows = 65535u;             // rows of one block (16-bit row field)
 constexpr unsigned kMaxLevels = 31u;              // longest run of one row inside one tile
-constexpr unsigned kDefaultTileStates = 9216u;
+constexpr unsigned kDefaultTileStates = 8192u;       // default tile: the largest of
+constexpr unsigned kMaxDefaultTileStates = 10240u;   // [8192, 10240] with the fewest waves
 constexpr unsigned long long kAutoMinEntries = 1ull << 22;
 constexpr long long kWaitCycles = 4000000000ll;   // ~2 s at 2 GHz
 constexpr size_t kBarrierBytes = 96;              // full[kStages], empty[kStages], qReady, qFree, two flags
@@ -817,12 +818,30 @@ int vi_plan_build(ViTilePlan *plan, const MDP *mdp, const int *S, const float *T
         cudaGetLastError();
         return NOVA_SUCCESS;
     }
+    const size_t reserve = 1024;  // static shared memory of the residual reduction, with room to spare
+    // Waves of blocks (rounds of Sb-state blocks over the SMs) a tile size
+    // leaves room for: the V ring and Q share the CTA's shared memory.
+    auto waves_for = [&](unsigned vt) -> unsigned {
+        const size_t fx = (size_t)kStages * vt * 4 + 16 + kBarrierBytes;
+        if ((size_t)optin < fx + reserve + (size_t)m * 4) return ~0u;
+        const unsigned rows = (unsigned)std::min<size_t>(((size_t)optin - fx - reserve) / 4, kMaxRows);
+        const unsigned sb = rows / m;
+        return sb == 0 ? ~0u : (unsigned)ceil_div(n, (unsigned long long)sms * sb);
+    };
     const unsigned setting = g_tile_states.load();
-    unsigned Vt = setting ? setting : kDefaultTileStates;
+    unsigned Vt = setting;
+    if (Vt == 0) {
+        // Default: the largest tile in [kDefaultTileStates, kMaxDefaultTileStates]
+        // (steps of 256 states) that needs no more waves than the smallest:
+        // fewer, longer tiles cut the per-slice work, another wave re-reads V.
+        Vt = kDefaultTileStates;
+        const unsigned w0 = waves_for(kDefaultTileStates);
+        for (unsigned vt = kDefaultTileStates + 256; vt <= kMaxDefaultTileStates; vt += 256)
+            if (waves_for(vt) <= w0) Vt = vt;
+    }
     Vt = std::min<unsigned>(Vt, (unsigned)round_up(n, 4));
     const unsigned tiles = ceil_div(n, Vt);
     const size_t fixed = (size_t)kStages * Vt * 4 + 16 + kBarrierBytes;
-    const size_t reserve = 1024;  // static shared memory of the residual reduction, with room to spare
     if ((size_t)optin < fixed + reserve + (size_t)m * 4) return NOVA_SUCCESS;
     const unsigned rowsMax = (unsigned)std::min<size_t>(((size_t)optin - fixed - reserve) / 4, kMaxRows);
     const unsigned SbMax = rowsMax / m;
