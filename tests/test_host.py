@@ -130,6 +130,13 @@ def test_execute_validation_before_any_device_work():
     assert L.pomdp_perseus_execute_cpu(p, ct.byref(per), pol) == INVALID_DATA
     assert L.pomdp_pbvi_update_gpu(p, ct.byref(alg)) == INVALID_DATA
     assert L.mdp_vi_execute_gpu(None, None, None) == INVALID_DATA
+    # solver settings reject a null or uninitialized solver and unknown modes
+    # before any device work
+    assert L.pomdp_pbvi_set_table_gpu(None, npp.TABLE_NEVER) == INVALID_DATA
+    assert L.pomdp_pbvi_set_table_gpu(ct.byref(alg), npp.TABLE_NEVER) == INVALID_DATA
+    assert L.pomdp_pbvi_set_table_gpu(ct.byref(alg), 7) == INVALID_DATA
+    assert L.pomdp_pbvi_set_scoring_gpu(ct.byref(alg), npp.SCORING_FP16) == INVALID_DATA
+    assert L.pomdp_pbvi_set_scoring_gpu(ct.byref(alg), 9) == INVALID_DATA
 
 
 def test_fault_injection_hook_is_wired():
