@@ -1,5 +1,7 @@
 """MDP model object (python/nova/mdp.py:40-305), without the file loader and
-the legacy `solve` (use MDPValueIterationCPU / MDPValueIterationGPU)."""
+the legacy `solve` (use MDPValueIterationCPU / MDPValueIterationGPU; the
+reference's `solve` calls mdp_vi_complete_* functions that its own library
+does not export, and time.clock, which Python 3.8 removed)."""
 import ctypes as ct
 
 import numpy as np
@@ -36,6 +38,19 @@ class MDP(nm.NovaMDP):
     def __del__(self):
         self.uninitialize_gpu()
         self.uninitialize()
+
+    def __str__(self):
+        """ The model's sizes and host arrays as text (arrays shown once allocated). """
+        def arr(ptr, count, shape):
+            return str(np.array([ptr[i] for i in range(count)]).reshape(shape)) if ptr else "(none)"
+        n, m, ns = int(self.n), int(self.m), int(self.ns)
+        goals = [int(self.goals[i]) for i in range(int(self.ng))] if self.goals else []
+        result = "n:       %d\nm:       %d\nns:      %d\ns0:      %d\ngoals:   %s\nhorizon: %d\ngamma:   %s\n\n" % (
+            n, m, ns, int(self.s0), str(goals), int(self.horizon), str(self.gamma))
+        result += "S(s, a, s'):\n%s\n\n" % arr(self.S, n * m * ns, (n, m, ns))
+        result += "T(s, a, s'):\n%s\n\n" % arr(self.T, n * m * ns, (n, m, ns))
+        result += "R(s, a):\n%s\n\n" % arr(self.R, n * m, (n, m))
+        return result
 
     def initialize(self, n, ns, m, gamma, horizon, epsilon, s0, ng):
         """ Allocate the MDP's arrays (mdp_initialize_cpu). """

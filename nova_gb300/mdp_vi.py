@@ -21,6 +21,11 @@ def _initial_v(m, Vinitial):
     return buf
 
 
+def _show(ptr, count):
+    """ A host array as text, or '(none)' while it is not allocated. """
+    return str(np.array([ptr[i] for i in range(count)])) if ptr else "(none)"
+
+
 class MDPValueIterationCPU(nmvi.NovaMDPValueIterationCPU):
     """ Value iteration (host buffers). """
 
@@ -43,6 +48,12 @@ class MDPValueIterationCPU(nmvi.NovaMDPValueIterationCPU):
         if result != 0:
             print("Failed to free the value iteration (CPU) algorithm.")
             raise Exception()
+
+    def __str__(self):
+        n = int(self.mdp.n)
+        return "Vinitial:\n%s\n\ncurrentHorizon: %d\n\nV:\n%s\n\nVprime:\n%s\n\npi:\n%s\n\n" % (
+            _show(self.Vinitial, n), int(self.currentHorizon), _show(self.V, n), _show(self.Vprime, n),
+            _show(self.pi, n))
 
     def solve(self):
         policy = mvf.MDPValueFunction()
@@ -76,6 +87,10 @@ class MDPValueIterationGPU(nmvi.NovaMDPValueIterationGPU):
         if result != 0:
             print("Failed to free the value iteration (GPU) algorithm.")
             raise Exception()
+
+    def __str__(self):
+        return "Vinitial:\n%s\n\ncurrentHorizon: %d\n\nnumThreads: %d\n\n" % (
+            _show(self.Vinitial, int(self.mdp.n)), int(self.currentHorizon), int(self.numThreads))
 
     def solve(self):
         policy = mvf.MDPValueFunction()

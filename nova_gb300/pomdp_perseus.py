@@ -1,10 +1,20 @@
 """Perseus solver objects (python/nova/pomdp_perseus.py:38-142), plus POMDPPerseusGPU."""
 import ctypes as ct
 
+import numpy as np
+
 from . import pomdp
 from . import pomdp_alpha_vectors as pav
 from . import nova_pomdp_perseus as npper
 from .pomdp_pbvi import _initial_gamma
+
+
+def _perseus_text(alg, extra):
+    """ The solver's initial alphas (an r x n array once set) and counters as text. """
+    r, n = int(alg.pomdp.r), int(alg.pomdp.n)
+    g0 = str(np.array([alg.GammaInitial[i] for i in range(r * n)]).reshape((r, n))) if alg.GammaInitial else "(none)"
+    return "GammaInitial:\n%s\n\ncurrentHorizon: %d\n\n%srGamma: %d\n\nrGammaPrime: %d\n\nrTilde: %d\n\n" % (
+        g0, int(alg.currentHorizon), extra, int(alg.rGamma), int(alg.rGammaPrime), int(alg.rTilde))
 
 
 class POMDPPerseusCPU(npper.NovaPOMDPPerseusCPU):
@@ -34,6 +44,9 @@ class POMDPPerseusCPU(npper.NovaPOMDPPerseusCPU):
         if result != 0:
             print("Failed to free the Perseus (CPU) algorithm.")
             raise Exception()
+
+    def __str__(self):
+        return _perseus_text(self, "")
 
     def solve(self):
         policy = pav.POMDPAlphaVectors()
@@ -72,6 +85,9 @@ class POMDPPerseusGPU(npper.NovaPOMDPPerseusGPU):
         if result != 0:
             print("Failed to free the Perseus (GPU) algorithm.")
             raise Exception()
+
+    def __str__(self):
+        return _perseus_text(self, "numThreads: %d\n\n" % int(self.numThreads))
 
     def solve(self):
         policy = pav.POMDPAlphaVectors()

@@ -289,3 +289,48 @@ def test_cassandra_loader_on_reference_domains(name):
     g = dict(n=L.n, ns=L.ns, m=L.m, z=L.z, r=L.r, rz=L.rz, horizon=L.horizon, gamma=L.gamma, S=L.S, T=L.T, O=L.O,
              R=L.R, Z=L.Z, B=L.B, Rmin=L.Rmin, Rmax=L.Rmax)
     _check_cassandra(p, g)
+
+
+def test_text_forms_of_models_and_solvers():
+    """__str__ of the MDP and of the VI and Perseus solver objects, as the
+    reference's wrapper offers, built without device work (the solver objects
+    are made with their fields set directly)."""
+    from nova_gb300 import synth
+    from nova_gb300.mdp import MDP
+    from nova_gb300.mdp_vi import MDPValueIterationCPU, MDPValueIterationGPU
+    from nova_gb300.pomdp_perseus import POMDPPerseusCPU, POMDPPerseusGPU
+    md = synth.random_mdp(n=3, m=2, ns=2, gamma=0.9, horizon=4, seed=3)
+    m = MDP.from_arrays(md)
+    text = str(m)
+    assert "n:       3" in text and "horizon: 4" in text and "S(s, a, s'):" in text and "R(s, a):" in text
+    V0 = (ct.c_float * 3)(1.0, 2.0, 3.0)
+    def bare(cls):
+        # An instance without __init__ (no device work) and nothing to free.
+        sub = type("Bare" + cls.__name__, (cls,), {"__del__": lambda self: None})
+        return sub.__new__(sub)
+
+    for cls in (MDPValueIterationCPU, MDPValueIterationGPU):
+        vi = bare(cls)
+        vi.mdp = m
+        vi.Vinitial = ct.cast(V0, ct.POINTER(ct.c_float))
+        vi.currentHorizon = 2
+        if issubclass(type(vi), MDPValueIterationCPU):
+            vi.V, vi.Vprime, vi.pi = ct.POINTER(ct.c_float)(), ct.POINTER(ct.c_float)(), ct.POINTER(ct.c_uint)()
+            t = str(vi)
+            assert "currentHorizon: 2" in t and "[1. 2. 3.]" in t and "V:\n(none)" in t
+        else:
+            vi.numThreads = 64
+            t = str(vi)
+            assert "numThreads: 64" in t and "[1. 2. 3.]" in t
+    pm = synth.random_pomdp(n=2, m=2, z=2, ns=2, r=2, rz=2, gamma=0.9, horizon=2, seed=3)
+    p = POMDP.from_arrays(pm)
+    G0 = (ct.c_float * 4)(1.0, 2.0, 3.0, 4.0)
+    for cls in (POMDPPerseusCPU, POMDPPerseusGPU):
+        per = bare(cls)
+        per.pomdp = p
+        per.GammaInitial = ct.cast(G0, ct.POINTER(ct.c_float))
+        per.currentHorizon, per.rGamma, per.rGammaPrime, per.rTilde = 1, 2, 0, 2
+        per.numThreads = 32
+        t = str(per)
+        assert "rGamma: 2" in t and "rTilde: 2" in t and "[[1. 2.]\n [3. 4.]]" in t
+        assert ("numThreads: 32" in t) == issubclass(type(per), POMDPPerseusGPU)
